@@ -1,0 +1,457 @@
+"""Benchmark of the channel-flow hot path on one GB300 (or N replicas).
+
+Workload (the reference's metric is quoted on it: 128^3 plain FP64):
+a 128 x 128 x 128 channel, 2*pi*h x 2h x pi*h, tanh wall stretching
+(gamma 2.0), seeded laminar-plus-noise state at Mach 0.5.  One step is one
+right-hand-side evaluation of the reference's per-step sequence: x halo,
+wall and periodic ghosts, Filter (ADM sensor), Flux_X/Y/Z_limiter and
+Viscous_terms, all FP64.  ``value`` = cells x steps / time (Mcell-updates/s
+per RHS) with every input resident in HBM; ``e2e`` = the same through the
+C-ABI on registered HOST arrays, with the state uploaded and the face fluxes
+and viscous terms (the RHS) downloaded every step.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gb300|reference]
+
+``--impl reference`` times the CPU implementation of the same steps (the C
+restatement of the reference routines in oracle/, OpenMP on all host
+cores), on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+GRID = (128, 128, 128)
+GAMMA = 2.0
+SEED = 2800
+FILTER_ARGS = (0.007, 1.0, 0.0)        # Roe_criterion, E_high, E_low (main.cpp:55-57)
+# algorithmic bytes per cell of each routine, FP64: arrays of the routine's
+# signature read and written once (Filter 7+3, limited fluxes 16/17 + 5,
+# viscous 36 + 4 arrays of 8 bytes)
+ALG_BYTES = {"Filter": 80, "Flux_X_limiter": 168, "Flux_Y_limiter": 176, "Flux_Z_limiter": 176,
+             "Viscous_terms": 320}
+L2_BYTES = 129 * 2 ** 20
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+# workload
+
+def make_host_workload(g):
+    """numpy arrays of the benchmark channel (host, set-up only)."""
+    from channel_flow_gb300 import synthetic as syn
+    cm = syn.flat_metrics(g, GAMMA, "cell")
+    J = cm["J"]
+    U = syn.channel_state(g, J, seed=SEED, mach=0.5, noise=0.05, jitter=0.01, gamma=GAMMA)
+    Yp = syn.y_points(g, gamma=GAMMA)
+    return {"U": U, "J": J, "cm": [cm[n] for n in syn.METRIC_NAMES], "Yp": Yp}
+
+
+class DeviceWorkload:
+    def __init__(self, ctx, g, host, torch):
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        z = lambda: torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+        self.U = [dev(a) for a in host["U"]]
+        self.J = dev(host["J"])
+        self.cm = [dev(a) for a in host["cm"]]
+        self.Yp = dev(host["Yp"])
+        # face metrics from the GPU Jacobian_u/v/w routines (flat walls)
+        self.fu = [z() for _ in range(10)]
+        self.fv = [z() for _ in range(10)]
+        self.fw = [z() for _ in range(10)]
+        ctx.Jacobian_u(*self.fu)
+        ctx.Jacobian_v(*self.fv, self.J, *self.cm)
+        ctx.Jacobian_w(*self.fw)
+        self.Ep = [z() for _ in range(3)]
+        self.Fx = [z() for _ in range(5)]
+        self.Fy = [z() for _ in range(5)]
+        self.Fz = [z() for _ in range(5)]
+        self.vF = [z() for _ in range(4)]
+        self.LL = [z() for _ in range(4)]
+        self.ML = [z() for _ in range(4)]
+        self.NL = [z() for _ in range(4)]
+        torch.cuda.synchronize()
+
+    def outputs(self):
+        return self.Fx + self.Fy + self.Fz + self.vF
+
+
+def rhs_calls(ctx, w, ptr):
+    """The per-step routine calls as (name, function, args) with the
+    pointer arguments resolved once; `ptr` maps a field to what the C-ABI
+    gets (a device pointer, or a registered host array's address)."""
+    lib, h = ctx.lib, ctx.h
+    U = [ptr(x) for x in w.U]
+    J = ptr(w.J)
+    cm = [ptr(x) for x in w.cm]
+    fu, fv, fw = ([ptr(x) for x in s] for s in (w.fu, w.fv, w.fw))
+    Ep = [ptr(x) for x in w.Ep]
+    F = {"x": [ptr(x) for x in w.Fx], "y": [ptr(x) for x in w.Fy], "z": [ptr(x) for x in w.Fz]}
+    vF = [ptr(x) for x in w.vF]
+    none10 = [None] * 10
+    from channel_flow_gb300 import _lib
+    visc = U + vF + [J] + cm + fu + fv + fw + [None] * 6 + [ptr(x) for x in w.LL] + [None] * 6 + \
+        [ptr(x) for x in w.ML] + [None] * 6 + [ptr(x) for x in w.NL]
+    visc_arr = _lib.ptr_array(visc)
+    calls = [
+        ("X_periodic", lib.cf_X_periodic, (h, 0, *U)),
+        ("Y_boundary_condition", lib.cf_Y_boundary_condition, (h, 0, *U, J)),
+        ("Z_boundary_condition", lib.cf_Z_boundary_condition, (h, 0, *U, J)),
+        ("Filter", lib.cf_Filter, (h, 0, *FILTER_ARGS, *U, ptr(w.Yp), *Ep, J)),
+        ("Flux_X_limiter", lib.cf_Flux_X_limiter, (h, 0, *U, *none10, J, *fu, *F["x"], Ep[0])),
+        ("Flux_Y_limiter", lib.cf_Flux_Y_limiter, (h, 0, *U, *none10, J, *fv, *F["y"], Ep[1])),
+        ("Flux_Z_limiter", lib.cf_Flux_Z_limiter, (h, 0, *U, *none10, J, *fw, *F["z"], Ep[2])),
+        ("Viscous_terms", lib.cf_Viscous_terms, (h, 0, visc_arr)),
+    ]
+    return calls
+
+
+# kernels launched per step: x halo 1, y wall 1, z periodic 1, Filter
+# (1 shell + 2 x 6 x 3 passes + 2 energy + 3 ghost fills + 3 thresholds = 45),
+# 3 flux kernels, viscous 3
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 45 + 3 + 3
+
+
+def run_calls(ctx, calls):
+    from channel_flow_gb300 import _lib
+    for name, fn, args in calls:
+        rc = fn(*args)
+        if rc:
+            _lib.check(ctx.lib, ctx.h, rc)
+
+
+# --------------------------------------------------------------------------
+# clocks
+
+class ClockSampler:
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        busy = [s for s in sm if smax and s > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU arm (C restatement of the reference routines)
+
+def cpu_rhs_port(g, host, faces):
+    """One RHS on the host cores with the C oracle (same routine sequence)."""
+    from oracle.cforacle import Port
+    port = Port()
+    U = [a.copy() for a in host["U"]]
+    J, cm, Yp = host["J"], host["cm"], host["Yp"]
+    z = lambda: np.zeros(g.shape)
+    Ep = [z() for _ in range(3)]
+    F = [[z() for _ in range(5)] for _ in range(3)]
+    scratch = [z() for _ in range(10)]
+    vF = [z() for _ in range(4)]
+    vs = [z() for _ in range(30)]
+
+    def step():
+        port.x_periodic(g, U)
+        port.Y_boundary_condition(g, U + [J])
+        port.Z_boundary_condition(g, U + [J])
+        port.Filter(g, *FILTER_ARGS, U + [Yp] + Ep + [J])
+        for d, name in enumerate(("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter")):
+            port.flux(name, g, U + scratch + [J] + faces[d] + F[d] + [Ep[d]])
+        port.Viscous_terms(g, U + vF + [J] + cm + faces[0] + faces[1] + faces[2] + vs)
+    return step
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def host_faces(g, host):
+    """face metrics on the host (C oracle of Jacobian_u/v/w, same gamma)"""
+    from oracle.cforacle import Port
+    port = Port()
+    faces = []
+    for w in ("u", "v", "w"):
+        arrs = [np.zeros(g.shape) for _ in range(10)]
+        extra = [host["J"]] + host["cm"] if w == "v" else []
+        port.Jacobian_face(w, g, GAMMA, arrs + extra)
+        faces.append(arrs)
+    return faces
+
+
+def time_cpu(g, host, steps, warmup):
+    faces = host_faces(g, host)
+    step = cpu_rhs_port(g, host, faces)
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = time.perf_counter() - t0
+    return g.cells * steps / dt / 1e6, dt / steps
+
+
+# --------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_exact", "fp32"])
+    ap.add_argument("--grid", default="x".join(map(str, GRID)))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dims = tuple(int(x) for x in args.grid.split("x"))
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from channel_flow_gb300 import synthetic as syn
+    g = syn.channel_grid(*dims)
+    workload = f"rhs_{dims[0]}x{dims[1]}x{dims[2]}_{args.precision}"
+    cfg = {"workload": workload, "grid": list(dims), "cells": g.cells,
+           "domain": "2*pi*h x 2h x pi*h, tanh stretching gamma 2.0, Mach 0.5, laminar + 5% noise",
+           "step": "x halo + wall/periodic ghosts + Filter + Flux_X/Y/Z_limiter + Viscous_terms",
+           "precision": args.precision,
+           "l2": "working set of a step about 1.5 GB (> 129 MB L2); no flush needed"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        host = make_host_workload(g)
+        value, sec = time_cpu(g, host, max(1, args.steps), max(0, min(args.warmup, 1)))
+        cores = cpu_threads()
+        sample = f"{args.steps} RHS evaluations of the {dims[0]}x{dims[1]}x{dims[2]} workload (C restatement, OpenMP)"
+        line = {"impl": "reference", "metric": "Mcell-updates/s per RHS", "value": value,
+                "unit": "Mcell-updates/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import channel_flow_gb300 as cf
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    host = make_host_workload(g)
+    ctx = cf.Context(g, precision=args.precision, gamma=GAMMA)
+    w = DeviceWorkload(ctx, g, host, torch)
+    calls = rhs_calls(ctx, w, lambda x: x.data_ptr())
+    stream = torch.cuda.current_stream()
+
+    # warm-up (allocates the scratch on the first call)
+    for _ in range(max(args.warmup, 3)):
+        run_calls(ctx, calls)
+    torch.cuda.synchronize()
+
+    # timed region: K steps, events around every routine for the roofline
+    names = [c[0] for c in calls]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for s in range(args.steps):
+            for n, (name, fn, a) in enumerate(calls):
+                ev[s][n].record(stream)
+                rc = fn(*a)
+                if rc:
+                    cf._lib.check(ctx.lib, ctx.h, rc)
+            ev[s][len(calls)].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    total_ms = t_start.elapsed_time(t_end)
+    if dist:
+        t = torch.tensor([total_ms])
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    per_routine = {nm: 0.0 for nm in names}
+    for s in range(args.steps):
+        for n, nm in enumerate(names):
+            per_routine[nm] += ev[s][n].elapsed_time(ev[s][n + 1]) / args.steps
+    ms_per_step = total_ms / args.steps
+    value = g.cells * args.steps * world / (total_ms * 1e-3) / 1e6
+
+    # roofline of the dominant routine with a byte model
+    hbm, peak_kind = peaks()
+    dom = max((nm for nm in names if nm in ALG_BYTES), key=lambda nm: per_routine[nm])
+    achieved = ALG_BYTES[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_kind": peak_kind,
+            "alg_bytes_per_cell": ALG_BYTES[dom], "traffic": None,
+            "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
+            "note": "FP64 on GB300 is DP-pipe bound; the HBM fraction is the byte-model figure"}
+
+    # e2e through the C-ABI with registered host arrays
+    e2e = None
+    try:
+        e2e = measure_e2e(ctx, g, host, w, torch, args.steps)
+    except Exception as exc:  # reported, not hidden
+        e2e = {"error": str(exc)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            csteps = 2 if g.cells >= 2_000_000 else 4
+            cval, csec = time_cpu(g, host, csteps, 0)
+            cpu = {"value": cval, "unit": "Mcell-updates/s", "cores": cpu_threads(), "kind": "port",
+                   "sample": f"{csteps} RHS evaluations of the full workload on the host cores "
+                             f"(C restatement of the reference routines, OpenMP), {csec:.2f} s each"}
+        except Exception as exc:
+            cpu = {"error": str(exc)}
+
+    if rank == 0:
+        line = {"metric": "Mcell-updates/s per RHS", "value": value, "unit": "Mcell-updates/s",
+                "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision != "fp32" else "f32", "data": "synthetic",
+                "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "clocks": clocks.summary(), "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+                "parallelism": "replicas" if world > 1 else "single"}
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def measure_e2e(ctx, g, host, w, torch, steps):
+    """Same steps through the C-ABI with HOST arrays registered as device
+    mirrors: upload the state, run the routines, download the RHS."""
+    n = ctx.field_count
+    pinned = lambda: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy().reshape(g.shape)
+    # host copies of every field the step uses
+    hostU = [pinned() for _ in range(5)]
+    for a, src in zip(hostU, host["U"]):
+        a[...] = src
+    hw = type("H", (), {})()
+    hw.U = hostU
+    statics = {}
+    for name in ("J", "Yp"):
+        statics[name] = pinned()
+    statics["J"][...] = host["J"]
+    statics["Yp"][...] = host["Yp"]
+    hw.J, hw.Yp = statics["J"], statics["Yp"]
+    hw.cm = [pinned() for _ in range(9)]
+    for a, src in zip(hw.cm, host["cm"]):
+        a[...] = src
+    for attr in ("fu", "fv", "fw"):
+        arrs = [pinned() for _ in range(10)]
+        for a, d in zip(arrs, getattr(w, attr)):
+            a[...] = d.cpu().numpy()
+        setattr(hw, attr, arrs)
+    for attr, cnt in (("Ep", 3), ("Fx", 5), ("Fy", 5), ("Fz", 5), ("vF", 4), ("LL", 4), ("ML", 4), ("NL", 4)):
+        setattr(hw, attr, [pinned() for _ in range(cnt)])
+    every = hw.U + [hw.J, hw.Yp] + hw.cm + hw.fu + hw.fv + hw.fw + hw.Ep + hw.Fx + hw.Fy + hw.Fz + hw.vF + \
+        hw.LL + hw.ML + hw.NL
+    for a in every:
+        ctx.register(a)
+    for a in every:
+        if a is not None:
+            ctx.upload(a)       # set-up: static inputs resident on the device
+    ctx.synchronize()
+    calls = rhs_calls(ctx, hw, lambda x: x.ctypes.data)
+    outs = hw.Fx + hw.Fy + hw.Fz + hw.vF
+    for _ in range(2):
+        run_calls(ctx, calls)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for a in hw.U:
+            ctx.upload(a)
+        run_calls(ctx, calls)
+        for a in outs:
+            ctx.download(a)
+    ctx.synchronize()
+    dt = time.perf_counter() - t0
+    for a in every:
+        ctx.lib.cf_unregister(ctx.h, a.ctypes.data)
+    field_bytes = n * 8
+    return {"value": g.cells * steps / dt / 1e6, "unit": "Mcell-updates/s",
+            "h2d_bytes_per_step": 5 * field_bytes, "d2h_bytes_per_step": len(outs) * field_bytes,
+            "ms_per_step": dt / steps * 1e3, "path": "C-ABI, registered host arrays"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

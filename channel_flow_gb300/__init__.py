@@ -1,0 +1,195 @@
+"""GB300-native hot path of the compressible channel-flow solver.
+
+``Context`` mirrors the reference solver's per-step routines
+(ricklee209/Channel_Flow, main.h): each method has the reference routine's
+name and takes the reference's arrays in the reference's order, as CUDA
+float64 tensors of shape (X_out+6, Y_out+4, Z_out+4) or raw device
+pointers.  The work runs in hand-written sm_103a kernels behind the C-ABI of
+``libcfgb300.so``; a missing library is an error, never a CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .synthetic import Grid, channel_grid, reference_grid  # noqa: F401
+
+__all__ = ["Context", "Grid", "channel_grid", "reference_grid", "CFError", "FieldSet"]
+CFError = _lib.CFError
+
+
+def _ptr(x):
+    if isinstance(x, int):
+        return x
+    if x is None:
+        return None
+    import torch
+    if isinstance(x, torch.Tensor):
+        if x.dtype != torch.float64 or not x.is_cuda or not x.is_contiguous():
+            raise ValueError("fields must be contiguous float64 CUDA tensors")
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):          # a registered host array
+        return x.ctypes.data
+    raise TypeError(f"unsupported field argument {type(x)}")
+
+
+class Context:
+    """One device context for one grid (the reference's one MPI rank)."""
+
+    def __init__(self, grid: Grid, precision: str = "fp64", stream=None, gamma: float = 1.5):
+        self.lib = _lib.load()
+        self.grid = grid
+        g = _lib.cf_grid(grid.X_out, grid.Y_out, grid.Z_out, grid.deltaXI, grid.deltaET, grid.deltaZT,
+                         grid.K, grid.R, grid.e, grid.Cv, grid.mu_L, grid.Pr_L, grid.f, grid.high)
+        h = C.c_void_p()
+        rc = self.lib.cf_create(C.byref(g), _lib.PREC[precision], C.byref(h))
+        _lib.check(self.lib, None, rc)
+        self.h = h.value
+        self.precision = precision
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+        self.set_stream(stream)
+        if gamma != 1.5:
+            self._ok(self.lib.cf_set_stretching(self.h, gamma))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc):
+        _lib.check(self.lib, self.h, rc)
+
+    # -- context ---------------------------------------------------------
+    def set_stream(self, stream):
+        self._ok(self.lib.cf_set_stream(self.h, stream if isinstance(stream, int) else int(stream)))
+
+    def set_precision(self, precision: str):
+        self._ok(self.lib.cf_set_precision(self.h, _lib.PREC[precision]))
+        self.precision = precision
+
+    def synchronize(self):
+        self._ok(self.lib.cf_synchronize(self.h))
+
+    def register(self, host: np.ndarray):
+        assert host.dtype == np.float64 and host.flags["C_CONTIGUOUS"] and host.size == self.field_count
+        self._ok(self.lib.cf_register(self.h, host.ctypes.data))
+
+    def upload(self, host: np.ndarray):
+        self._ok(self.lib.cf_upload(self.h, host.ctypes.data))
+
+    def download(self, host: np.ndarray):
+        self._ok(self.lib.cf_download(self.h, host.ctypes.data))
+
+    @property
+    def field_count(self) -> int:
+        return int(self.lib.cf_field_count(self.h))
+
+    def check_finite(self, field):
+        self._ok(self.lib.cf_check_finite(self.h, _ptr(field)))
+
+    # -- boundary conditions (Y_/Z_boundary_condition.cpp, main.cpp:156-244)
+    def Y_boundary_condition(self, U1_, U2_, U3_, U4_, U5_, J, myid=0):
+        self._ok(self.lib.cf_Y_boundary_condition(self.h, myid, *map(_ptr, (U1_, U2_, U3_, U4_, U5_, J))))
+
+    def Z_boundary_condition(self, U1_, U2_, U3_, U4_, U5_, J, myid=0):
+        self._ok(self.lib.cf_Z_boundary_condition(self.h, myid, *map(_ptr, (U1_, U2_, U3_, U4_, U5_, J))))
+
+    def X_periodic(self, U1_, U2_, U3_, U4_, U5_, myid=0):
+        self._ok(self.lib.cf_X_periodic(self.h, myid, *map(_ptr, (U1_, U2_, U3_, U4_, U5_))))
+
+    # -- fluxes: the reference's 32 arrays ---------------------------------
+    def _flux(self, name, arrays, myid):
+        if len(arrays) != 32:
+            raise ValueError(f"{name} takes 32 arrays, got {len(arrays)}")
+        self._ok(getattr(self.lib, "cf_" + name)(self.h, myid, *map(_ptr, arrays)))
+
+    def Flux_X_limiter(self, *arrays, myid=0): self._flux("Flux_X_limiter", arrays, myid)
+    def Flux_Y_limiter(self, *arrays, myid=0): self._flux("Flux_Y_limiter", arrays, myid)
+    def Flux_Z_limiter(self, *arrays, myid=0): self._flux("Flux_Z_limiter", arrays, myid)
+    def Flux_X(self, *arrays, myid=0): self._flux("Flux_X", arrays, myid)
+    def Flux_Y(self, *arrays, myid=0): self._flux("Flux_Y", arrays, myid)
+    def Flux_Z(self, *arrays, myid=0): self._flux("Flux_Z", arrays, myid)
+
+    def flux(self, name, arrays, myid=0):
+        self._flux(name, arrays, myid)
+
+    # -- viscous terms and sensor -----------------------------------------
+    def Viscous_terms(self, *arrays, myid=0):
+        if len(arrays) != 79:
+            raise ValueError("Viscous_terms takes 79 arrays")
+        self._ok(self.lib.cf_Viscous_terms(self.h, myid, _lib.ptr_array([_ptr(a) for a in arrays])))
+
+    def Filter(self, Roe_criterion, E_high, E_low, U1_, U2_, U3_, U4_, U5_, Y_point, EpX, EpY, EpZ, J, myid=0):
+        self._ok(self.lib.cf_Filter(self.h, myid, Roe_criterion, E_high, E_low,
+                                    *map(_ptr, (U1_, U2_, U3_, U4_, U5_, Y_point, EpX, EpY, EpZ, J))))
+
+    # -- time integration --------------------------------------------------
+    def RK3NODT(self, RK, deltaT, *arrays, myid=0):
+        if len(arrays) != 49:
+            raise ValueError("RK3NODT takes 49 arrays")
+        self._ok(self.lib.cf_RK3NODT(self.h, myid, RK, deltaT, None, None, None, None, None,
+                                     _lib.ptr_array([_ptr(a) for a in arrays])))
+
+    def Hyperplane(self):
+        g = self.grid
+        X_np = g.X_out + 6
+        Nijk = np.zeros(((X_np - 3) + g.ny + g.nz + 7, 2), np.int32)
+        ijk = np.zeros(((X_np - 6) * g.Y_out * g.Z_out * 3 + 1, 3), np.int32)
+        self._ok(self.lib.cf_Hyperplane(self.h, 0, Nijk.ctypes.data, ijk.ctypes.data))
+        return Nijk, ijk
+
+    def Dual_time_stepping(self, deltaT, *arrays, Nijk=None, ijk=None, myid=0):
+        if len(arrays) != 64:
+            raise ValueError("Dual_time_stepping takes 64 arrays")
+        er = np.zeros(5)
+        e = [er[n:].ctypes.data for n in range(5)]
+        self._ok(self.lib.cf_Dual_time_stepping(
+            self.h, myid, deltaT, *e, None if Nijk is None else Nijk.ctypes.data,
+            None if ijk is None else ijk.ctypes.data, _lib.ptr_array([_ptr(a) for a in arrays])))
+        return er
+
+    def DPLUSGS(self, deltaT, *arrays, myid=0):
+        if len(arrays) != 64:
+            raise ValueError("DPLUSGS takes 64 arrays")
+        er = np.zeros(5)
+        e = [er[n:].ctypes.data for n in range(5)]
+        self._ok(self.lib.cf_DPLUSGS(self.h, myid, deltaT, *e, _lib.ptr_array([_ptr(a) for a in arrays])))
+        return er
+
+    # -- face metrics ------------------------------------------------------
+    def Jacobian_u(self, *arrays, myid=0):
+        self._ok(self.lib.cf_Jacobian_u(self.h, myid, _lib.ptr_array([_ptr(a) for a in arrays])))
+
+    def Jacobian_v(self, *arrays, myid=0):
+        self._ok(self.lib.cf_Jacobian_v(self.h, myid, _lib.ptr_array([_ptr(a) for a in arrays])))
+
+    def Jacobian_w(self, *arrays, myid=0):
+        self._ok(self.lib.cf_Jacobian_w(self.h, myid, _lib.ptr_array([_ptr(a) for a in arrays])))
+
+
+class FieldSet:
+    """Device fields of one grid, allocated as one (n, X_np, Y_m, Z_m) float64
+    block so that related arrays are adjacent in HBM."""
+
+    def __init__(self, grid: Grid, n: int, device="cuda"):
+        import torch
+        self.block = torch.zeros((n,) + grid.shape, dtype=torch.float64, device=device)
+
+    def __getitem__(self, i):
+        return self.block[i]
+
+    def __len__(self):
+        return self.block.shape[0]
+
+    def list(self):
+        return [self.block[i] for i in range(self.block.shape[0])]

@@ -1,0 +1,98 @@
+"""ctypes binding of libcfgb300.so (the C-ABI in include/channel_flow_gb300.h).
+
+The library is built in-tree by ``channel_flow_gb300.build``.  Loading fails
+loudly when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libcfgb300.so"
+
+CF_OK, CF_ERR_ARG, CF_ERR_CUDA, CF_ERR_NONFINITE, CF_ERR_NOMEM, CF_ERR_STATE = range(6)
+PREC = {"fp64_exact": 0, "fp64": 1, "fp32": 2}
+
+
+class cf_grid(C.Structure):
+    _fields_ = [("X_out", C.c_int), ("Y_out", C.c_int), ("Z_out", C.c_int),
+                ("deltaXI", C.c_double), ("deltaET", C.c_double), ("deltaZT", C.c_double),
+                ("K", C.c_double), ("R", C.c_double), ("e", C.c_double),
+                ("Cv", C.c_double), ("mu_L", C.c_double), ("Pr_L", C.c_double),
+                ("f", C.c_double), ("high", C.c_double)]
+
+
+class CFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+_lock = threading.Lock()
+
+P = C.c_void_p
+_SIGS = {
+    "cf_library_version": ([], C.c_int),
+    "cf_error_string": ([C.c_int], C.c_char_p),
+    "cf_last_error": ([P], C.c_char_p),
+    "cf_grid_reference": ([C.POINTER(cf_grid), C.c_int, C.c_int, C.c_int], C.c_int),
+    "cf_create": ([C.POINTER(cf_grid), C.c_int, C.POINTER(P)], C.c_int),
+    "cf_destroy": ([P], None),
+    "cf_set_precision": ([P, C.c_int], C.c_int),
+    "cf_set_stream": ([P, P], C.c_int),
+    "cf_set_stretching": ([P, C.c_double], C.c_int),
+    "cf_synchronize": ([P], C.c_int),
+    "cf_field_count": ([P], C.c_size_t),
+    "cf_register": ([P, P], C.c_int),
+    "cf_unregister": ([P, P], C.c_int),
+    "cf_upload": ([P, P], C.c_int),
+    "cf_download": ([P, P], C.c_int),
+    "cf_device_ptr": ([P, P], P),
+    "cf_check_finite": ([P, P], C.c_int),
+    "cf_Y_boundary_condition": ([P, C.c_int] + [P] * 6, C.c_int),
+    "cf_Z_boundary_condition": ([P, C.c_int] + [P] * 6, C.c_int),
+    "cf_X_periodic": ([P, C.c_int] + [P] * 5, C.c_int),
+    "cf_Viscous_terms": ([P, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_Filter": ([P, C.c_int, C.c_double, C.c_double, C.c_double] + [P] * 10, C.c_int),
+    "cf_RK3NODT": ([P, C.c_int, C.c_int, C.c_double] + [P] * 5 + [C.POINTER(P)], C.c_int),
+    "cf_Hyperplane": ([P, C.c_int, P, P], C.c_int),
+    "cf_Dual_time_stepping": ([P, C.c_int, C.c_double] + [P] * 5 + [P, P, C.POINTER(P)], C.c_int),
+    "cf_DPLUSGS": ([P, C.c_int, C.c_double] + [P] * 5 + [C.POINTER(P)], C.c_int),
+    "cf_Jacobian_u": ([P, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_Jacobian_v": ([P, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_Jacobian_w": ([P, C.c_int, C.POINTER(P)], C.c_int),
+}
+for _n in ("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter", "Flux_X", "Flux_Y", "Flux_Z"):
+    _SIGS["cf_" + _n] = ([P, C.c_int] + [P] * 32, C.c_int)
+
+EXPORTED = sorted(_SIGS)
+
+
+def load():
+    """Load (not build) the library; raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with `python -m channel_flow_gb300.build` "
+                    "(the channel-flow kernels have no CPU fallback)")
+            lib = C.CDLL(str(LIB_PATH))
+            for name, (args, res) in _SIGS.items():
+                fn = getattr(lib, name)
+                fn.argtypes = args
+                fn.restype = res
+            _lib = lib
+    return _lib
+
+
+def check(lib, ctx, rc):
+    if rc != CF_OK:
+        msg = lib.cf_last_error(ctx).decode() if ctx else lib.cf_error_string(rc).decode()
+        raise CFError(rc, msg or lib.cf_error_string(rc).decode())
+
+
+def ptr_array(ptrs):
+    return (P * len(ptrs))(*ptrs)

@@ -1,0 +1,96 @@
+"""Build the CUDA library ``channel_flow_gb300/libcfgb300.so`` (sm_103a).
+
+Three translation units, compiled in parallel with nvcc:
+
+* ``cf_variant.cu`` as namespace ``cf_exact`` with ``--fmad=false``: the FP64
+  kernels without fused multiply-add, whose results equal the reference's
+  bit for bit;
+* ``cf_variant.cu`` as namespace ``cf_fast`` with contraction on and the FP32
+  instantiations;
+* ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h).
+
+Usage: ``python -m channel_flow_gb300.build [--verbose] [--ptxas]``
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+LIB = PKG / "libcfgb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and Path(c).exists():
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def sources():
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + \
+        [PKG.parent / "include" / "channel_flow_gb300.h"]
+
+
+def up_to_date() -> bool:
+    if not LIB.exists():
+        return False
+    t = LIB.stat().st_mtime
+    return all(s.stat().st_mtime <= t for s in sources())
+
+
+def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Path:
+    if not force and up_to_date():
+        return LIB
+    out = PKG / "_build"
+    out.mkdir(exist_ok=True)
+    base = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            "--expt-relaxed-constexpr", f"-I{CSRC}"]
+    if ptxas:
+        base += ["-Xptxas", "-v"]
+    units = [
+        ("cf_variant.cu", "cf_exact.o", ["-DCF_NS=cf_exact", "--fmad=false"]),
+        ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "--fmad=true"]),
+        ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
+    ]
+
+    def cc(u):
+        src, obj, extra = u
+        cmd = base + extra + ["-c", str(CSRC / src), "-o", str(out / obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed ({src} {' '.join(extra)}):\n{r.stderr[-6000:]}")
+        return r.stderr
+
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        logs = list(ex.map(cc, units))
+    if verbose or ptxas:
+        for log in logs:
+            sys.stderr.write(log)
+    tmp = PKG / f"libcfgb300.{os.getpid()}.tmp"
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp)] + [str(out / u[1]) for u in units] + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="build libcfgb300.so for sm_103a")
+    ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--ptxas", action="store_true", help="print register/spill usage (-Xptxas -v)")
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args(argv)
+    print(build(a.verbose, a.ptxas, a.force))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,607 @@
+// C-ABI of the GB300 channel-flow hot path: context, device mirrors of host
+// arrays, argument resolution and one entry point per reference routine
+// (declarations and contracts: include/channel_flow_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/channel_flow_gb300.h"
+#include "cf_launch.h"
+
+#define CF_VERSION 100
+
+struct cf_ctx {
+    cf_dims d;
+    int prec = CF_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    double gamma = 1.5;
+    std::unordered_map<const double *, double *> mirrors;
+    std::unordered_map<std::string, std::pair<double *, size_t>> scratch;
+    std::vector<int> nijk;            // plane tables, Hyperplane layout (host)
+    std::vector<int> ijk;
+    int *ijk_dev = nullptr;
+    bool tables_checked = false;
+    double *er_dev = nullptr;         // 5 doubles + device counter space
+    double *er_host = nullptr;        // pinned
+    std::string err;
+};
+
+namespace {
+
+int fail(cf_ctx *c, int code, const char *fmt, ...)
+{
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_check(cf_ctx *c, cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return CF_OK;
+    return fail(c, CF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// field pointer of an argument: the device mirror of a registered host
+// array, or the pointer itself (a device pointer)
+inline double *R(cf_ctx *c, const double *p)
+{
+    auto it = c->mirrors.find(p);
+    return it == c->mirrors.end() ? const_cast<double *>(p) : it->second;
+}
+
+int check_ptrs(cf_ctx *c, const double *const *p, int n, const char *who)
+{
+    for (int i = 0; i < n; i++)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "%s: array argument %d is NULL", who, i);
+    return CF_OK;
+}
+
+// scratch of nfields fields, owned by the context (allocated on first use)
+double *scratch(cf_ctx *c, const char *key, int nfields)
+{
+    const size_t bytes = (size_t)nfields * c->d.total() * sizeof(double);
+    auto &e = c->scratch[key];
+    if (e.first && e.second >= bytes) return e.first;
+    if (e.first) cudaFree(e.first);
+    e.first = nullptr;
+    e.second = 0;
+    if (cudaMalloc(&e.first, bytes) != cudaSuccess) {
+        e.first = nullptr;
+        return nullptr;
+    }
+    e.second = bytes;
+    return e.first;
+}
+
+// cells of plane m = i+j+k in i-major order, exactly the tables of
+// Hyperplane.cpp:50-78 (ijk 1-based, Nijk[m] = {last index, count})
+void build_tables(cf_ctx *c)
+{
+    const cf_dims &d = c->d;
+    const int nplanes = (d.X_out + 3) + d.ny + d.nz + 7;
+    c->nijk.assign((size_t)nplanes * 2, 0);
+    c->ijk.assign(((size_t)d.X_out * d.Y_out * d.Z_out * 3 + 1) * 3, 0);
+    int ii = 0;
+    for (int m = 7; m <= d.gend + d.ny + d.nz; m++) {
+        int mi = 0;
+        for (int i = 3; i <= d.gend; i++)
+            for (int j = 2; j <= d.ny; j++) {
+                const int k = m - i - j;
+                if (k >= 2 && k <= d.nz) {
+                    mi++;
+                    ii++;
+                    c->ijk[3 * (size_t)ii] = i;
+                    c->ijk[3 * (size_t)ii + 1] = j;
+                    c->ijk[3 * (size_t)ii + 2] = k;
+                }
+            }
+        c->nijk[2 * (size_t)m] = ii;
+        c->nijk[2 * (size_t)m + 1] = mi;
+    }
+}
+
+__global__ void k_count_nonfinite(cf_dims d, const double *f, unsigned long long *bad)
+{
+    const int k = 2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 2 + (int)blockIdx.y;
+    const int i = 3 + (int)blockIdx.z;
+    if (k > d.nz) return;
+    const double v = f[d.ix(i, j, k)];
+    if (!isfinite(v)) atomicAdd(bad, 1ull);
+}
+
+inline bool exact(const cf_ctx *c) { return c->prec == CF_PREC_FP64_EXACT; }
+inline int kprec(const cf_ctx *c) { return c->prec == CF_PREC_FP32 ? 1 : 0; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int cf_library_version(void) { return CF_VERSION; }
+
+const char *cf_error_string(int code)
+{
+    switch (code) {
+    case CF_OK: return "ok";
+    case CF_ERR_ARG: return "invalid argument";
+    case CF_ERR_CUDA: return "CUDA error";
+    case CF_ERR_NONFINITE: return "non-finite value";
+    case CF_ERR_NOMEM: return "device allocation failed";
+    case CF_ERR_STATE: return "call out of order";
+    default: return "unknown error";
+    }
+}
+
+const char *cf_last_error(const cf_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int cf_grid_reference(cf_grid *g, int X_out, int Y_out, int Z_out)
+{
+    if (!g) return CF_ERR_ARG;
+    const double h = 0.5 * 0.005;
+    const double pi = 3.14159265358979323846;
+    g->X_out = X_out; g->Y_out = Y_out; g->Z_out = Z_out;
+    g->deltaXI = 4 * pi * h / X_out;
+    g->deltaET = 1.0 / Y_out;
+    g->deltaZT = 2 * pi * h / Z_out;
+    g->K = 1.4; g->R = 287; g->e = 0.0001;
+    g->Cv = 717.5; g->mu_L = 0.0000185; g->Pr_L = 0.72;
+    g->f = 599.29876710; g->high = 0.005;
+    return CF_OK;
+}
+
+int cf_create(const cf_grid *g, int precision, cf_ctx **out)
+{
+    if (!g || !out) return CF_ERR_ARG;
+    *out = nullptr;
+    if (g->X_out < 6 || g->Y_out < 6 || g->Z_out < 6) return CF_ERR_ARG;
+    if (precision < CF_PREC_FP64_EXACT || precision > CF_PREC_FP32) return CF_ERR_ARG;
+    cf_ctx *c = new cf_ctx();
+    cf_dims &d = c->d;
+    d.X_out = g->X_out; d.Y_out = g->Y_out; d.Z_out = g->Z_out;
+    d.Ym = g->Y_out + 4; d.Zm = g->Z_out + 4;
+    d.gend = g->X_out + 2; d.ny = g->Y_out + 1; d.nz = g->Z_out + 1;
+    d.dXI = g->deltaXI; d.dET = g->deltaET; d.dZT = g->deltaZT;
+    d.K = g->K; d.R = g->R; d.e = g->e; d.Cv = g->Cv; d.mu_L = g->mu_L; d.Pr_L = g->Pr_L;
+    d.f = g->f; d.high = g->high;
+    c->prec = precision;
+    build_tables(c);
+    cudaError_t e = cudaMalloc(&c->ijk_dev, c->ijk.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(c->ijk_dev, c->ijk.data(), c->ijk.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&c->er_dev, 16 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->er_host, 16 * sizeof(double));
+    if (e != cudaSuccess) {
+        cf_destroy(c);
+        return CF_ERR_CUDA;
+    }
+    *out = c;
+    return CF_OK;
+}
+
+void cf_destroy(cf_ctx *c)
+{
+    if (!c) return;
+    for (auto &m : c->mirrors) cudaFree(m.second);
+    for (auto &s : c->scratch) cudaFree(s.second.first);
+    if (c->ijk_dev) cudaFree(c->ijk_dev);
+    if (c->er_dev) cudaFree(c->er_dev);
+    if (c->er_host) cudaFreeHost(c->er_host);
+    delete c;
+}
+
+int cf_set_precision(cf_ctx *c, int precision)
+{
+    if (!c || precision < CF_PREC_FP64_EXACT || precision > CF_PREC_FP32) return CF_ERR_ARG;
+    c->prec = precision;
+    return CF_OK;
+}
+
+int cf_set_stream(cf_ctx *c, void *stream)
+{
+    if (!c) return CF_ERR_ARG;
+    c->stream = (cudaStream_t)stream;
+    return CF_OK;
+}
+
+int cf_set_stretching(cf_ctx *c, double gamma)
+{
+    if (!c || !(gamma > 0)) return CF_ERR_ARG;
+    c->gamma = gamma;
+    return CF_OK;
+}
+
+int cf_synchronize(cf_ctx *c)
+{
+    if (!c) return CF_ERR_ARG;
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+
+size_t cf_field_count(const cf_ctx *c) { return c ? c->d.total() : 0; }
+
+int cf_register(cf_ctx *c, double *host)
+{
+    if (!c || !host) return CF_ERR_ARG;
+    if (c->mirrors.count(host)) return CF_OK;
+    double *dev = nullptr;
+    if (cudaMalloc(&dev, c->d.total() * sizeof(double)) != cudaSuccess)
+        return fail(c, CF_ERR_NOMEM, "cf_register: cudaMalloc of %zu doubles failed", c->d.total());
+    c->mirrors[host] = dev;
+    return CF_OK;
+}
+
+int cf_unregister(cf_ctx *c, double *host)
+{
+    if (!c) return CF_ERR_ARG;
+    auto it = c->mirrors.find(host);
+    if (it == c->mirrors.end()) return fail(c, CF_ERR_ARG, "cf_unregister: pointer not registered");
+    cudaFree(it->second);
+    c->mirrors.erase(it);
+    return CF_OK;
+}
+
+int cf_upload(cf_ctx *c, const double *host)
+{
+    if (!c) return CF_ERR_ARG;
+    auto it = c->mirrors.find(host);
+    if (it == c->mirrors.end()) return fail(c, CF_ERR_ARG, "cf_upload: pointer not registered");
+    return cuda_check(c, cudaMemcpyAsync(it->second, host, c->d.total() * sizeof(double), cudaMemcpyHostToDevice,
+                                         c->stream), "cf_upload");
+}
+
+int cf_download(cf_ctx *c, double *host)
+{
+    if (!c) return CF_ERR_ARG;
+    auto it = c->mirrors.find(host);
+    if (it == c->mirrors.end()) return fail(c, CF_ERR_ARG, "cf_download: pointer not registered");
+    int rc = cuda_check(c, cudaMemcpyAsync(host, it->second, c->d.total() * sizeof(double), cudaMemcpyDeviceToHost,
+                                           c->stream), "cf_download");
+    if (rc) return rc;
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "cf_download sync");
+}
+
+double *cf_device_ptr(cf_ctx *c, const double *p) { return c ? R(c, p) : nullptr; }
+
+int cf_check_finite(cf_ctx *c, const double *field)
+{
+    if (!c || !field) return CF_ERR_ARG;
+    const cf_dims &d = c->d;
+    unsigned long long *bad = reinterpret_cast<unsigned long long *>(c->er_dev + 8);
+    cudaMemsetAsync(bad, 0, sizeof *bad, c->stream);
+    dim3 g((unsigned)((d.Z_out + 127) / 128), (unsigned)d.Y_out, (unsigned)d.X_out);
+    k_count_nonfinite<<<g, 128, 0, c->stream>>>(d, R(c, field), bad);
+    unsigned long long h = 0;
+    int rc = cuda_check(c, cudaMemcpyAsync(&h, bad, sizeof h, cudaMemcpyDeviceToHost, c->stream), "cf_check_finite");
+    if (rc) return rc;
+    rc = cuda_check(c, cudaStreamSynchronize(c->stream), "cf_check_finite sync");
+    if (rc) return rc;
+    return h ? fail(c, CF_ERR_NONFINITE, "%llu non-finite interior values", h) : CF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// boundary conditions
+
+int cf_Y_boundary_condition(cf_ctx *c, int, double *U1_, double *U2_, double *U3_, double *U4_, double *U5_,
+                            double *J)
+{
+    if (!c) return CF_ERR_ARG;
+    const double *p[6] = {U1_, U2_, U3_, U4_, U5_, J};
+    if (int rc = check_ptrs(c, p, 6, "Y_boundary_condition")) return rc;
+    cf_ptr5 U{{R(c, U1_), R(c, U2_), R(c, U3_), R(c, U4_), R(c, U5_)}};
+    cudaError_t e = exact(c) ? cf_exact::y_wall(c->d, U, R(c, J), c->stream)
+                             : cf_fast::y_wall(c->d, U, R(c, J), c->stream);
+    return cuda_check(c, e, "Y_boundary_condition");
+}
+
+int cf_Z_boundary_condition(cf_ctx *c, int, double *U1_, double *U2_, double *U3_, double *U4_, double *U5_,
+                            double *J)
+{
+    if (!c) return CF_ERR_ARG;
+    const double *p[5] = {U1_, U2_, U3_, U4_, U5_};
+    if (int rc = check_ptrs(c, p, 5, "Z_boundary_condition")) return rc;
+    (void)J;
+    cf_ptr5 U{{R(c, U1_), R(c, U2_), R(c, U3_), R(c, U4_), R(c, U5_)}};
+    return cuda_check(c, cf_exact::z_periodic(c->d, U, c->stream), "Z_boundary_condition");
+}
+
+int cf_X_periodic(cf_ctx *c, int, double *U1_, double *U2_, double *U3_, double *U4_, double *U5_)
+{
+    if (!c) return CF_ERR_ARG;
+    const double *p[5] = {U1_, U2_, U3_, U4_, U5_};
+    if (int rc = check_ptrs(c, p, 5, "X_periodic")) return rc;
+    cf_ptr5 U{{R(c, U1_), R(c, U2_), R(c, U3_), R(c, U4_), R(c, U5_)}};
+    return cuda_check(c, cf_exact::x_periodic(c->d, U, c->stream), "X_periodic");
+}
+
+// ---------------------------------------------------------------------------
+// fluxes
+
+static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double *const *p32)
+{
+    if (!c) return CF_ERR_ARG;
+    // arrays 5..14 (ML/MR) are the reference's scratch and are not needed
+    for (int i = 0; i < 32; i++) {
+        if (i >= 5 && i < 15) continue;
+        if (i == 15 && dir == 0 && limited) continue;       // X limiter does not read J
+        if (i == 31 && !limited) continue;                  // unlimited fluxes do not read Ep
+        if (!p32[i]) return fail(c, CF_ERR_ARG, "%s: array argument %d is NULL", who, i);
+    }
+    cf_flux_args a;
+    for (int n = 0; n < 5; n++) a.U[n] = R(c, p32[n]);
+    a.J = p32[15] ? R(c, p32[15]) : nullptr;
+    a.Jf = R(c, p32[16]);
+    for (int n = 0; n < 9; n++) a.m[n] = R(c, p32[17 + n]);
+    for (int n = 0; n < 5; n++) a.F[n] = R(c, p32[26 + n]);
+    a.Ep = p32[31] ? R(c, p32[31]) : nullptr;
+    cudaError_t e = exact(c) ? cf_exact::flux(c->d, a, dir, limited, 0, c->stream)
+                             : cf_fast::flux(c->d, a, dir, limited, kprec(c), c->stream);
+    return cuda_check(c, e, who);
+}
+
+#define CF_FLUX_LIST                                                                                  \
+    U1_, U2_, U3_, U4_, U5_, MR1, MR2, MR3, MR4, MR5, ML1, ML2, ML3, ML4, ML5, J, J_f, xidx_f, xidy_f, \
+        xidz_f, etdx_f, etdy_f, etdz_f, ztdx_f, ztdy_f, ztdz_f, inF1, inF2, inF3, inF4, inF5, Ep
+
+#define CF_FLUX_ENTRY(name, dir, lim)                                   \
+    int cf_##name(cf_ctx *c, int, CF_FLUX_ARRAYS)                       \
+    {                                                                   \
+        double *const p[32] = {CF_FLUX_LIST};                           \
+        return flux_common(c, #name, dir, lim, p);                      \
+    }
+
+CF_FLUX_ENTRY(Flux_X_limiter, 0, true)
+CF_FLUX_ENTRY(Flux_Y_limiter, 1, true)
+CF_FLUX_ENTRY(Flux_Z_limiter, 2, true)
+CF_FLUX_ENTRY(Flux_X, 0, false)
+CF_FLUX_ENTRY(Flux_Y, 1, false)
+CF_FLUX_ENTRY(Flux_Z, 2, false)
+
+// ---------------------------------------------------------------------------
+// viscous terms
+
+int cf_Viscous_terms(cf_ctx *c, int, double **p)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    // read: U (0-4), J (9), face metric sets (19-48); written: vF (5-8),
+    // LL2..5 (55-58), ML2..5 (65-68), NL2..5 (75-78)
+    static const int need[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30,
+                               31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48,
+                               55, 56, 57, 58, 65, 66, 67, 68, 75, 76, 77, 78};
+    for (int i : need)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "Viscous_terms: array argument %d is NULL", i);
+    cf_visc_args a;
+    for (int n = 0; n < 5; n++) a.U[n] = R(c, p[n]);
+    for (int n = 0; n < 4; n++) a.vF[n] = R(c, p[5 + n]);
+    a.J = R(c, p[9]);
+    for (int f = 0; f < 3; f++) {
+        a.Jf[f] = R(c, p[19 + 10 * f]);
+        for (int n = 0; n < 9; n++) a.mf[f][n] = R(c, p[20 + 10 * f + n]);
+    }
+    for (int n = 0; n < 4; n++) {
+        a.LL[n] = R(c, p[55 + n]);
+        a.ML[n] = R(c, p[65 + n]);
+        a.NL[n] = R(c, p[75 + n]);
+    }
+    double *prim = scratch(c, "visc_prim", 4);
+    if (!prim) return fail(c, CF_ERR_NOMEM, "Viscous_terms: scratch allocation failed");
+    for (int n = 0; n < 4; n++) a.prim[n] = prim + (size_t)n * c->d.total();
+    cudaError_t e = exact(c) ? cf_exact::viscous(c->d, a, 0, c->stream)
+                             : cf_fast::viscous(c->d, a, kprec(c), c->stream);
+    return cuda_check(c, e, "Viscous_terms");
+}
+
+// ---------------------------------------------------------------------------
+// sensor
+
+int cf_Filter(cf_ctx *c, int, double Roe_criterion, double E_high, double E_low, double *U1_, double *U2_,
+              double *U3_, double *U4_, double *U5_, double *Y_point, double *EpX, double *EpY, double *EpZ,
+              double *J)
+{
+    if (!c) return CF_ERR_ARG;
+    const double *p[10] = {U1_, U2_, U3_, U4_, U5_, Y_point, EpX, EpY, EpZ, J};
+    if (int rc = check_ptrs(c, p, 10, "Filter")) return rc;
+    cf_filter_args a;
+    for (int n = 0; n < 5; n++) a.U[n] = R(c, p[n]);
+    a.Yp = R(c, Y_point);
+    a.J = R(c, J);
+    a.Ep[0] = R(c, EpX); a.Ep[1] = R(c, EpY); a.Ep[2] = R(c, EpZ);
+    double *s = scratch(c, "filter", 27);
+    if (!s) return fail(c, CF_ERR_NOMEM, "Filter: scratch allocation failed");
+    const size_t n = c->d.total();
+    int f = 0;
+    for (int v = 0; v < 5; v++) a.gx[v] = s + n * f++;
+    for (int v = 0; v < 5; v++) a.gy[v] = s + n * f++;
+    for (int l = 0; l < 2; l++)
+        for (int v = 0; v < 5; v++) a.lev[l][v] = s + n * f++;
+    for (int v = 0; v < 5; v++) a.acc[v] = s + n * f++;
+    a.Eh = s + n * f++;
+    a.E2h = s + n * f++;
+    // the switch Ep is a threshold decision: the FP64 sensor always runs in
+    // the no-FMA build so that it takes the reference's decisions exactly
+    cudaError_t e = c->prec == CF_PREC_FP32
+                        ? cf_fast::filter(c->d, a, Roe_criterion, E_high, E_low, 1, c->stream)
+                        : cf_exact::filter(c->d, a, Roe_criterion, E_high, E_low, 0, c->stream);
+    return cuda_check(c, e, "Filter");
+}
+
+// ---------------------------------------------------------------------------
+// time integration
+
+int cf_RK3NODT(cf_ctx *c, int, int RK, double deltaT, double *, double *, double *, double *, double *,
+               double **p)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    if (RK < 1 || RK > 3) return fail(c, CF_ERR_ARG, "RK3NODT: RK must be 1, 2 or 3");
+    static const int need[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 15, 25, 26, 27, 28, 29, 30, 31, 32, 33, 34,
+                               35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48};
+    for (int i : need)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "RK3NODT: array argument %d is NULL", i);
+    cf_rk3_args a;
+    for (int n = 0; n < 5; n++) {
+        a.U_[n] = R(c, p[n]);
+        a.U[n] = R(c, p[5 + n]);
+        a.Fx[n] = R(c, p[25 + n]);
+        a.Fy[n] = R(c, p[30 + n]);
+        a.Fz[n] = R(c, p[35 + n]);
+        a.MR[n] = R(c, p[44 + n]);
+    }
+    a.J = R(c, p[15]);
+    for (int n = 0; n < 4; n++) a.vF[n] = R(c, p[40 + n]);
+    cudaError_t e = exact(c) ? cf_exact::rk3(c->d, a, RK, deltaT, 0, c->stream)
+                             : cf_fast::rk3(c->d, a, RK, deltaT, kprec(c), c->stream);
+    return cuda_check(c, e, "RK3NODT");
+}
+
+int cf_Hyperplane(cf_ctx *c, int, int *Nijk, int *ijk)
+{
+    if (!c || !Nijk || !ijk) return CF_ERR_ARG;
+    std::memcpy(Nijk, c->nijk.data(), c->nijk.size() * sizeof(int));
+    std::memcpy(ijk, c->ijk.data(), c->ijk.size() * sizeof(int));
+    return CF_OK;
+}
+
+static int lu_args(cf_ctx *c, double **p, const char *who, cf_lu_args &a)
+{
+    static const int skip_lo = 44;  // everything up to MR is read or written
+    (void)skip_lo;
+    for (int i = 0; i < 64; i++)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "%s: array argument %d is NULL", who, i);
+    for (int n = 0; n < 5; n++) {
+        a.U_[n] = R(c, p[n]);
+        a.U[n] = R(c, p[5 + n]);
+        a.Uq[n] = R(c, p[10 + n]);
+        a.Fx[n] = R(c, p[25 + n]);
+        a.Fy[n] = R(c, p[30 + n]);
+        a.Fz[n] = R(c, p[35 + n]);
+        a.MR[n] = R(c, p[44 + n]);
+        a.NR[n] = R(c, p[49 + n]);
+        a.NL[n] = R(c, p[54 + n]);
+        a.Res[n] = R(c, p[59 + n]);
+    }
+    a.J = R(c, p[15]);
+    for (int n = 0; n < 9; n++) a.m[n] = R(c, p[16 + n]);
+    for (int n = 0; n < 4; n++) a.vF[n] = R(c, p[40 + n]);
+    cf_dims &d = c->d;
+    const size_t np = cf_fast::lu_partial_count(d);
+    auto &e = c->scratch["lu_partial"];
+    if (!e.first || e.second < 5 * np * sizeof(double)) {
+        if (e.first) cudaFree(e.first);
+        e.first = nullptr;
+        if (cudaMalloc(&e.first, 5 * np * sizeof(double)) != cudaSuccess) {
+            e.first = nullptr;
+            return fail(c, CF_ERR_NOMEM, "%s: scratch allocation failed", who);
+        }
+        e.second = 5 * np * sizeof(double);
+    }
+    a.partial = e.first;
+    return CF_OK;
+}
+
+static int lu_finish_host(cf_ctx *c, const cf_lu_args &a, double *er[5], const char *who)
+{
+    cudaError_t e = exact(c) ? cf_exact::lu_finish(c->d, a, c->er_dev, c->stream)
+                             : cf_fast::lu_finish(c->d, a, c->er_dev, c->stream);
+    if (int rc = cuda_check(c, e, who)) return rc;
+    if (int rc = cuda_check(c, cudaMemcpyAsync(c->er_host, c->er_dev, 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                                               c->stream), who)) return rc;
+    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), who)) return rc;
+    for (int n = 0; n < 5; n++)
+        if (er[n]) *er[n] = c->er_host[n];
+    return CF_OK;
+}
+
+int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4,
+                          double *er5, int *Nijk, int *ijk, double **p)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    // the plane tables are a fixed function of the grid; the context holds
+    // them already.  Tables handed in are checked once against them.
+    if (Nijk && ijk && !c->tables_checked) {
+        if (std::memcmp(Nijk, c->nijk.data(), c->nijk.size() * sizeof(int)) != 0)
+            return fail(c, CF_ERR_ARG, "Dual_time_stepping: Nijk differs from the Hyperplane tables of this grid");
+        c->tables_checked = true;
+    }
+    cf_lu_args a;
+    if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
+    const cf_dims &d = c->d;
+    const bool ex = exact(c);
+    const int pr = ex ? 0 : kprec(c);
+    cudaError_t e = ex ? cf_exact::lu_prepare(d, a, deltaT, true, 0, c->stream)
+                       : cf_fast::lu_prepare(d, a, deltaT, true, pr, c->stream);
+    if (int rc = cuda_check(c, e, "Dual_time_stepping")) return rc;
+    const int mlast = d.gend + d.ny + d.nz;
+    for (int sweep = 1; sweep <= 2; sweep++) {
+        for (int m = 7; m <= mlast; m++) {
+            const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
+            e = ex ? cf_exact::lu_plane(d, a, c->ijk_dev, first, cnt, true, deltaT, 0, c->stream)
+                   : cf_fast::lu_plane(d, a, c->ijk_dev, first, cnt, true, deltaT, pr, c->stream);
+            if (e != cudaSuccess) return cuda_check(c, e, "Dual_time_stepping forward plane");
+        }
+        for (int m = mlast; m >= 7; m--) {
+            const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
+            e = ex ? cf_exact::lu_plane(d, a, c->ijk_dev, first, cnt, false, deltaT, 0, c->stream)
+                   : cf_fast::lu_plane(d, a, c->ijk_dev, first, cnt, false, deltaT, pr, c->stream);
+            if (e != cudaSuccess) return cuda_check(c, e, "Dual_time_stepping backward plane");
+        }
+        e = cf_fast::lu_copy(d, a, c->stream);
+        if (int rc = cuda_check(c, e, "Dual_time_stepping copy")) return rc;
+    }
+    double *er[5] = {er1, er2, er3, er4, er5};
+    return lu_finish_host(c, a, er, "Dual_time_stepping");
+}
+
+int cf_DPLUSGS(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,
+               double **p)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    cf_lu_args a;
+    if (int rc = lu_args(c, p, "DPLUSGS", a)) return rc;
+    const cf_dims &d = c->d;
+    const bool ex = exact(c);
+    const int pr = ex ? 0 : kprec(c);
+    cudaError_t e = ex ? cf_exact::lu_prepare(d, a, deltaT, false, 0, c->stream)
+                       : cf_fast::lu_prepare(d, a, deltaT, false, pr, c->stream);
+    if (int rc = cuda_check(c, e, "DPLUSGS")) return rc;
+    for (int sweep = 1; sweep <= 4; sweep++) {
+        e = ex ? cf_exact::lu_jacobi(d, a, deltaT, 0, c->stream) : cf_fast::lu_jacobi(d, a, deltaT, pr, c->stream);
+        if (int rc = cuda_check(c, e, "DPLUSGS sweep")) return rc;
+        e = cf_fast::lu_copy(d, a, c->stream);
+        if (int rc = cuda_check(c, e, "DPLUSGS copy")) return rc;
+    }
+    double *er[5] = {er1, er2, er3, er4, er5};
+    return lu_finish_host(c, a, er, "DPLUSGS");
+}
+
+// ---------------------------------------------------------------------------
+// face metrics
+
+static int jacobian_common(cf_ctx *c, double **p, int which, const char *who)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    const int n = which == 1 ? 20 : 10;
+    for (int i = 0; i < n; i++)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "%s: array argument %d is NULL", who, i);
+    cf_metric_args a;
+    a.Jf = R(c, p[0]);
+    for (int t = 0; t < 9; t++) a.m[t] = R(c, p[1 + t]);
+    a.Jc = which == 1 ? R(c, p[10]) : nullptr;
+    for (int t = 0; t < 9; t++) a.mc[t] = which == 1 ? R(c, p[11 + t]) : nullptr;
+    return cuda_check(c, cf_fast::face_metrics(c->d, a, which, c->gamma, c->stream), who);
+}
+
+int cf_Jacobian_u(cf_ctx *c, int, double **p) { return jacobian_common(c, p, 0, "Jacobian_u"); }
+int cf_Jacobian_v(cf_ctx *c, int, double **p) { return jacobian_common(c, p, 1, "Jacobian_v"); }
+int cf_Jacobian_w(cf_ctx *c, int, double **p) { return jacobian_common(c, p, 2, "Jacobian_w"); }
+
+}  // extern "C"

@@ -1,0 +1,30 @@
+// Shared device-side definitions of the channel-flow hot path.
+//
+// Layout (the reference's single-rank layout, Array.h:7): every field is one
+// double[X_out+6][Y_out+4][Z_out+4] array with z fastest.  Interior cells are
+// i = 3..gend (gend = X_out+2), j = 2..ny (ny = Y_out+1), k = 2..nz
+// (nz = Z_out+1).  Face arrays use the same extents with one index shifted
+// by -1 (x faces inFx[i][j-1][k-1] between cells i and i+1, and so on).
+#pragma once
+
+#include "cf_types.h"
+
+#ifndef CF_NS
+#error "CF_NS (the build-variant namespace) must be defined by the including translation unit"
+#endif
+
+
+
+// The reference's min/max macros (Flux_X_limiter.cpp:13-14): plain
+// comparisons, so NaN and signed zeros resolve as they do there.
+template <typename T>
+__device__ __forceinline__ T rmin(T a, T b) { return (a < b) ? a : b; }
+template <typename T>
+__device__ __forceinline__ T rmax(T a, T b) { return (a > b) ? a : b; }
+
+
+#define CF_BOX_INDEX(b, i, j, k)                                    \
+    const int k = (b).k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); \
+    const int j = (b).j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y); \
+    const int i = (b).i0 + (int)blockIdx.z;                         \
+    if (k >= (b).k0 + (b).nk || j >= (b).j0 + (b).nj) return

@@ -1,0 +1,34 @@
+// Host launchers of one build variant of the kernels.  cf_variant.cu is
+// compiled twice: namespace cf_exact with --fmad=false (every FP64 result
+// equals the reference's bit for bit) and namespace cf_fast with fused
+// multiply-add (FP64 within 1e-12; also the FP32 instantiations).
+// prec: 0 = double, 1 = float arithmetic inside the kernel.
+#pragma once
+#include "cf_types.h"
+
+#define CF_DECLARE_LAUNCHERS(NS)                                                                        \
+    namespace NS {                                                                                      \
+    cudaError_t x_periodic(const cf_dims &d, const cf_ptr5 &U, cudaStream_t s);                         \
+    cudaError_t y_wall(const cf_dims &d, const cf_ptr5 &U, const double *J, cudaStream_t s);            \
+    cudaError_t z_periodic(const cf_dims &d, const cf_ptr5 &U, cudaStream_t s);                         \
+    cudaError_t flux(const cf_dims &d, const cf_flux_args &a, int dir, bool limited, int prec,          \
+                     cudaStream_t s);                                                                   \
+    cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStream_t s);            \
+    cudaError_t filter(const cf_dims &d, const cf_filter_args &a, double crit, double hi, double lo,   \
+                       int prec, cudaStream_t s);                                                       \
+    cudaError_t rk3(const cf_dims &d, const cf_rk3_args &a, int RK, double dt, int prec,               \
+                    cudaStream_t s);                                                                    \
+    cudaError_t lu_prepare(const cf_dims &d, const cf_lu_args &a, double dt, bool copy_nr, int prec,   \
+                           cudaStream_t s);                                                             \
+    cudaError_t lu_plane(const cf_dims &d, const cf_lu_args &a, const int *ijk, int first, int count,  \
+                         bool forward, double dt, int prec, cudaStream_t s);                            \
+    cudaError_t lu_jacobi(const cf_dims &d, const cf_lu_args &a, double dt, int prec, cudaStream_t s); \
+    cudaError_t lu_copy(const cf_dims &d, const cf_lu_args &a, cudaStream_t s);                        \
+    cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, cudaStream_t s);     \
+    size_t lu_partial_count(const cf_dims &d);                                                          \
+    cudaError_t face_metrics(const cf_dims &d, const cf_metric_args &a, int which, double gamma,       \
+                             cudaStream_t s);                                                           \
+    }
+
+CF_DECLARE_LAUNCHERS(cf_exact)
+CF_DECLARE_LAUNCHERS(cf_fast)

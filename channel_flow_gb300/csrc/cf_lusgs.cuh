@@ -1,0 +1,388 @@
+// Dual-time LU-SGS: hyperplane Gauss-Seidel (Dual_time_stepping.cpp) and
+// the data-parallel Jacobi variant (DPLUSGS.cpp).
+//
+// Plane m of the hyperplane sweep holds the cells with i + j + k = m; every
+// cell of a plane depends only on cells of the previous plane, so one
+// launch per plane processes it in parallel and the result equals the
+// reference's plane-ordered loop.  Cells come from the reference's own
+// plane tables (Hyperplane.cpp), uploaded once per context.
+#pragma once
+#include "cf_common.cuh"
+
+
+namespace CF_NS {
+
+template <typename T>
+struct lstate {
+    T rho, u, v, w, VV, P, C, Tt, H, beta;
+};
+
+// Dual_time_stepping.cpp:344-363
+template <typename T>
+__device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args &a, size_t q)
+{
+    lstate<T> s;
+    const T K = T(d.K);
+    T u1 = T(a.U_[0][q]), Jq = T(a.J[q]);
+    s.rho = u1 * Jq;
+    s.u = T(a.U_[1][q]) / u1;
+    s.v = T(a.U_[2][q]) / u1;
+    s.w = T(a.U_[3][q]) / u1;
+    s.VV = s.u * s.u + s.v * s.v + s.w * s.w;
+    s.P = (T(a.U_[4][q]) * Jq - T(0.5) * s.rho * s.VV) * (K - T(1));
+    s.C = K * s.P / s.rho;
+    s.Tt = s.P / s.rho;
+    s.H = T(0.5) * s.VV + s.C / (K - T(1));
+    s.beta = rmax(s.VV / s.C, T(d.e));
+    return s;
+}
+
+// split Jacobian of one neighbour cell along metric row m0..m2
+// (Dual_time_stepping.cpp:619-651 x, 669-700 y/z; entries 52-54 associate
+// differently in x than in y and z, kept as written)
+template <typename T>
+struct lsplit {
+    T p11, p12, p13, p14, p21, p22, p31, p33, p41, p44, p51, p52, p53, p54, p55, m11, m22;
+};
+template <typename T>
+__device__ __forceinline__ lsplit<T> lu_split(lstate<T> s, T m0, T m1, T m2, bool xform, T K)
+{
+    lsplit<T> A;
+    T U = m0 * s.u + m1 * s.v + m2 * s.w;
+    T S = sqrt(U * U * (s.beta - T(1)) * (s.beta - T(1)) + T(4) * s.beta * s.C * (m0 * m0 + m1 * m1 + m2 * m2));
+    T lambda = ((s.beta + T(1)) * fabs(U) + S) / T(2);
+    T dd = fabs(lambda);
+    A.p11 = T(0.5) * (s.beta * U + dd);
+    A.p12 = T(0.5) * s.P * K * s.beta * m0;
+    A.p13 = T(0.5) * s.P * K * s.beta * m1;
+    A.p14 = T(0.5) * s.P * K * s.beta * m2;
+    A.p21 = T(0.5) * m0 / s.rho;
+    A.p22 = T(0.5) * (U + dd);
+    A.p31 = T(0.5) * m1 / s.rho;
+    A.p33 = A.p22;
+    A.p41 = T(0.5) * m2 / s.rho;
+    A.p44 = A.p22;
+    A.p51 = T(0.5) * U * (K - T(1)) * (s.beta - T(1)) / s.rho / K;
+    if (xform) {
+        A.p52 = T(0.5) * m0 * s.beta * s.Tt * (K - T(1));
+        A.p53 = T(0.5) * m1 * s.beta * s.Tt * (K - T(1));
+        A.p54 = T(0.5) * m2 * s.beta * s.Tt * (K - T(1));
+    } else {
+        A.p52 = T(0.5) * s.beta * s.Tt * (K - T(1)) * m0;
+        A.p53 = T(0.5) * s.beta * s.Tt * (K - T(1)) * m1;
+        A.p54 = T(0.5) * s.beta * s.Tt * (K - T(1)) * m2;
+    }
+    A.p55 = A.p22;
+    A.m11 = T(0.5) * (s.beta * U - dd);
+    A.m22 = T(0.5) * (U - dd);
+    return A;
+}
+
+template <typename T>
+struct ldiag {
+    T d11, d22, d51;
+};
+// Dual_time_stepping.cpp:447-489
+template <typename T>
+__device__ __forceinline__ ldiag<T> lu_diag(const cf_dims &d, const cf_lu_args &a, size_t q, lstate<T> s,
+                                            T deltaT)
+{
+    const T K = T(d.K);
+    T xix = T(a.m[0][q]), xiy = T(a.m[1][q]), xiz = T(a.m[2][q]);
+    T etx = T(a.m[3][q]), ety = T(a.m[4][q]), etz = T(a.m[5][q]);
+    T ztx = T(a.m[6][q]), zty = T(a.m[7][q]), ztz = T(a.m[8][q]);
+    T beta = s.beta, C = s.C;
+    T U = xix * s.u + xiy * s.v + xiz * s.w;
+    T V = etx * s.u + ety * s.v + etz * s.w;
+    T W = ztx * s.u + zty * s.v + ztz * s.w;
+    T Sx = sqrt(U * U * (beta - T(1)) * (beta - T(1)) + T(4) * beta * C * (xix * xix + xiy * xiy + xiz * xiz));
+    T Sy = sqrt(V * V * (beta - T(1)) * (beta - T(1)) + T(4) * beta * C * (etx * etx + ety * ety + etz * etz));
+    T Sz = sqrt(W * W * (beta - T(1)) * (beta - T(1)) + T(4) * beta * C * (ztx * ztx + zty * zty + ztz * ztz));
+    T lambdaX = ((beta + T(1)) * fabs(U) + Sx) / T(2);
+    T lambdaY = ((beta + T(1)) * fabs(V) + Sy) / T(2);
+    T lambdaZ = ((beta + T(1)) * fabs(W) + Sz) / T(2);
+    T lambda = lambdaX / T(d.dXI) + lambdaY / T(d.dET) + lambdaZ / T(d.dZT);
+    ldiag<T> g;
+    g.d11 = T(2) * deltaT / (T(3) * beta + T(2) * lambda * deltaT);
+    g.d22 = T(2) * deltaT / (T(3) + T(2) * lambda * deltaT);
+    T temp1 = T(6) * (K - T(1)) * (beta - T(1)) * deltaT;
+    T temp2 = K * (T(3) + T(2) * lambda * deltaT) * (T(3) * beta + T(2) * lambda * deltaT) * s.rho;
+    g.d51 = -temp1 / temp2;
+    return g;
+}
+
+// NL/NR ghost shell = 0 (Dual_time_stepping.cpp:195-316)
+__global__ void k_lu_zero(cf_dims d, cf_lu_args a, size_t n)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const size_t plane = d.plane();
+    const int i = (int)(q / plane);
+    const size_t r = q - (size_t)i * plane;
+    const int j = (int)(r / (size_t)d.Zm);
+    const int k = (int)(r - (size_t)j * (size_t)d.Zm);
+    const int nyy = d.ny + 1, nzz = d.nz + 1;
+    const bool xpl = (i == 2 || i == d.gend + 1) && j >= 1 && j <= nyy && k >= 1 && k <= nzz;
+    const bool in_x = i >= 2 && i <= d.gend + 1;
+    const bool yrow = in_x && (j == 1 || j == nyy) && k >= 1 && k <= nzz;
+    const bool zcol = in_x && (k == 1 || k == nzz) && j >= 1 && j <= nyy;
+    if (!(xpl || yrow || zcol)) return;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        a.NL[v][q] = 0;
+        a.NR[v][q] = 0;
+    }
+}
+
+// BDF2 residual, Gamma^-1 R and the diagonal solve (Dual_time_stepping.cpp:339-506)
+template <typename T>
+__global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf_box b, double dt, int copy_nr)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const size_t q = d.ix(i, j, k);
+    const T K = T(d.K), deltaT = T(dt);
+    lstate<T> s = lu_state<T>(d, a, q);
+    T rho = s.rho, u = s.u, v = s.v, w = s.w, VV = s.VV, Tt = s.Tt, H = s.H, beta = s.beta;
+    T temp = rho * K;
+    T d11 = -(H * (K - T(1)) + VV - K * (Tt + VV)) * beta;
+    T d12 = -(K - T(1)) * u * beta;
+    T d13 = -(K - T(1)) * v * beta;
+    T d14 = -(K - T(1)) * w * beta;
+    T d15 = (K - T(1)) * beta;
+    T d21 = -u / rho, d22 = T(1) / rho;
+    T d31 = -v / rho;
+    T d41 = -w / rho;
+    T d51 = (K - T(1)) * (VV + K * Tt * beta + (K - T(1)) * VV * beta + H * (T(-1) + beta - K * beta)) / temp;
+    T d52 = -(K - T(1)) * u * (T(1) + (K - T(1)) * beta) / temp;
+    T d53 = -(K - T(1)) * v * (T(1) + (K - T(1)) * beta) / temp;
+    T d54 = -(K - T(1)) * w * (T(1) + (K - T(1)) * beta) / temp;
+    T d55 = (K - T(1)) * (T(1) + (K - T(1)) * beta) / temp;
+    const size_t fx = d.ix(i, j - 1, k - 1), f0 = d.ix(i - 1, j - 1, k - 1);
+    const size_t fy = d.ix(i - 1, j, k - 1), fz = d.ix(i - 1, j - 1, k);
+    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
+    T Rk[5];
+#pragma unroll
+    for (int n = 0; n < 5; n++) {
+        T Rp = -(T(3) * T(a.U_[n][q]) - T(4) * T(a.U[n][q]) + T(a.Uq[n][q])) / (T(2) * deltaT);
+        T Rf = -((T(a.Fx[n][fx]) - T(a.Fx[n][f0])) / dXI + (T(a.Fy[n][fy]) - T(a.Fy[n][f0])) / dET +
+                 (T(a.Fz[n][fz]) - T(a.Fz[n][f0])) / dZT);
+        Rk[n] = Rp + Rf;
+    }
+    const T f = T(d.f), Jq = T(a.J[q]);
+    Rk[1] = Rk[1] + T(a.vF[0][q]) + f / Jq;
+    Rk[2] = Rk[2] + T(a.vF[1][q]);
+    Rk[3] = Rk[3] + T(a.vF[2][q]);
+    Rk[4] = Rk[4] + T(a.vF[3][q]) + f * u / Jq;
+    T MR1 = (d11 * Rk[0] + d12 * Rk[1] + d13 * Rk[2] + d14 * Rk[3] + d15 * Rk[4]);
+    T MR2 = (d21 * Rk[0] + d22 * Rk[1]);
+    T MR3 = (d31 * Rk[0] + d22 * Rk[2]);
+    T MR4 = (d41 * Rk[0] + d22 * Rk[3]);
+    T MR5 = (d51 * Rk[0] + d52 * Rk[1] + d53 * Rk[2] + d54 * Rk[3] + d55 * Rk[4]);
+    a.MR[0][q] = double(MR1); a.MR[1][q] = double(MR2); a.MR[2][q] = double(MR3);
+    a.MR[3][q] = double(MR4); a.MR[4][q] = double(MR5);
+    ldiag<T> g = lu_diag<T>(d, a, q, s, deltaT);
+    T nl[5] = {g.d11 * MR1, g.d22 * MR2, g.d22 * MR3, g.d22 * MR4, g.d51 * MR1 + g.d22 * MR5};
+#pragma unroll
+    for (int n = 0; n < 5; n++) {
+        a.NL[n][q] = double(nl[n]);
+        if (copy_nr) a.NR[n][q] = double(nl[n]);
+    }
+}
+
+// L*N from cells i-1, j-1, k-1 (Dual_time_stepping.cpp:751-811)
+template <typename T>
+__device__ __forceinline__ void lu_lower(const cf_dims &d, const cf_lu_args &a, double *const *N, int i, int j,
+                                         int k, T *LL)
+{
+    const T K = T(d.K);
+    const size_t qa = d.ix(i - 1, j, k), qb = d.ix(i, j - 1, k), qc = d.ix(i, j, k - 1);
+    lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
+    lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
+    lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), T(a.m[6][qc]), T(a.m[7][qc]), T(a.m[8][qc]), false, K);
+    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
+    T a0 = T(N[0][qa]), a1 = T(N[1][qa]), a2 = T(N[2][qa]), a3 = T(N[3][qa]), a4 = T(N[4][qa]);
+    T b0 = T(N[0][qb]), b1 = T(N[1][qb]), b2 = T(N[2][qb]), b3 = T(N[3][qb]), b4 = T(N[4][qb]);
+    T c0 = T(N[0][qc]), c1 = T(N[1][qc]), c2 = T(N[2][qc]), c3 = T(N[3][qc]), c4 = T(N[4][qc]);
+    LL[0] = (-A.p11 * a0 - A.p12 * a1 - A.p13 * a2 - A.p14 * a3) / dXI +
+            (-B.p11 * b0 - B.p12 * b1 - B.p13 * b2 - B.p14 * b3) / dET +
+            (-C.p11 * c0 - C.p12 * c1 - C.p13 * c2 - C.p14 * c3) / dZT;
+    LL[1] = (-A.p21 * a0 - A.p22 * a1) / dXI + (-B.p21 * b0 - B.p22 * b1) / dET + (-C.p21 * c0 - C.p22 * c1) / dZT;
+    LL[2] = (-A.p31 * a0 - A.p33 * a2) / dXI + (-B.p31 * b0 - B.p33 * b2) / dET + (-C.p31 * c0 - C.p33 * c2) / dZT;
+    LL[3] = (-A.p41 * a0 - A.p44 * a3) / dXI + (-B.p41 * b0 - B.p44 * b3) / dET + (-C.p41 * c0 - C.p44 * c3) / dZT;
+    LL[4] = (-A.p51 * a0 - A.p52 * a1 - A.p53 * a2 - A.p54 * a3 - A.p55 * a4) / dXI +
+            (-B.p51 * b0 - B.p52 * b1 - B.p53 * b2 - B.p54 * b3 - B.p55 * b4) / dET +
+            (-C.p51 * c0 - C.p52 * c1 - C.p53 * c2 - C.p54 * c3 - C.p55 * c4) / dZT;
+}
+
+// U*N from cells i+1, j+1, k+1 (Dual_time_stepping.cpp:1116-1177)
+template <typename T>
+__device__ __forceinline__ void lu_upper(const cf_dims &d, const cf_lu_args &a, double *const *N, int i, int j,
+                                         int k, T *UU)
+{
+    const T K = T(d.K);
+    const size_t qa = d.ix(i + 1, j, k), qb = d.ix(i, j + 1, k), qc = d.ix(i, j, k + 1);
+    lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
+    lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
+    lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), T(a.m[6][qc]), T(a.m[7][qc]), T(a.m[8][qc]), false, K);
+    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
+    T a0 = T(N[0][qa]), a1 = T(N[1][qa]), a2 = T(N[2][qa]), a3 = T(N[3][qa]), a4 = T(N[4][qa]);
+    T b0 = T(N[0][qb]), b1 = T(N[1][qb]), b2 = T(N[2][qb]), b3 = T(N[3][qb]), b4 = T(N[4][qb]);
+    T c0 = T(N[0][qc]), c1 = T(N[1][qc]), c2 = T(N[2][qc]), c3 = T(N[3][qc]), c4 = T(N[4][qc]);
+    UU[0] = (+A.m11 * a0 + A.p12 * a1 + A.p13 * a2 + A.p14 * a3) / dXI +
+            (+B.m11 * b0 + B.p12 * b1 + B.p13 * b2 + B.p14 * b3) / dET +
+            (+C.m11 * c0 + C.p12 * c1 + C.p13 * c2 + C.p14 * c3) / dZT;
+    UU[1] = (+A.p21 * a0 + A.m22 * a1) / dXI + (+B.p21 * b0 + B.m22 * b1) / dET + (+C.p21 * c0 + C.m22 * c1) / dZT;
+    UU[2] = (+A.p31 * a0 + A.m22 * a2) / dXI + (+B.p31 * b0 + B.m22 * b2) / dET + (+C.p31 * c0 + C.m22 * c2) / dZT;
+    UU[3] = (+A.p41 * a0 + A.m22 * a3) / dXI + (+B.p41 * b0 + B.m22 * b3) / dET + (+C.p41 * c0 + C.m22 * c3) / dZT;
+    UU[4] = (+A.p51 * a0 + A.p52 * a1 + A.p53 * a2 + A.p54 * a3 + A.m22 * a4) / dXI +
+            (+B.p51 * b0 + B.p52 * b1 + B.p53 * b2 + B.p54 * b3 + B.m22 * b4) / dET +
+            (+C.p51 * c0 + C.p52 * c1 + C.p53 * c2 + C.p54 * c3 + C.m22 * c4) / dZT;
+}
+
+// forward plane: NL = D^-1 (MR - L NL) (Dual_time_stepping.cpp:594-877)
+template <typename T>
+__global__ void k_lu_forward(cf_dims d, cf_lu_args a, const int *__restrict__ ijk, int first, int count, double dt)
+{
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= count) return;
+    const int *c = ijk + 3 * (size_t)(first + t);
+    const int i = c[0], j = c[1], k = c[2];
+    const size_t q = d.ix(i, j, k);
+    T LL[5];
+    lu_lower<T>(d, a, a.NL, i, j, k, LL);
+    ldiag<T> g = lu_diag<T>(d, a, q, lu_state<T>(d, a, q), T(dt));
+    T r0 = T(a.MR[0][q]) - LL[0];
+    a.NL[0][q] = double(g.d11 * r0);
+    a.NL[1][q] = double(g.d22 * (T(a.MR[1][q]) - LL[1]));
+    a.NL[2][q] = double(g.d22 * (T(a.MR[2][q]) - LL[2]));
+    a.NL[3][q] = double(g.d22 * (T(a.MR[3][q]) - LL[3]));
+    a.NL[4][q] = double(g.d51 * r0 + g.d22 * (T(a.MR[4][q]) - LL[4]));
+}
+
+// backward plane: NR = NL - D^-1 U NR (Dual_time_stepping.cpp:926-1245)
+template <typename T>
+__global__ void k_lu_backward(cf_dims d, cf_lu_args a, const int *__restrict__ ijk, int first, int count, double dt)
+{
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= count) return;
+    const int *c = ijk + 3 * (size_t)(first + t);
+    const int i = c[0], j = c[1], k = c[2];
+    const size_t q = d.ix(i, j, k);
+    T UU[5];
+    lu_upper<T>(d, a, a.NR, i, j, k, UU);
+    ldiag<T> g = lu_diag<T>(d, a, q, lu_state<T>(d, a, q), T(dt));
+    a.NR[0][q] = double(T(a.NL[0][q]) - g.d11 * UU[0]);
+    a.NR[1][q] = double(T(a.NL[1][q]) - g.d22 * UU[1]);
+    a.NR[2][q] = double(T(a.NL[2][q]) - g.d22 * UU[2]);
+    a.NR[3][q] = double(T(a.NL[3][q]) - g.d22 * UU[3]);
+    a.NR[4][q] = double(T(a.NL[4][q]) - (g.d51 * UU[0] + g.d22 * UU[4]));
+}
+
+// Jacobi sweep: NR = D^-1 (MR - L NL - U NL) (DPLUSGS.cpp:573-1121, with the
+// upper neighbours at j+1, k+1)
+template <typename T>
+__global__ void __launch_bounds__(256) k_lu_jacobi(cf_dims d, cf_lu_args a, cf_box b, double dt)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const size_t q = d.ix(i, j, k);
+    T LL[5], UU[5];
+    lu_lower<T>(d, a, a.NL, i, j, k, LL);
+    lu_upper<T>(d, a, a.NL, i, j, k, UU);
+    ldiag<T> g = lu_diag<T>(d, a, q, lu_state<T>(d, a, q), T(dt));
+    T r0 = T(a.MR[0][q]) - LL[0] - UU[0];
+    a.NR[0][q] = double(g.d11 * r0);
+    a.NR[1][q] = double(g.d22 * (T(a.MR[1][q]) - LL[1] - UU[1]));
+    a.NR[2][q] = double(g.d22 * (T(a.MR[2][q]) - LL[2] - UU[2]));
+    a.NR[3][q] = double(g.d22 * (T(a.MR[3][q]) - LL[3] - UU[3]));
+    a.NR[4][q] = double(g.d51 * r0 + g.d22 * (T(a.MR[4][q]) - LL[4] - UU[4]));
+}
+
+// interior copy NL <- NR (Dual_time_stepping.cpp:1261-1274)
+__global__ void k_lu_copy(cf_dims d, cf_lu_args a, cf_box b)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const size_t q = d.ix(i, j, k);
+#pragma unroll
+    for (int v = 0; v < 5; v++) a.NL[v][q] = a.NR[v][q];
+}
+
+// primitive update and the squared-change arrays (Dual_time_stepping.cpp:
+// 1290-1326), FP64 in every precision mode; each block also writes its
+// partial sums of Residual^2 (the reference's Sum(Delta^2)^2 norm)
+__global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_box b)
+{
+    const int k = b.k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = b.j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = b.i0 + (int)blockIdx.z;
+    double r2[5] = {0, 0, 0, 0, 0};
+    if (k < b.k0 + b.nk && j < b.j0 + b.nj) {
+        const size_t q = d.ix(i, j, k);
+        const double K = d.K, Jq = a.J[q];
+        double rhoold = a.U_[0][q] * Jq;
+        double Uold = a.U_[1][q] / a.U_[0][q];
+        double Vold = a.U_[2][q] / a.U_[0][q];
+        double Wold = a.U_[3][q] / a.U_[0][q];
+        double VVold = Uold * Uold + Vold * Vold + Wold * Wold;
+        double Pold = (a.U_[4][q] * Jq - 0.5 * rhoold * VVold) * (K - 1);
+        double Told = Pold / rhoold;
+        double P = Pold + a.NR[0][q] * Jq;
+        double U = Uold + a.NR[1][q] * Jq;
+        double V = Vold + a.NR[2][q] * Jq;
+        double W = Wold + a.NR[3][q] * Jq;
+        double Tt = Told + a.NR[4][q] * Jq;
+        double rho = P / Tt;
+        a.U_[0][q] = rho / Jq;
+        a.U_[1][q] = rho * U / Jq;
+        a.U_[2][q] = rho * V / Jq;
+        a.U_[3][q] = rho * W / Jq;
+        a.U_[4][q] = (P / (K - 1) + 0.5 * rho * (U * U + V * V + W * W)) / Jq;
+        double r[5] = {(P - Pold) * (P - Pold), (U - Uold) * (U - Uold), (V - Vold) * (V - Vold),
+                       (W - Wold) * (W - Wold), (Tt - Told) * (Tt - Told)};
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            a.Res[n][q] = r[n];
+            r2[n] = r[n] * r[n];
+        }
+    }
+    // block reduction in a fixed order (deterministic)
+    __shared__ double sh[5][256];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int n = 0; n < 5; n++) sh[n][tid] = r2[n];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (tid < w)
+#pragma unroll
+            for (int n = 0; n < 5; n++) sh[n][tid] += sh[n][tid + w];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int n = 0; n < 5; n++) a.partial[5 * blk + n] = sh[n][0];
+    }
+}
+
+// final reduction of the block partial sums, one block, fixed order;
+// er[n] = sqrt(sum) * DN (Dual_time_stepping.cpp:1348-1352)
+__global__ void k_lu_norm(const double *partial, size_t nblk, double DN, double *er)
+{
+    __shared__ double sh[5][256];
+    const int tid = threadIdx.x;
+    double s[5] = {0, 0, 0, 0, 0};
+    for (size_t b = tid; b < nblk; b += 256)
+#pragma unroll
+        for (int n = 0; n < 5; n++) s[n] += partial[5 * b + n];
+#pragma unroll
+    for (int n = 0; n < 5; n++) sh[n][tid] = s[n];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (tid < w)
+#pragma unroll
+            for (int n = 0; n < 5; n++) sh[n][tid] += sh[n][tid + w];
+        __syncthreads();
+    }
+    if (tid < 5) er[tid] = sqrt(sh[tid][0]) * DN;
+}
+
+}  // namespace CF_NS

@@ -1,0 +1,110 @@
+// Plain data types shared by the kernels and the C-ABI layer (no device code).
+//
+// Layout (the reference's single-rank layout, Array.h:7): every field is one
+// double[X_out+6][Y_out+4][Z_out+4] array with z fastest.  Interior cells are
+// i = 3..gend (gend = X_out+2), j = 2..ny (ny = Y_out+1), k = 2..nz
+// (nz = Z_out+1).  Face arrays use the same extents with one index shifted
+// by -1 (x faces inFx[i][j-1][k-1] between cells i and i+1, and so on).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+struct cf_dims {
+    int X_out, Y_out, Z_out;
+    int Ym, Zm;               // Y_out+4, Z_out+4: row and plane strides
+    int gend, ny, nz;         // X_out+2, Y_out+1, Z_out+1
+    double dXI, dET, dZT;     // computational spacings
+    double K, R, e;           // gamma, gas constant, preconditioning floor
+    double Cv, mu_L, Pr_L;
+    double f, high;           // body force, channel height 2h
+
+    __host__ __device__ __forceinline__ size_t ix(int i, int j, int k) const
+    {
+        return ((size_t)i * (size_t)Ym + (size_t)j) * (size_t)Zm + (size_t)k;
+    }
+    __host__ __device__ __forceinline__ size_t plane() const { return (size_t)Ym * (size_t)Zm; }
+    __host__ __device__ __forceinline__ size_t total() const { return (size_t)(X_out + 6) * plane(); }
+};
+
+struct cf_ptr5 {
+    double *p[5];
+};
+
+// Launch geometry of one index box [i0,i0+ni) x [j0,j0+nj) x [k0,k0+nk):
+// 32 consecutive z indices per warp (coalesced), 8 rows per block,
+// one x plane per grid layer.
+struct cf_box {
+    int i0, j0, k0, ni, nj, nk;
+};
+
+static inline dim3 box_block() { return dim3(32, 8, 1); }
+static inline dim3 box_grid(const cf_box &b)
+{
+    return dim3((unsigned)((b.nk + 31) / 32), (unsigned)((b.nj + 7) / 8), (unsigned)b.ni);
+}
+static inline cf_box make_box(int i0, int i1, int j0, int j1, int k0, int k1)
+{
+    cf_box b{i0, j0, k0, i1 - i0 + 1, j1 - j0 + 1, k1 - k0 + 1};
+    if (b.ni < 0) b.ni = 0;
+    if (b.nj < 0) b.nj = 0;
+    if (b.nk < 0) b.nk = 0;
+    return b;
+}
+
+struct cf_flux_args {
+    const double *U[5];   // U1_..U5_ (conserved / J)
+    const double *J;      // cell Jacobian
+    const double *Jf;     // face Jacobian J_u / J_v / J_w
+    const double *m[9];   // face metrics xidx..ztdz of the same face set
+    const double *Ep;     // sensor EpX / EpY / EpZ (limited fluxes only)
+    double *F[5];         // inF1..inF5
+};
+
+struct cf_visc_args {
+    const double *U[5];
+    double *vF[4];
+    const double *J;
+    const double *Jf[3];       // J_u, J_v, J_w
+    const double *mf[3][9];    // x-, y-, z-face metrics
+    double *LL[4], *ML[4], *NL[4];   // x/y/z face fluxes of variables 2..5
+    double *prim[4];           // scratch: u, v, w, T of every cell
+};
+
+struct cf_filter_args {
+    const double *U[5];
+    const double *Yp;       // Y_point
+    const double *J;
+    double *Ep[3];          // EpX, EpY, EpZ
+    double *gx[5], *gy[5], *lev[2][5], *acc[5];   // scratch
+    double *Eh, *E2h;                               // scratch
+};
+
+struct cf_lu_args {
+    double *U_[5];
+    const double *U[5], *Uq[5];
+    const double *J;
+    const double *m[9];      // cell metrics xidx..ztdz
+    const double *Fx[5], *Fy[5], *Fz[5];
+    const double *vF[4];
+    double *MR[5], *NR[5], *NL[5], *Res[5];
+    double *partial;         // scratch: per-block partial norm sums (5 per block)
+};
+
+struct cf_rk3_args {
+    double *U_[5];
+    const double *U[5];
+    const double *J;
+    const double *Fx[5], *Fy[5], *Fz[5];
+    const double *vF[4];
+    double *MR[5];
+};
+
+struct cf_metric_args {
+    double *Jf;
+    double *m[9];
+    const double *Jc;       // cell J (Jacobian_v wall rows)
+    const double *mc[9];    // cell metrics (Jacobian_v wall rows)
+};
+

@@ -1,0 +1,155 @@
+// One build variant of the hot-path kernels (see cf_launch.h).  The build
+// compiles this file twice, with -DCF_NS=cf_exact --fmad=false and with
+// -DCF_NS=cf_fast -DCF_WITH_FLOAT.
+#include "cf_flux.cuh"
+#include "cf_bc.cuh"
+#include "cf_visc.cuh"
+#include "cf_filter.cuh"
+#include "cf_lusgs.cuh"
+#include "cf_launch.h"
+
+#ifdef CF_WITH_FLOAT
+#define CF_DISPATCH(prec, call_double, call_float) ((prec) == 1 ? (call_float) : (call_double))
+#else
+#define CF_DISPATCH(prec, call_double, call_float) ((prec) == 1 ? cudaErrorNotSupported : (call_double))
+#endif
+
+namespace CF_NS {
+
+cudaError_t x_periodic(const cf_dims &d, const cf_ptr5 &U, cudaStream_t s)
+{
+    const size_t n = d.plane() * 6;
+    k_x_periodic<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, U);
+    return cudaGetLastError();
+}
+
+cudaError_t y_wall(const cf_dims &d, const cf_ptr5 &U, const double *J, cudaStream_t s)
+{
+    // Y_boundary_condition.cpp:41-50: i = 2..gend+1, k = 2..nz, both walls
+    cf_box b = make_box(2, d.gend + 1, 0, 1, 2, d.nz);
+    k_y_wall<double><<<box_grid(b), box_block(), 0, s>>>(d, U, J, b);
+    return cudaGetLastError();
+}
+
+cudaError_t z_periodic(const cf_dims &d, const cf_ptr5 &U, cudaStream_t s)
+{
+    // Z_boundary_condition.cpp:162-188: i = 2..gend+1, j = 0..nyyy
+    cf_box b = make_box(2, d.gend + 1, 0, d.ny + 2, 0, 0);
+    dim3 g((unsigned)((b.nj + 127) / 128), (unsigned)b.ni);
+    k_z_periodic<<<g, 128, 0, s>>>(d, U, b);
+    return cudaGetLastError();
+}
+
+cudaError_t flux(const cf_dims &d, const cf_flux_args &a, int dir, bool limited, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, launch_flux<double>(d, a, dir, limited, s), launch_flux<float>(d, a, dir, limited, s));
+}
+
+cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, launch_viscous<double>(d, a, s), launch_viscous<float>(d, a, s));
+}
+
+cudaError_t filter(const cf_dims &d, const cf_filter_args &a, double crit, double hi, double lo, int prec,
+                   cudaStream_t s)
+{
+    return CF_DISPATCH(prec, launch_filter<double>(d, a, crit, hi, lo, s),
+                       launch_filter<float>(d, a, crit, hi, lo, s));
+}
+
+template <typename T>
+static cudaError_t rk3_t(const cf_dims &d, const cf_rk3_args &a, int RK, double dt, cudaStream_t s)
+{
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    k_rk3<T><<<box_grid(b), box_block(), 0, s>>>(d, a, b, RK, dt);
+    return cudaGetLastError();
+}
+cudaError_t rk3(const cf_dims &d, const cf_rk3_args &a, int RK, double dt, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, rk3_t<double>(d, a, RK, dt, s), rk3_t<float>(d, a, RK, dt, s));
+}
+
+template <typename T>
+static cudaError_t lu_prepare_t(const cf_dims &d, const cf_lu_args &a, double dt, bool copy_nr, cudaStream_t s)
+{
+    const size_t n = d.total();
+    k_lu_zero<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    k_lu_assemble<T><<<box_grid(b), box_block(), 0, s>>>(d, a, b, dt, copy_nr ? 1 : 0);
+    return cudaGetLastError();
+}
+cudaError_t lu_prepare(const cf_dims &d, const cf_lu_args &a, double dt, bool copy_nr, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_prepare_t<double>(d, a, dt, copy_nr, s), lu_prepare_t<float>(d, a, dt, copy_nr, s));
+}
+
+template <typename T>
+static cudaError_t lu_plane_t(const cf_dims &d, const cf_lu_args &a, const int *ijk, int first, int count,
+                              bool forward, double dt, cudaStream_t s)
+{
+    if (count <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((count + 127) / 128);
+    if (forward) k_lu_forward<T><<<blocks, 128, 0, s>>>(d, a, ijk, first, count, dt);
+    else k_lu_backward<T><<<blocks, 128, 0, s>>>(d, a, ijk, first, count, dt);
+    return cudaGetLastError();
+}
+cudaError_t lu_plane(const cf_dims &d, const cf_lu_args &a, const int *ijk, int first, int count, bool forward,
+                     double dt, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_plane_t<double>(d, a, ijk, first, count, forward, dt, s),
+                       lu_plane_t<float>(d, a, ijk, first, count, forward, dt, s));
+}
+
+template <typename T>
+static cudaError_t lu_jacobi_t(const cf_dims &d, const cf_lu_args &a, double dt, cudaStream_t s)
+{
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    k_lu_jacobi<T><<<box_grid(b), box_block(), 0, s>>>(d, a, b, dt);
+    return cudaGetLastError();
+}
+cudaError_t lu_jacobi(const cf_dims &d, const cf_lu_args &a, double dt, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_jacobi_t<double>(d, a, dt, s), lu_jacobi_t<float>(d, a, dt, s));
+}
+
+cudaError_t lu_copy(const cf_dims &d, const cf_lu_args &a, cudaStream_t s)
+{
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    k_lu_copy<<<box_grid(b), box_block(), 0, s>>>(d, a, b);
+    return cudaGetLastError();
+}
+
+size_t lu_partial_count(const cf_dims &d)
+{
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    dim3 g = box_grid(b);
+    return (size_t)g.x * g.y * g.z;
+}
+
+cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, cudaStream_t s)
+{
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    dim3 g = box_grid(b);
+    k_lu_update<<<g, box_block(), 0, s>>>(d, a, b);
+    const double DN = 1. / (d.X_out * d.Y_out * d.Z_out);
+    k_lu_norm<<<1, 256, 0, s>>>(a.partial, lu_partial_count(d), DN, er_dev);
+    return cudaGetLastError();
+}
+
+cudaError_t face_metrics(const cf_dims &d, const cf_metric_args &a, int which, double gamma, cudaStream_t s)
+{
+    cf_box b;
+    double joff;
+    if (which == 0) { b = make_box(2, d.gend, 1, d.ny - 1, 1, d.nz - 1); joff = 0.5; }       // Jacobian_u
+    else if (which == 1) { b = make_box(2, d.gend - 1, 1, d.ny, 1, d.nz - 1); joff = 1.0; }  // Jacobian_v
+    else { b = make_box(2, d.gend - 1, 1, d.ny - 1, 1, d.nz); joff = 0.5; }                  // Jacobian_w
+    k_face_metrics<<<box_grid(b), box_block(), 0, s>>>(d, a, b, gamma, joff);
+    if (which == 1) {
+        cf_box w = make_box(2, d.gend - 1, 0, 0, 1, d.nz - 1);
+        dim3 g((unsigned)((w.nk + 127) / 128), (unsigned)w.ni);
+        k_v_wall_rows<<<g, 128, 0, s>>>(d, a, w);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace CF_NS

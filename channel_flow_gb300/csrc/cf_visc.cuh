@@ -1,0 +1,231 @@
+// Viscous and heat-flux terms (Viscous_terms.cpp:15-886).
+//
+// Three kernels: (1) primitive u, v, w, T of every cell into scratch (the
+// reference repeats this conversion for each of the 13 neighbours with the
+// same expression, so precomputing it once changes no value); (2) for every
+// cell of i = 3..gend+1, j = 2..nyy, k = 2..nzz the x-, y- and z-face
+// fluxes on its low faces into the caller's LL2..5 / ML2..5 / NL2..5 arrays,
+// as the reference does; (3) the central divergence vF2..vF5.
+#pragma once
+#include "cf_common.cuh"
+
+
+namespace CF_NS {
+
+template <typename T>
+__global__ void k_visc_prim(cf_dims d, cf_visc_args a, size_t n)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const T K = T(d.K), R = T(d.R);
+    T rho = T(a.U[0][q]);
+    T U = T(a.U[1][q]) / rho;
+    T V = T(a.U[2][q]) / rho;
+    T W = T(a.U[3][q]) / rho;
+    T VV = U * U + V * V + W * W;
+    T Jq = T(a.J[q]);
+    T P = (T(a.U[4][q]) - T(0.5) * rho * VV) * (K - T(1)) * Jq;
+    T Tt = P / (rho * R) / Jq;
+    a.prim[0][q] = double(U);
+    a.prim[1][q] = double(V);
+    a.prim[2][q] = double(W);
+    a.prim[3][q] = double(Tt);
+}
+
+template <typename T>
+struct vgrad {
+    T du, dv, dw, du2, dv2, dw2, duv, dvw, duw, dT;
+};
+template <typename T>
+struct vcell {
+    T u, v, w, t;
+};
+
+template <typename T>
+__device__ __forceinline__ vcell<T> ld(const cf_visc_args &a, size_t q)
+{
+    return vcell<T>{T(a.prim[0][q]), T(a.prim[1][q]), T(a.prim[2][q]), T(a.prim[3][q])};
+}
+
+// one-sided difference c - n (Viscous_terms.cpp:400-415)
+template <typename T>
+__device__ __forceinline__ vgrad<T> g2(vcell<T> c, vcell<T> n, T inv)
+{
+    vgrad<T> d;
+    d.du = (c.u - n.u) * inv;
+    d.dv = (c.v - n.v) * inv;
+    d.dw = (c.w - n.w) * inv;
+    d.du2 = (c.u * c.u - n.u * n.u) * inv;
+    d.dv2 = (c.v * c.v - n.v * n.v) * inv;
+    d.dw2 = (c.w * c.w - n.w * n.w) * inv;
+    d.duv = (c.u * c.v - n.u * n.v) * inv;
+    d.dvw = (c.v * c.w - n.v * n.w) * inv;
+    d.duw = (c.u * c.w - n.u * n.w) * inv;
+    d.dT = (c.t - n.t) * inv;
+    return d;
+}
+// four-point tangential difference p + q - r - s (Viscous_terms.cpp:419-451);
+// the mixed products take their second factor from q2, which reproduces
+// the z-face y-derivative kUj*iVj of Viscous_terms.cpp:728-730
+template <typename T>
+__device__ __forceinline__ vgrad<T> g4(vcell<T> p, vcell<T> q, vcell<T> r, vcell<T> s, vcell<T> q2, T inv)
+{
+    vgrad<T> d;
+    d.du = (p.u + q.u - r.u - s.u) * inv;
+    d.dv = (p.v + q.v - r.v - s.v) * inv;
+    d.dw = (p.w + q.w - r.w - s.w) * inv;
+    d.du2 = (p.u * p.u + q.u * q.u - r.u * r.u - s.u * s.u) * inv;
+    d.dv2 = (p.v * p.v + q.v * q.v - r.v * r.v - s.v * s.v) * inv;
+    d.dw2 = (p.w * p.w + q.w * q.w - r.w * r.w - s.w * s.w) * inv;
+    d.duv = (p.u * p.v + q.u * q2.v - r.u * r.v - s.u * s.v) * inv;
+    d.dvw = (p.v * p.w + q.v * q2.w - r.v * r.w - s.v * s.w) * inv;
+    d.duw = (p.u * p.w + q.u * q2.w - r.u * r.w - s.u * s.w) * inv;
+    d.dT = (p.t + q.t - r.t - s.t) * inv;
+    return d;
+}
+
+// coefficient sets of one face (Viscous_terms.cpp:471-526)
+template <typename T>
+struct vsym {
+    T s1, s2, s3, s4, s5, s6, s7;
+};
+template <typename T>
+struct vcross {
+    T x1, x2, x3, x4, x5, x6, x7, x8, x9, x10;
+};
+template <typename T>
+__device__ __forceinline__ vsym<T> csym(T p0, T p1, T p2)
+{
+    vsym<T> c;
+    c.s1 = (T(4.) / T(3)) * p0 * p0 + p1 * p1 + p2 * p2;
+    c.s2 = p0 * p0 + (T(4.) / T(3)) * p1 * p1 + p2 * p2;
+    c.s3 = p0 * p0 + p1 * p1 + (T(4.) / T(3)) * p2 * p2;
+    c.s4 = p0 * p0 + p1 * p1 + p2 * p2;
+    c.s5 = (T(1.) / T(3)) * p0 * p1;
+    c.s6 = (T(1.) / T(3)) * p1 * p2;
+    c.s7 = (T(1.) / T(3)) * p0 * p2;
+    return c;
+}
+template <typename T>
+__device__ __forceinline__ vcross<T> ccross(T p0, T p1, T p2, T q0, T q1, T q2)
+{
+    vcross<T> c;
+    c.x1 = (T(4.) / T(3)) * p0 * q0 + p1 * q1 + p2 * q2;
+    c.x2 = p0 * q0 + (T(4.) / T(3)) * p1 * q1 + p2 * q2;
+    c.x3 = p0 * q0 + p1 * q1 + (T(4.) / T(3)) * p2 * q2;
+    c.x4 = p0 * q0 + p1 * q1 + p2 * q2;
+    c.x5 = p0 * q1 - (T(2.) / T(3)) * p1 * q0;
+    c.x6 = p0 * q2 - (T(2.) / T(3)) * p2 * q0;
+    c.x7 = p1 * q0 - (T(2.) / T(3)) * p0 * q1;
+    c.x8 = p1 * q2 - (T(2.) / T(3)) * p2 * q1;
+    c.x9 = p2 * q0 - (T(2.) / T(3)) * p0 * q2;
+    c.x10 = p2 * q1 - (T(2.) / T(3)) * p1 * q2;
+    return c;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const T K = T(d.K), Cv = T(d.Cv), mu_E = T(d.mu_L), Pr_E = T(d.Pr_L);
+    const T invXI = T(1.) / T(d.dXI), invET = T(1.) / T(d.dET), invZT = T(1.) / T(d.dZT);
+    const T inv4XI = T(1.) / (T(4) * T(d.dXI)), inv4ET = T(1.) / (T(4) * T(d.dET)),
+            inv4ZT = T(1.) / (T(4) * T(d.dZT));
+    const size_t q = d.ix(i, j, k), f = d.ix(i - 1, j - 1, k - 1);
+    const vcell<T> c = ld<T>(a, q);
+    const vcell<T> im = ld<T>(a, d.ix(i - 1, j, k)), jm = ld<T>(a, d.ix(i, j - 1, k)),
+                   km = ld<T>(a, d.ix(i, j, k - 1));
+    const vcell<T> ip = ld<T>(a, d.ix(i + 1, j, k)), jp = ld<T>(a, d.ix(i, j + 1, k)),
+                   kp = ld<T>(a, d.ix(i, j, k + 1));
+    const vcell<T> imjp = ld<T>(a, d.ix(i - 1, j + 1, k)), imkp = ld<T>(a, d.ix(i - 1, j, k + 1));
+    const vcell<T> ipjm = ld<T>(a, d.ix(i + 1, j - 1, k)), ipkm = ld<T>(a, d.ix(i + 1, j, k - 1));
+    const vcell<T> jmkp = ld<T>(a, d.ix(i, j - 1, k + 1)), jpkm = ld<T>(a, d.ix(i, j + 1, k - 1));
+    const vcell<T> imjm = ld<T>(a, d.ix(i - 1, j - 1, k)), jmkm = ld<T>(a, d.ix(i, j - 1, k - 1)),
+                   imkm = ld<T>(a, d.ix(i - 1, j, k - 1));
+
+    // ---- x face (Viscous_terms.cpp:398-547) ----
+    {
+        vgrad<T> X = g2<T>(c, im, invXI);
+        vgrad<T> Y = g4<T>(jp, imjp, jm, imjm, imjp, inv4ET);
+        vgrad<T> Z = g4<T>(kp, imkp, km, imkm, imkp, inv4ZT);
+        const double *const *m = a.mf[0];
+        T m0 = T(m[0][f]), m1 = T(m[1][f]), m2 = T(m[2][f]);
+        vsym<T> A = csym<T>(m0, m1, m2);
+        vcross<T> D = ccross<T>(m0, m1, m2, T(m[3][f]), T(m[4][f]), T(m[5][f]));
+        vcross<T> E = ccross<T>(m0, m1, m2, T(m[6][f]), T(m[7][f]), T(m[8][f]));
+        T Ux = T(0.5) * (c.u + im.u), Vx = T(0.5) * (c.v + im.v), Wx = T(0.5) * (c.w + im.w);
+        T Jf = T(a.Jf[0][f]);
+        a.LL[0][q] = double(mu_E * (A.s1 * X.du + A.s5 * X.dv + A.s7 * X.dw + D.x1 * Y.du + D.x7 * Y.dv + D.x9 * Y.dw + E.x1 * Z.du + E.x7 * Z.dv + E.x9 * Z.dw) / Jf);
+        a.LL[1][q] = double(mu_E * (A.s5 * X.du + A.s2 * X.dv + A.s6 * X.dw + D.x5 * Y.du + D.x2 * Y.dv + D.x10 * Y.dw + E.x5 * Z.du + E.x2 * Z.dv + E.x10 * Z.dw) / Jf);
+        a.LL[2][q] = double(mu_E * (A.s7 * X.du + A.s6 * X.dv + A.s3 * X.dw + D.x6 * Y.du + D.x8 * Y.dv + D.x3 * Y.dw + E.x6 * Z.du + E.x8 * Z.dv + E.x3 * Z.dw) / Jf);
+        a.LL[3][q] = double(mu_E * (T(0.5) * A.s1 * X.du2 + T(0.5) * A.s2 * X.dv2 + T(0.5) * A.s3 * X.dw2 + A.s5 * X.duv + A.s6 * X.dvw + A.s7 * X.duw + Cv * K * A.s4 * X.dT / (Pr_E) +
+            T(0.5) * D.x1 * Y.du2 + T(0.5) * D.x2 * Y.dv2 + T(0.5) * D.x3 * Y.dw2 + D.x5 * Vx * Y.du + D.x6 * Wx * Y.du + D.x7 * Ux * Y.dv + D.x8 * Wx * Y.dv + D.x9 * Ux * Y.dw + D.x10 * Vx * Y.dw + Cv * K * D.x4 * Y.dT / (Pr_E) +
+            T(0.5) * E.x1 * Z.du2 + T(0.5) * E.x2 * Z.dv2 + T(0.5) * E.x3 * Z.dw2 + E.x5 * Vx * Z.du + E.x6 * Wx * Z.du + E.x7 * Ux * Z.dv + E.x8 * Wx * Z.dv + E.x9 * Ux * Z.dw + E.x10 * Vx * Z.dw + Cv * K * E.x4 * Z.dT / (Pr_E)) / Jf);
+    }
+    // ---- y face (Viscous_terms.cpp:550-695) ----
+    {
+        vgrad<T> X = g4<T>(ip, ipjm, im, imjm, ipjm, inv4XI);
+        vgrad<T> Y = g2<T>(c, jm, invET);
+        vgrad<T> Z = g4<T>(kp, jmkp, km, jmkm, jmkp, inv4ZT);
+        const double *const *m = a.mf[1];
+        T m0 = T(m[0][f]), m1 = T(m[1][f]), m2 = T(m[2][f]);
+        T e0 = T(m[3][f]), e1 = T(m[4][f]), e2 = T(m[5][f]);
+        vsym<T> B = csym<T>(e0, e1, e2);
+        vcross<T> D = ccross<T>(m0, m1, m2, e0, e1, e2);
+        vcross<T> F = ccross<T>(e0, e1, e2, T(m[6][f]), T(m[7][f]), T(m[8][f]));
+        T Uy = T(0.5) * (c.u + jm.u), Vy = T(0.5) * (c.v + jm.v), Wy = T(0.5) * (c.w + jm.w);
+        T Jf = T(a.Jf[1][f]);
+        a.ML[0][q] = double(mu_E * (D.x1 * X.du + D.x5 * X.dv + D.x6 * X.dw + B.s1 * Y.du + B.s5 * Y.dv + B.s7 * Y.dw + F.x1 * Z.du + F.x7 * Z.dv + F.x9 * Z.dw) / Jf);
+        a.ML[1][q] = double(mu_E * (D.x7 * X.du + D.x2 * X.dv + D.x8 * X.dw + B.s5 * Y.du + B.s2 * Y.dv + B.s6 * Y.dw + F.x5 * Z.du + F.x2 * Z.dv + F.x10 * Z.dw) / Jf);
+        a.ML[2][q] = double(mu_E * (D.x9 * X.du + D.x10 * X.dv + D.x3 * X.dw + B.s7 * Y.du + B.s6 * Y.dv + B.s3 * Y.dw + F.x6 * Z.du + F.x8 * Z.dv + F.x3 * Z.dw) / Jf);
+        a.ML[3][q] = double(mu_E * (T(0.5) * B.s1 * Y.du2 + T(0.5) * B.s2 * Y.dv2 + T(0.5) * B.s3 * Y.dw2 + B.s5 * Y.duv + B.s6 * Y.dvw + B.s7 * Y.duw + Cv * K * B.s4 * Y.dT / (Pr_E) +
+            T(0.5) * D.x1 * X.du2 + T(0.5) * D.x2 * X.dv2 + T(0.5) * D.x3 * X.dw2 + D.x5 * Uy * X.dv + D.x6 * Uy * X.dw + D.x7 * Vy * X.du + D.x8 * Vy * X.dw + D.x9 * Wy * X.du + D.x10 * Wy * X.dv + Cv * K * D.x4 * X.dT / (Pr_E) +
+            T(0.5) * F.x1 * Z.du2 + T(0.5) * F.x2 * Z.dv2 + T(0.5) * F.x3 * Z.dw2 + F.x5 * Vy * Z.du + F.x6 * Wy * Z.du + F.x7 * Uy * Z.dv + F.x8 * Wy * Z.dv + F.x9 * Uy * Z.dw + F.x10 * Vy * Z.dw + Cv * K * F.x4 * Z.dT / (Pr_E)) / Jf);
+    }
+    // ---- z face (Viscous_terms.cpp:698-841) ----
+    {
+        vgrad<T> X = g4<T>(ip, ipkm, im, imkm, ipkm, inv4XI);
+        vgrad<T> Y = g4<T>(jp, jpkm, jm, jmkm, imjp, inv4ET);
+        vgrad<T> Z = g2<T>(c, km, invZT);
+        const double *const *m = a.mf[2];
+        T z0 = T(m[6][f]), z1 = T(m[7][f]), z2 = T(m[8][f]);
+        vsym<T> Cc = csym<T>(z0, z1, z2);
+        vcross<T> E = ccross<T>(T(m[0][f]), T(m[1][f]), T(m[2][f]), z0, z1, z2);
+        vcross<T> F = ccross<T>(T(m[3][f]), T(m[4][f]), T(m[5][f]), z0, z1, z2);
+        T Uz = T(0.5) * (c.u + km.u), Vz = T(0.5) * (c.v + km.v), Wz = T(0.5) * (c.w + km.w);
+        T Jf = T(a.Jf[2][f]);
+        a.NL[0][q] = double(mu_E * (E.x1 * X.du + E.x5 * X.dv + E.x6 * X.dw + F.x1 * Y.du + F.x5 * Y.dv + F.x6 * Y.dw + Cc.s1 * Z.du + Cc.s5 * Z.dv + Cc.s7 * Z.dw) / Jf);
+        a.NL[1][q] = double(mu_E * (E.x7 * X.du + E.x2 * X.dv + E.x8 * X.dw + F.x7 * Y.du + F.x2 * Y.dv + F.x8 * Y.dw + Cc.s5 * Z.du + Cc.s2 * Z.dv + Cc.s6 * Z.dw) / Jf);
+        a.NL[2][q] = double(mu_E * (E.x9 * X.du + E.x10 * X.dv + E.x3 * X.dw + F.x9 * Y.du + F.x10 * Y.dv + F.x3 * Y.dw + Cc.s7 * Z.du + Cc.s6 * Z.dv + Cc.s3 * Z.dw) / Jf);
+        a.NL[3][q] = double(mu_E * (T(0.5) * Cc.s1 * Z.du2 + T(0.5) * Cc.s2 * Z.dv2 + T(0.5) * Cc.s3 * Z.dw2 + Cc.s5 * Z.duv + Cc.s6 * Z.dvw + Cc.s7 * Z.duw + Cv * K * Cc.s4 * Z.dT / (Pr_E) +
+            T(0.5) * E.x1 * X.du2 + T(0.5) * E.x2 * X.dv2 + T(0.5) * E.x3 * X.dw2 + E.x5 * Uz * X.dv + E.x6 * Uz * X.dw + E.x7 * Vz * X.du + E.x8 * Vz * X.dw + E.x9 * Wz * X.du + E.x10 * Wz * X.dv + Cv * K * E.x4 * X.dT / (Pr_E) +
+            T(0.5) * F.x1 * Y.du2 + T(0.5) * F.x2 * Y.dv2 + T(0.5) * F.x3 * Y.dw2 + F.x5 * Uz * Y.dv + F.x6 * Uz * Y.dw + F.x7 * Vz * Y.du + F.x8 * Vz * Y.dw + F.x9 * Wz * Y.du + F.x10 * Wz * Y.dv + Cv * K * F.x4 * Y.dT / (Pr_E)) / Jf);
+    }
+}
+
+// Viscous_terms.cpp:854-883
+template <typename T>
+__global__ void k_visc_div(cf_dims d, cf_visc_args a, cf_box b)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const T invXI = T(1.) / T(d.dXI), invET = T(1.) / T(d.dET), invZT = T(1.) / T(d.dZT);
+    const size_t q = d.ix(i, j, k), qi = d.ix(i + 1, j, k), qj = d.ix(i, j + 1, k), qk = q + 1;
+#pragma unroll
+    for (int v = 0; v < 4; v++)
+        a.vF[v][q] = double((T(a.LL[v][qi]) - T(a.LL[v][q])) * invXI + (T(a.ML[v][qj]) - T(a.ML[v][q])) * invET +
+                            (T(a.NL[v][qk]) - T(a.NL[v][q])) * invZT);
+}
+
+template <typename T>
+cudaError_t launch_viscous(const cf_dims &d, const cf_visc_args &a, cudaStream_t s)
+{
+    const size_t n = d.total();
+    k_visc_prim<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
+    cf_box bf = make_box(3, d.gend + 1, 2, d.ny + 1, 2, d.nz + 1);
+    k_visc_faces<T><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+    cf_box bd = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    k_visc_div<T><<<box_grid(bd), box_block(), 0, s>>>(d, a, bd);
+    return cudaGetLastError();
+}
+
+}  // namespace CF_NS

@@ -1,0 +1,190 @@
+/*
+ * channel_flow_gb300: C ABI of the GB300 (sm_103a) implementation of the
+ * channel-flow solver's per-step hot path.
+ *
+ * Each routine entry point replaces one free function of the reference
+ * solver (ricklee209/Channel_Flow, prototypes in main.h) and keeps its
+ * argument order and meaning: the reference passes `double (*)[Y_m][Z_m]`
+ * rows, here every field is a plain `double *` to X_np*Y_m*Z_m contiguous
+ * doubles (z fastest, X_np = X_out+6, Y_m = Y_out+4, Z_m = Z_out+4), the
+ * reference's single-rank layout (Array.h:7).  Scalars keep their meaning.
+ *
+ * Field pointers are either device pointers or host arrays registered with
+ * cf_register() (the routine then works on the registered device mirror;
+ * cf_upload()/cf_download() move the data at IO points).  All work is
+ * queued on the context's stream; routines that return scalars (the
+ * residual norms) synchronise that stream.
+ *
+ * Every function returns CF_OK or an error code; cf_last_error() gives the
+ * message.  The reference's routines return void and check nothing.
+ *
+ * A context is not thread-safe: one host thread drives one context, as one
+ * MPI rank drives its routines in the reference.
+ */
+#ifndef CHANNEL_FLOW_GB300_H
+#define CHANNEL_FLOW_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CF_OK 0
+#define CF_ERR_ARG 1         /* bad argument, unknown pointer, grid too small */
+#define CF_ERR_CUDA 2        /* a CUDA call failed (message in cf_last_error) */
+#define CF_ERR_NONFINITE 3   /* cf_check_finite found a NaN or Inf */
+#define CF_ERR_NOMEM 4       /* device allocation failed */
+#define CF_ERR_STATE 5       /* call out of order (e.g. sweep before Hyperplane) */
+
+/* arithmetic modes of the flux, viscous, filter and LU-SGS kernels */
+#define CF_PREC_FP64_EXACT 0 /* FP64, no fused multiply-add: equals the reference bit for bit */
+#define CF_PREC_FP64 1       /* FP64 with fused multiply-add (within 1e-12 of the reference) */
+#define CF_PREC_FP32 2       /* FP32 kernels, FP64 state update and norms */
+
+typedef struct cf_ctx cf_ctx;
+
+/* Grid and constants.  The reference fixes these at compile time:
+ * Resolution.h (X_out, Y_out, Z_out, deltaXI, deltaET, deltaZT), prm.h
+ * (K = 1.4, R = 287, e = 1e-4, f = 599.29876710, high = 0.005) and
+ * Viscous_terms.h (Cv = 717.5, mu_L = 1.85e-5, Pr_L = 0.72). */
+typedef struct {
+    int X_out, Y_out, Z_out;
+    double deltaXI, deltaET, deltaZT;
+    double K, R, e, Cv, mu_L, Pr_L, f, high;
+} cf_grid;
+
+/* ------------------------------------------------------------------ */
+/* context                                                              */
+/* ------------------------------------------------------------------ */
+
+/* Fill g with the reference's constants and its 4*pi*h x 2h x 2*pi*h
+ * domain for the given cell counts. */
+int cf_grid_reference(cf_grid *g, int X_out, int Y_out, int Z_out);
+
+/* Create a context on the current CUDA device.  Each extent must be >= 6. */
+int cf_create(const cf_grid *g, int precision, cf_ctx **out);
+void cf_destroy(cf_ctx *ctx);
+int cf_set_precision(cf_ctx *ctx, int precision);
+int cf_set_stream(cf_ctx *ctx, void *cuda_stream); /* cudaStream_t; NULL = legacy default */
+/* Wall-normal stretching parameter of the analytic metrics (Jacobian_u/v/w):
+ * the reference hard-codes 1.5 (Jacobian_u.cpp:19). */
+int cf_set_stretching(cf_ctx *ctx, double gamma);
+int cf_synchronize(cf_ctx *ctx);
+const char *cf_last_error(const cf_ctx *ctx);
+const char *cf_error_string(int code);
+size_t cf_field_count(const cf_ctx *ctx); /* doubles per field: X_np*Y_m*Z_m */
+int cf_library_version(void);
+
+/* ------------------------------------------------------------------ */
+/* host arrays and device mirrors                                        */
+/* ------------------------------------------------------------------ */
+int cf_register(cf_ctx *ctx, double *host);   /* allocate the device mirror of one field */
+int cf_unregister(cf_ctx *ctx, double *host);
+int cf_upload(cf_ctx *ctx, const double *host);
+int cf_download(cf_ctx *ctx, double *host);
+double *cf_device_ptr(cf_ctx *ctx, const double *host_or_device);
+
+/* 0 if every interior value of the field is finite, else CF_ERR_NONFINITE
+ * (synchronises the stream). */
+int cf_check_finite(cf_ctx *ctx, const double *field);
+
+/* ------------------------------------------------------------------ */
+/* boundary conditions                                                  */
+/* ------------------------------------------------------------------ */
+
+/* replaces Y_boundary_condition (Y_boundary_condition.cpp:14) */
+int cf_Y_boundary_condition(cf_ctx *ctx, int myid, double *U1_, double *U2_, double *U3_,
+                            double *U4_, double *U5_, double *J);
+/* replaces Z_boundary_condition (Z_boundary_condition.cpp:15) */
+int cf_Z_boundary_condition(cf_ctx *ctx, int myid, double *U1_, double *U2_, double *U3_,
+                            double *U4_, double *U5_, double *J);
+/* replaces the x halo exchange and periodic seam of the step loop
+ * (main.cpp:156-244): fills the three ghost planes on each side with the
+ * periodic image of the interior */
+int cf_X_periodic(cf_ctx *ctx, int myid, double *U1_, double *U2_, double *U3_, double *U4_,
+                  double *U5_);
+
+/* ------------------------------------------------------------------ */
+/* inviscid fluxes                                                      */
+/* ------------------------------------------------------------------ */
+/* All six take the reference's 32 arrays: U1_..U5_, MR1..MR5, ML1..ML5
+ * (reference scratch; not touched here), J, the face Jacobian, the nine face
+ * metrics, the five face fluxes inF1..inF5 (written) and the sensor Ep (read
+ * by the limited fluxes only). */
+#define CF_FLUX_ARRAYS                                                                          \
+    double *U1_, double *U2_, double *U3_, double *U4_, double *U5_, double *MR1, double *MR2,  \
+        double *MR3, double *MR4, double *MR5, double *ML1, double *ML2, double *ML3,            \
+        double *ML4, double *ML5, double *J, double *J_f, double *xidx_f, double *xidy_f,        \
+        double *xidz_f, double *etdx_f, double *etdy_f, double *etdz_f, double *ztdx_f,          \
+        double *ztdy_f, double *ztdz_f, double *inF1, double *inF2, double *inF3, double *inF4,  \
+        double *inF5, double *Ep
+
+/* replaces Flux_X_limiter (Flux_X_limiter.cpp:17) */
+int cf_Flux_X_limiter(cf_ctx *ctx, int myid, CF_FLUX_ARRAYS);
+/* replaces Flux_Y_limiter (Flux_Y_limiter.cpp:16) */
+int cf_Flux_Y_limiter(cf_ctx *ctx, int myid, CF_FLUX_ARRAYS);
+/* replaces Flux_Z_limiter (Flux_Z_limiter.cpp:16) */
+int cf_Flux_Z_limiter(cf_ctx *ctx, int myid, CF_FLUX_ARRAYS);
+/* replace Flux_X / Flux_Y / Flux_Z (Flux_X.cpp:18, Flux_Y.cpp:17, Flux_Z.cpp:17) */
+int cf_Flux_X(cf_ctx *ctx, int myid, CF_FLUX_ARRAYS);
+int cf_Flux_Y(cf_ctx *ctx, int myid, CF_FLUX_ARRAYS);
+int cf_Flux_Z(cf_ctx *ctx, int myid, CF_FLUX_ARRAYS);
+
+/* ------------------------------------------------------------------ */
+/* viscous terms and sensor                                             */
+/* ------------------------------------------------------------------ */
+
+/* replaces Viscous_terms (Viscous_terms.cpp:15): 79 arrays U1_..U5_,
+ * vF2..vF5, J, 9 cell metrics, J_u + 9, J_v + 9, J_w + 9, then the scratch
+ * LR1..5, LL1..5, MR1..5, ML1..5, NR1..5, NL1..5 (LL2..5, ML2..5, NL2..5
+ * receive the face fluxes as in the reference) */
+int cf_Viscous_terms(cf_ctx *ctx, int myid, double **arrays79);
+
+/* replaces Filter (Filter.cpp:12): U1_..U5_, Y_point, EpX, EpY, EpZ, J */
+int cf_Filter(cf_ctx *ctx, int myid, double Roe_criterion, double E_high, double E_low,
+              double *U1_, double *U2_, double *U3_, double *U4_, double *U5_, double *Y_point,
+              double *EpX, double *EpY, double *EpZ, double *J);
+
+/* ------------------------------------------------------------------ */
+/* time integration                                                     */
+/* ------------------------------------------------------------------ */
+
+/* replaces RK3NODT (RK3NODT.cpp:18): 49 arrays U1_..5, U1..5, U1q..5, J,
+ * 9 cell metrics, inFx1..5, inFy1..5, inFz1..5, vF2..5, MR1..5; er1..er5
+ * are not written (as in the reference) */
+int cf_RK3NODT(cf_ctx *ctx, int myid, int RK, double deltaT, double *er1, double *er2,
+               double *er3, double *er4, double *er5, double **arrays49);
+
+/* replaces Hyperplane (Hyperplane.cpp:18): fills the host plane tables
+ * Nijk[(X_np-3)+ny+nz+7][2] and ijk[(X_np-6)*Y_out*Z_out*3][3] and keeps a
+ * device copy for the sweeps */
+int cf_Hyperplane(cf_ctx *ctx, int myid, int *Nijk, int *ijk);
+
+/* replaces Dual_time_stepping (Dual_time_stepping.cpp:18): 64 arrays as
+ * RK3NODT plus NR1..5, NL1..5, Residual1..5; writes er1..er5 */
+int cf_Dual_time_stepping(cf_ctx *ctx, int myid, double deltaT, double *er1, double *er2,
+                          double *er3, double *er4, double *er5, int *Nijk, int *ijk,
+                          double **arrays64);
+
+/* replaces DPLUSGS (DPLUSGS.cpp:18): same arrays, 4 Jacobi sweeps */
+int cf_DPLUSGS(cf_ctx *ctx, int myid, double deltaT, double *er1, double *er2, double *er3,
+               double *er4, double *er5, double **arrays64);
+
+/* ------------------------------------------------------------------ */
+/* face metrics                                                         */
+/* ------------------------------------------------------------------ */
+/* replace Jacobian_u / Jacobian_w (Jacobian_u.cpp:15, Jacobian_w.cpp:14):
+ * J_f then xidx_f..ztdz_f (10 arrays) */
+int cf_Jacobian_u(cf_ctx *ctx, int myid, double **arrays10);
+int cf_Jacobian_w(cf_ctx *ctx, int myid, double **arrays10);
+/* replaces Jacobian_v (Jacobian_v.cpp:17): J_v + 9 face metrics, then J +
+ * 9 cell metrics (read for the wall rows) */
+int cf_Jacobian_v(cf_ctx *ctx, int myid, double **arrays20);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

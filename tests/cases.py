@@ -5,8 +5,15 @@ routine's argument order (main.h), filled with a seeded channel state,
 perturbed curvilinear metrics and random (but identical) initial contents of
 the output and scratch arrays, so that two implementations handed copies of
 the same list can be compared array by array.
+
+Inputs are built from the seeded PCG64 generator and IEEE-exact arithmetic
+(+, -, *, /, sqrt) only, so every machine regenerates them bit for bit; the
+golden fixtures can therefore store hashes of the reference's outputs.
 """
 from __future__ import annotations
+
+import hashlib
+import math
 
 import numpy as np
 
@@ -15,6 +22,10 @@ from channel_flow_gb300 import synthetic as syn
 # test grids (X_out, Y_out, Z_out): the second one has Z_out > Y_out + 1 so
 # that Flux_Z_limiter takes its 3rd-order branch for k >= ny
 GRIDS = [(12, 10, 8), (8, 6, 12), (16, 12, 10)]
+GOLDEN_GRID = (6, 6, 8)
+DELTA_T = 0.00000005                       # main.cpp:53
+FILTER_ARGS = (0.007, 1.0, 0.0)            # Roe_criterion, E_high, E_low (main.cpp:55-57)
+METRIC_NAMES = syn.METRIC_NAMES
 
 
 def grid(dims):
@@ -25,14 +36,75 @@ def _rand_like(g, rng, scale=1.0):
     return scale * rng.uniform(-1, 1, g.shape)
 
 
+def _eta(g, joff):
+    """normalised wall-normal position of row j (0 at the lower wall)"""
+    j = np.arange(g.shape[1], dtype=np.float64)
+    return (j - joff) * g.deltaET
+
+
 def metric_set(g, where, seed, perturb=0.02):
-    m = syn.flat_metrics(g, 1.5, where, perturb=perturb, seed=seed)
-    return [m["J"]] + [m[n] for n in syn.METRIC_NAMES]
+    """J and nine metrics of a stretched flat channel (arithmetic stand-in for
+    the tanh stretching: dy/deta = high*(0.25 + 4.5 eta (1 - eta))), plus
+    seeded relative noise on all ten arrays and noise-filled cross terms."""
+    joff = {"cell": 1.5, "u": 0.5, "v": 1.0, "w": 0.5}[where]
+    eta = _eta(g, joff)
+    ydet = g.high * (0.25 + 4.5 * eta * (1 - eta))
+    etdy1 = 1.0 / ydet
+    rng = np.random.default_rng(seed)
+    J = np.broadcast_to((1.0 / ydet)[None, :, None], g.shape).copy()
+    m = {n: np.zeros(g.shape) for n in METRIC_NAMES}
+    m["xidx"][:] = 1.0
+    m["etdy"][:] = etdy1[None, :, None]
+    m["ztdz"][:] = 1.0
+    if perturb > 0:
+        scale = {"xi": 1.0, "et": float(np.max(etdy1)), "zt": 1.0}
+        for n in METRIC_NAMES:
+            m[n] *= 1 + perturb * rng.uniform(-1, 1, g.shape)
+            m[n] += perturb * scale[n[:2]] * rng.uniform(-1, 1, g.shape)
+        J *= 1 + perturb * rng.uniform(-1, 1, g.shape)
+    return [J] + [m[n] for n in METRIC_NAMES]
 
 
-def state(g, seed):
-    J = syn.flat_metrics(g, 1.5, "cell", perturb=0.02, seed=seed + 1000)["J"]
-    return syn.channel_state(g, J, seed=seed), J
+def y_points(g):
+    """monotone wall distance with the ghost rule of Grid.cpp:86-108"""
+    eta = _eta(g, 1.5)
+    yp = 0.5 * g.high * eta * eta * (3 - 2 * eta) + 0.01 * g.high * eta
+    ny = g.ny
+    yp[1] = -yp[2]
+    yp[ny + 1] = yp[ny] + 2 * yp[2]
+    yp[0] = 2 * yp[1] - yp[2]
+    yp[ny + 2] = 2 * yp[ny + 1] - yp[ny]
+    return np.broadcast_to(yp[None, :, None], g.shape).copy()
+
+
+def state(g, seed, mach=0.5, noise=0.05, jitter=0.01):
+    """seeded conserved state U/J and the cell Jacobian J"""
+    J = metric_set(g, "cell", seed + 1000)[0]
+    rng = np.random.default_rng(seed)
+    ub = mach * math.sqrt(g.K * g.R * syn.T_WALL)
+    eta = np.clip(_eta(g, 1.5), 0.0, 1.0)
+    prof = 1.5 * ub * (1 - (2 * eta - 1) ** 2)
+    rho = syn.RHO_REF * (1 + jitter * rng.uniform(-1, 1, g.shape))
+    T = syn.T_WALL * (1 + jitter * rng.uniform(-1, 1, g.shape))
+    u = prof[None, :, None] + noise * ub * rng.uniform(-1, 1, g.shape)
+    v = noise * ub * rng.uniform(-1, 1, g.shape)
+    w = noise * ub * rng.uniform(-1, 1, g.shape)
+    p = rho * g.R * T
+    E = p / (g.K - 1) + 0.5 * rho * (u * u + v * v + w * w)
+    return [np.ascontiguousarray(x / J) for x in (rho, rho * u, rho * v, rho * w, E)], J
+
+
+def copy_case(arrays):
+    return [np.array(a, copy=True) for a in arrays]
+
+
+# --------------------------------------------------------------------------
+# per-routine argument lists
+
+def bc_case(g, seed=0):
+    """6 arrays: U1_..U5_, J"""
+    U, J = state(g, seed)
+    return U + [J]
 
 
 def flux_case(g, direction, seed=0, ep_values=(0.0, 0.5, 1.0)):
@@ -45,10 +117,6 @@ def flux_case(g, direction, seed=0, ep_values=(0.0, 0.5, 1.0)):
     F = [_rand_like(g, rng) for _ in range(5)]
     Ep = rng.choice(np.asarray(ep_values, dtype=np.float64), size=g.shape)
     return U + MR + ML + [J] + fm + F + [Ep]
-
-
-def copy_case(arrays):
-    return [np.array(a, copy=True) for a in arrays]
 
 
 def viscous_case(g, seed=0):
@@ -68,21 +136,14 @@ def filter_case(g, seed=0):
     """10 arrays in Filter's order: U1_..5, Y_point, EpX, EpY, EpZ, J."""
     rng = np.random.default_rng(seed + 9)
     U, J = state(g, seed)
-    Yp = syn.y_points(g)
-    return U + [Yp] + [_rand_like(g, rng) for _ in range(3)] + [J]
-
-
-FILTER_ARGS = (0.007, 1.0, 0.0)   # Roe_criterion, E_high, E_low (main.cpp:55-57)
-
-
-DELTA_T = 0.00000005   # main.cpp:53
+    return U + [y_points(g)] + [_rand_like(g, rng) for _ in range(3)] + [J]
 
 
 def dt_case(g, seed=0, nslots=64):
     """Dual-time / RK3 signature (main.h:653): U1_..5, U1..5, U1q..5, J,
     9 cell metrics, inFx/y/z 1..5, vF2..5, MR1..5 [, NR1..5, NL1..5,
     Residual1..5].  U and Uq are the state with 1e-6 relative noise, the
-    fluxes O(1) with 5 % noise."""
+    fluxes of realistic magnitude with 5 % noise."""
     rng = np.random.default_rng(seed + 13)
     U_, J = state(g, seed)
     U = [x * (1 + 1e-6 * rng.uniform(-1, 1, g.shape)) for x in U_]
@@ -95,3 +156,46 @@ def dt_case(g, seed=0, nslots=64):
     out = U_ + U + Uq + [J] + cm + Fx + Fy + Fz + vF
     out += [_rand_like(g, rng) for _ in range(nslots - len(out))]
     return out
+
+
+def jacobian_case(g, which, seed=0):
+    """10 face arrays (J_f + 9), random initial content; Jacobian_v also
+    gets J + 9 cell metrics"""
+    rng = np.random.default_rng(seed + 17)
+    out = [rng.uniform(0.5, 1.5, g.shape) for _ in range(10)]
+    if which == "v":
+        out += metric_set(g, "cell", seed + 23)
+    return out
+
+
+# --------------------------------------------------------------------------
+# which arrays each routine writes (slots compared by the tests)
+
+FLUX_OUT = list(range(26, 31))
+VISC_OUT = [5, 6, 7, 8] + [55, 56, 57, 58, 65, 66, 67, 68, 75, 76, 77, 78]
+FILTER_OUT = [6, 7, 8]
+RK3_OUT = list(range(0, 5)) + list(range(44, 49))
+LU_OUT = list(range(0, 5)) + list(range(44, 64))
+BC_OUT = list(range(0, 5))
+JAC_OUT = list(range(0, 10))
+
+
+def ylim_undefined_mask(g, slot):
+    """Entries of Flux_Y_limiter's outputs that depend on the reference's
+    uninitialised jL/jR (Flux_Y_limiter.cpp:120-232): face fluxes at faces
+    j = 2, ny-2, ny-1 (all five variables) and at the wall faces 1 and ny
+    (the normal-momentum flux, the only one not set to zero there)."""
+    m = np.zeros(g.shape, dtype=bool)
+    ny = g.ny
+    if slot in FLUX_OUT:
+        rows = [2, ny - 2, ny - 1] + ([1, ny] if slot == 28 else [])
+        for j in rows:
+            m[:, j, :] = True
+    return m
+
+
+def digest(a, mask=None):
+    a = np.array(a, dtype=np.float64, copy=True)
+    if mask is not None:
+        a[mask] = 0.0
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()[:32]

@@ -1,0 +1,57 @@
+"""The C oracle against the reference solver's own routines (compiled from
+the reference sources by oracle/build_ref.py): equal bit for bit on every
+written array, except the Flux_Y_limiter faces that depend on the
+reference's uninitialised jL/jR.  Runs where the reference checkout exists."""
+import numpy as np
+import pytest
+
+import cases
+import routines
+from oracle import cforacle
+
+pytestmark = pytest.mark.skipif(not cforacle.reference_available(),
+                                reason="reference sources not present on this machine")
+
+
+@pytest.mark.parametrize("dims", cases.GRIDS)
+@pytest.mark.parametrize("name", [r.name for r in routines.ROUTINES])
+def test_port_equals_reference(dims, name, port):
+    r = routines.BY_NAME[name]
+    g = cases.grid(dims)
+    ref = cforacle.Reference(g)
+    a = r.build(g, 3)
+    want, got = cases.copy_case(a), cases.copy_case(a)
+    e_ref = routines.run_cpu(ref, r, g, want)
+    e_port = routines.run_cpu(port, r, g, got)
+    diff = routines.compare(r, g, got, want)
+    assert all(v == 0 for v in diff.values()), f"{name} mismatching entries per slot: {diff}"
+    # everything the routine does not write stays as it was
+    for i in range(len(a)):
+        if i not in r.outputs and not (name.startswith("Flux") and 5 <= i < 15) \
+                and not (name == "Viscous_terms" and i >= 49) and not (name == "Y_boundary_condition"):
+            assert np.array_equal(got[i], a[i], equal_nan=True), f"{name} modified input slot {i}"
+    if r.scalars:
+        assert np.array_equal(e_ref, e_port), (e_ref, e_port)
+
+
+def test_flux_y_limiter_differs_only_where_reference_is_undefined(port):
+    """The unmasked comparison differs only inside the documented mask."""
+    r = routines.BY_NAME["Flux_Y_limiter"]
+    g = cases.grid(cases.GRIDS[0])
+    ref = cforacle.Reference(g)
+    a = r.build(g, 5)
+    want, got = cases.copy_case(a), cases.copy_case(a)
+    routines.run_cpu(ref, r, g, want)
+    routines.run_cpu(port, r, g, got)
+    for i in r.outputs:
+        bad = got[i] != want[i]
+        assert not np.any(bad & ~cases.ylim_undefined_mask(g, i))
+
+
+def test_hyperplane_tables_equal(port):
+    for dims in cases.GRIDS:
+        g = cases.grid(dims)
+        ref = cforacle.Reference(g)
+        n1, i1 = ref.Hyperplane(g)
+        n2, i2 = port.Hyperplane(g)
+        assert np.array_equal(n1, n2) and np.array_equal(i1, i2)
