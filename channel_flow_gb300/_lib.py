@@ -16,11 +16,11 @@ PREC = {"fp64_exact": 0, "fp64": 1, "fp32": 2}
 
 
 class cf_grid(C.Structure):
-    _fields_ = [("X_out", C.c_int), ("Y_out", C.c_int), ("Z_out", C.c_int),
-                ("deltaXI", C.c_double), ("deltaET", C.c_double), ("deltaZT", C.c_double),
-                ("K", C.c_double), ("R", C.c_double), ("e", C.c_double),
-                ("Cv", C.c_double), ("mu_L", C.c_double), ("Pr_L", C.c_double),
-                ("f", C.c_double), ("high", C.c_double)]
+    _fields_ = [("cells_x", C.c_int), ("cells_y", C.c_int), ("cells_z", C.c_int),
+                ("d_xi", C.c_double), ("d_eta", C.c_double), ("d_zeta", C.c_double),
+                ("gamma_gas", C.c_double), ("r_gas", C.c_double), ("beta_min", C.c_double),
+                ("cv", C.c_double), ("mu", C.c_double), ("prandtl", C.c_double),
+                ("body_force", C.c_double), ("height", C.c_double)]
 
 
 class CFError(RuntimeError):

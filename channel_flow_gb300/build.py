@@ -69,7 +69,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
             raise RuntimeError(f"nvcc failed ({src} {' '.join(extra)}):\n{r.stderr[-6000:]}")
         return r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         logs = list(ex.map(cc, units))
     if verbose or ptxas:
         for log in logs:

@@ -147,18 +147,18 @@ const char *cf_error_string(int code)
 
 const char *cf_last_error(const cf_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
-int cf_grid_reference(cf_grid *g, int X_out, int Y_out, int Z_out)
+int cf_grid_reference(cf_grid *g, int cells_x, int cells_y, int cells_z)
 {
     if (!g) return CF_ERR_ARG;
     const double h = 0.5 * 0.005;
     const double pi = 3.14159265358979323846;
-    g->X_out = X_out; g->Y_out = Y_out; g->Z_out = Z_out;
-    g->deltaXI = 4 * pi * h / X_out;
-    g->deltaET = 1.0 / Y_out;
-    g->deltaZT = 2 * pi * h / Z_out;
-    g->K = 1.4; g->R = 287; g->e = 0.0001;
-    g->Cv = 717.5; g->mu_L = 0.0000185; g->Pr_L = 0.72;
-    g->f = 599.29876710; g->high = 0.005;
+    g->cells_x = cells_x; g->cells_y = cells_y; g->cells_z = cells_z;
+    g->d_xi = 4 * pi * h / cells_x;
+    g->d_eta = 1.0 / cells_y;
+    g->d_zeta = 2 * pi * h / cells_z;
+    g->gamma_gas = 1.4; g->r_gas = 287; g->beta_min = 0.0001;
+    g->cv = 717.5; g->mu = 0.0000185; g->prandtl = 0.72;
+    g->body_force = 599.29876710; g->height = 0.005;
     return CF_OK;
 }
 
@@ -166,16 +166,16 @@ int cf_create(const cf_grid *g, int precision, cf_ctx **out)
 {
     if (!g || !out) return CF_ERR_ARG;
     *out = nullptr;
-    if (g->X_out < 6 || g->Y_out < 6 || g->Z_out < 6) return CF_ERR_ARG;
+    if (g->cells_x < 6 || g->cells_y < 6 || g->cells_z < 6) return CF_ERR_ARG;
     if (precision < CF_PREC_FP64_EXACT || precision > CF_PREC_FP32) return CF_ERR_ARG;
     cf_ctx *c = new cf_ctx();
     cf_dims &d = c->d;
-    d.X_out = g->X_out; d.Y_out = g->Y_out; d.Z_out = g->Z_out;
-    d.Ym = g->Y_out + 4; d.Zm = g->Z_out + 4;
-    d.gend = g->X_out + 2; d.ny = g->Y_out + 1; d.nz = g->Z_out + 1;
-    d.dXI = g->deltaXI; d.dET = g->deltaET; d.dZT = g->deltaZT;
-    d.K = g->K; d.R = g->R; d.e = g->e; d.Cv = g->Cv; d.mu_L = g->mu_L; d.Pr_L = g->Pr_L;
-    d.f = g->f; d.high = g->high;
+    d.X_out = g->cells_x; d.Y_out = g->cells_y; d.Z_out = g->cells_z;
+    d.Ym = g->cells_y + 4; d.Zm = g->cells_z + 4;
+    d.gend = g->cells_x + 2; d.ny = g->cells_y + 1; d.nz = g->cells_z + 1;
+    d.dXI = g->d_xi; d.dET = g->d_eta; d.dZT = g->d_zeta;
+    d.K = g->gamma_gas; d.R = g->r_gas; d.e = g->beta_min; d.Cv = g->cv; d.mu_L = g->mu; d.Pr_L = g->prandtl;
+    d.f = g->body_force; d.high = g->height;
     c->prec = precision;
     build_tables(c);
     cudaError_t e = cudaMalloc(&c->ijk_dev, c->ijk.size() * sizeof(int));

@@ -46,13 +46,17 @@ extern "C" {
 typedef struct cf_ctx cf_ctx;
 
 /* Grid and constants.  The reference fixes these at compile time:
- * Resolution.h (X_out, Y_out, Z_out, deltaXI, deltaET, deltaZT), prm.h
- * (K = 1.4, R = 287, e = 1e-4, f = 599.29876710, high = 0.005) and
- * Viscous_terms.h (Cv = 717.5, mu_L = 1.85e-5, Pr_L = 0.72). */
+ * Resolution.h (cell counts X_out, Y_out, Z_out and spacings deltaXI,
+ * deltaET, deltaZT), prm.h (K = 1.4, R = 287, e = 1e-4, f = 599.29876710,
+ * high = 0.005) and Viscous_terms.h (Cv = 717.5, mu_L = 1.85e-5,
+ * Pr_L = 0.72).  The field names differ from those macro names so that this
+ * header can be included after the reference's headers. */
 typedef struct {
-    int X_out, Y_out, Z_out;
-    double deltaXI, deltaET, deltaZT;
-    double K, R, e, Cv, mu_L, Pr_L, f, high;
+    int cells_x, cells_y, cells_z;          /* X_out, Y_out, Z_out */
+    double d_xi, d_eta, d_zeta;             /* deltaXI, deltaET, deltaZT */
+    double gamma_gas, r_gas, beta_min;      /* K, R, e */
+    double cv, mu, prandtl;                 /* Cv, mu_L, Pr_L */
+    double body_force, height;              /* f, high */
 } cf_grid;
 
 /* ------------------------------------------------------------------ */
@@ -61,7 +65,7 @@ typedef struct {
 
 /* Fill g with the reference's constants and its 4*pi*h x 2h x 2*pi*h
  * domain for the given cell counts. */
-int cf_grid_reference(cf_grid *g, int X_out, int Y_out, int Z_out);
+int cf_grid_reference(cf_grid *g, int cells_x, int cells_y, int cells_z);
 
 /* Create a context on the current CUDA device.  Each extent must be >= 6. */
 int cf_create(const cf_grid *g, int precision, cf_ctx **out);
