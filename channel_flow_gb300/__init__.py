@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib
 from .synthetic import Grid, channel_grid, reference_grid  # noqa: F401
 
-__all__ = ["Context", "Grid", "channel_grid", "reference_grid", "CFError", "FieldSet"]
+__all__ = ["Context", "Grid", "channel_grid", "reference_grid", "CFError", "FieldSet", "dplusgs_noalloc"]
 CFError = _lib.CFError
 
 
@@ -175,6 +175,27 @@ class Context:
 
     def Jacobian_w(self, *arrays, myid=0):
         self._ok(self.lib.cf_Jacobian_w(self.h, myid, _lib.ptr_array([_ptr(a) for a in arrays])))
+
+
+def dplusgs_noalloc(grid: Grid, deltaT, *arrays, stream=None):
+    """DPLUSGS through the allocation-free entry point (no context, scratch in
+    a fixed file-scope device array): for callers that cannot allocate
+    device memory, e.g. inside a CUDA stream capture.  Returns the residual
+    norms er1..er5."""
+    lib = _lib.load()
+    if len(arrays) != 64:
+        raise ValueError("DPLUSGS takes 64 arrays")
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    g = _lib.cf_grid(grid.X_out, grid.Y_out, grid.Z_out, grid.deltaXI, grid.deltaET, grid.deltaZT,
+                     grid.K, grid.R, grid.e, grid.Cv, grid.mu_L, grid.Pr_L, grid.f, grid.high)
+    er = np.zeros(5)
+    e = [er[n:].ctypes.data for n in range(5)]
+    rc = lib.cf_DPLUSGS_noalloc(C.byref(g), stream, deltaT, *e, _lib.ptr_array([_ptr(a) for a in arrays]))
+    if rc != _lib.CF_OK:
+        raise CFError(rc, "cf_DPLUSGS_noalloc: " + lib.cf_error_string(rc).decode())
+    return er
 
 
 class FieldSet:

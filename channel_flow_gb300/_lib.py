@@ -60,6 +60,7 @@ _SIGS = {
     "cf_Hyperplane": ([P, C.c_int, P, P], C.c_int),
     "cf_Dual_time_stepping": ([P, C.c_int, C.c_double] + [P] * 5 + [P, P, C.POINTER(P)], C.c_int),
     "cf_DPLUSGS": ([P, C.c_int, C.c_double] + [P] * 5 + [C.POINTER(P)], C.c_int),
+    "cf_DPLUSGS_noalloc": ([C.POINTER(cf_grid), P, C.c_double] + [P] * 5 + [C.POINTER(P)], C.c_int),
     "cf_Jacobian_u": ([P, C.c_int, C.POINTER(P)], C.c_int),
     "cf_Jacobian_v": ([P, C.c_int, C.POINTER(P)], C.c_int),
     "cf_Jacobian_w": ([P, C.c_int, C.POINTER(P)], C.c_int),

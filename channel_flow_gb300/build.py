@@ -7,7 +7,9 @@ Three translation units, compiled in parallel with nvcc:
   bit for bit;
 * ``cf_variant.cu`` as namespace ``cf_fast`` with contraction on and the FP32
   instantiations;
-* ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h).
+* ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h);
+* ``cf_noalloc.cu``: the allocation-free DPLUSGS entry point (its scratch is
+  a file-scope device array).
 
 Usage: ``python -m channel_flow_gb300.build [--verbose] [--ptxas]``
 """
@@ -59,6 +61,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         ("cf_variant.cu", "cf_exact.o", ["-DCF_NS=cf_exact", "--fmad=false"]),
         ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "--fmad=true"]),
         ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
+        ("cf_noalloc.cu", "cf_noalloc.o", ["-DCF_NS=cf_noalloc", "--fmad=false"]),
     ]
 
     def cc(u):

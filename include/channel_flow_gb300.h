@@ -176,6 +176,21 @@ int cf_Dual_time_stepping(cf_ctx *ctx, int myid, double deltaT, double *er1, dou
 int cf_DPLUSGS(cf_ctx *ctx, int myid, double deltaT, double *er1, double *er2, double *er3,
                double *er4, double *er5, double **arrays64);
 
+/* Allocation-free DPLUSGS: no counterpart in the reference.  Same arrays,
+ * arithmetic and results as cf_DPLUSGS in CF_PREC_FP64_EXACT mode, but it
+ * needs no context and calls no cudaMalloc/cudaFree, for callers that may
+ * not allocate device memory (inside a CUDA stream capture, in loops where
+ * an allocation's device-wide synchronisation is unaffordable, under a
+ * memory manager that owns all device memory).  Its only scratch, the
+ * residual-norm partial sums, is a fixed 10 MB file-scope device array per
+ * GPU, so grids needing more than 262144 reduction blocks
+ * (ceil(cells_z/32) * ceil(cells_y/8) * cells_x) are rejected with CF_ERR_ARG.
+ * All calls share that array: calls overlapping on the GPU race.  The first
+ * call on a device looks the array's address up; make it before any stream
+ * capture.  er1..er5 are host pointers; the call synchronises the stream. */
+int cf_DPLUSGS_noalloc(const cf_grid *g, void *cuda_stream, double deltaT, double *er1, double *er2,
+                       double *er3, double *er4, double *er5, double **arrays64);
+
 /* ------------------------------------------------------------------ */
 /* face metrics                                                         */
 /* ------------------------------------------------------------------ */
