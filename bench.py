@@ -42,7 +42,14 @@ FILTER_ARGS = (0.007, 1.0, 0.0)        # Roe_criterion, E_high, E_low (main.cpp:
 # signature read and written once (Filter 7+3, limited fluxes 16/17 + 5,
 # viscous 36 + 4 arrays of 8 bytes)
 ALG_BYTES = {"Filter": 80, "Flux_X_limiter": 168, "Flux_Y_limiter": 176, "Flux_Z_limiter": 176,
-             "Viscous_terms": 320}
+             "Viscous_terms": 320, "Dual_time_stepping": 2680}
+# single-kernel routines eligible as "the dominant kernel" of the roofline
+ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>",
+                "Flux_Z_limiter": "k_flux<2,true,double>"}
+# DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
+# launch on the 96^3 case divided by its cells; profiles/k_flux_z_limiter_96.md)
+NCU_TRAFFIC_PER_CELL = {"Flux_Z_limiter": (82.365440e6 + 13.323008e6) / (96 * 96 * 96)}
+LU_SUBITERATIONS = 10   # LU-SGS sub-iterations per physical step (configs 0 and 1)
 L2_BYTES = 129 * 2 ** 20
 
 
@@ -323,45 +330,41 @@ def main():
     torch.cuda.synchronize()
 
     # timed region: K steps, events around every routine for the roofline
-    names = [c[0] for c in calls]
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(args.steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        t_start = torch.cuda.Event(enable_timing=True)
-        t_end = torch.cuda.Event(enable_timing=True)
-        t_start.record(stream)
-        for s in range(args.steps):
-            for n, (name, fn, a) in enumerate(calls):
-                ev[s][n].record(stream)
-                rc = fn(*a)
-                if rc:
-                    cf._lib.check(ctx.lib, ctx.h, rc)
-            ev[s][len(calls)].record(stream)
-        t_end.record(stream)
-        torch.cuda.synchronize()
-    total_ms = t_start.elapsed_time(t_end)
+        total_ms, per_routine = timed_steps(ctx, calls, args.steps, stream, torch)
     if dist:
         t = torch.tensor([total_ms])
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    per_routine = {nm: 0.0 for nm in names}
-    for s in range(args.steps):
-        for n, nm in enumerate(names):
-            per_routine[nm] += ev[s][n].elapsed_time(ev[s][n + 1]) / args.steps
     ms_per_step = total_ms / args.steps
     value = g.cells * args.steps * world / (total_ms * 1e-3) / 1e6
 
-    # roofline of the dominant routine with a byte model
+    # roofline of the dominant single kernel (the slowest limited flux) with
+    # the byte model; traffic = ncu DRAM bytes per cell x cells
     hbm, peak_kind = peaks()
-    dom = max((nm for nm in names if nm in ALG_BYTES), key=lambda nm: per_routine[nm])
+    dom = max(ROOF_KERNELS, key=lambda nm: per_routine[nm])
     achieved = ALG_BYTES[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "peak_kind": peak_kind,
-            "alg_bytes_per_cell": ALG_BYTES[dom], "traffic": None,
+    traffic = NCU_TRAFFIC_PER_CELL.get(dom)
+    roof = {"bound": "hbm", "kernel": ROOF_KERNELS[dom], "routine": dom, "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
+            "alg_bytes_per_cell": ALG_BYTES[dom], "launch_ms": per_routine[dom],
+            "traffic": traffic * g.cells if traffic else None,
+            "traffic_source": "ncu dram bytes of one launch at 96^3 scaled by cells" if traffic else None,
+            "fp64_pipe_active_pct": 88.1 if dom == "Flux_Z_limiter" else None,
             "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
-            "note": "FP64 on GB300 is DP-pipe bound; the HBM fraction is the byte-model figure"}
+            "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 88% pipe busy, "
+                    "DRAM 0.5%); the HBM fraction is the byte-model figure"}
+
+    # secondary measurements on the same workload: FP32 kernels, and one
+    # dual-time pseudo-iteration (RHS + hyperplane LU-SGS) per precision
+    extra = {}
+    try:
+        extra = secondary(ctx, g, w, calls, stream, torch, args)
+    except Exception as exc:
+        extra = {"error": repr(exc)}
 
     # e2e through the C-ABI with registered host arrays
     e2e = None
@@ -386,7 +389,7 @@ def main():
                 "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.precision != "fp32" else "f32", "data": "synthetic",
-                "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "secondary": extra,
                 "clocks": clocks.summary(), "gpu_launches": LAUNCHES_PER_STEP * args.steps,
                 "parallelism": "replicas" if world > 1 else "single"}
         print(json.dumps(line))
@@ -394,6 +397,84 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def timed_steps(ctx, calls, steps, stream, torch):
+    """K steps bracketed by CUDA events on the context's stream, with an
+    event between every two routine calls; returns (total ms, ms per routine)."""
+    from channel_flow_gb300 import _lib
+    names = [c[0] for c in calls]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(calls) + 1)] for _ in range(steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for s in range(steps):
+        for n, (name, fn, a) in enumerate(calls):
+            ev[s][n].record(stream)
+            rc = fn(*a)
+            if rc:
+                _lib.check(ctx.lib, ctx.h, rc)
+        ev[s][len(calls)].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    per = {nm: 0.0 for nm in names}
+    for s in range(steps):
+        for n, nm in enumerate(names):
+            per[nm] += ev[s][n].elapsed_time(ev[s][n + 1]) / steps
+    return t_start.elapsed_time(t_end), per
+
+
+def secondary(ctx, g, w, calls, stream, torch, args):
+    """FP32 RHS on the same workload, and the dual-time LU-SGS
+    pseudo-iteration (RHS + Dual_time_stepping) in FP64 and FP32."""
+    from channel_flow_gb300 import _lib
+    out = {}
+    steps = max(2, min(args.steps, 5))
+    prec0 = ctx.precision
+    z = lambda: torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    U0 = [u.clone() for u in w.U]
+    Un = [u.clone() for u in w.U]
+    Uq = [u.clone() for u in w.U]
+    lu = [z() for _ in range(20)]          # MR, NR, NL, Residual
+    arrays = w.U + Un + Uq + [w.J] + w.cm + w.Fx + w.Fy + w.Fz + w.vF + lu
+    ptrs = _lib.ptr_array([a.data_ptr() for a in arrays])
+    er = np.zeros(5)
+    e = [er[n:].ctypes.data for n in range(5)]
+    Nijk, ijk = ctx.Hyperplane()
+    dt = 0.00000005
+    for prec in ("fp64", "fp32"):
+        ctx.set_precision(prec)
+        for _ in range(2):
+            run_calls(ctx, calls)
+        torch.cuda.synchronize()
+        tot, per = timed_steps(ctx, calls, steps, stream, torch)
+        rhs_ms = tot / steps
+        # one pseudo-iteration's LU-SGS; the state is restored between calls
+        lu_ms = []
+        for it in range(3):
+            for u, u0 in zip(w.U, U0):
+                u.copy_(u0)
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            rc = ctx.lib.cf_Dual_time_stepping(ctx.h, 0, dt, *e, Nijk.ctypes.data, ijk.ctypes.data, ptrs)
+            t1.record(stream)
+            torch.cuda.synchronize()
+            _lib.check(ctx.lib, ctx.h, rc)
+            if it > 0:
+                lu_ms.append(t0.elapsed_time(t1))
+        for u, u0 in zip(w.U, U0):
+            u.copy_(u0)
+        dts = sum(lu_ms) / len(lu_ms)
+        out[prec] = {"rhs_ms": rhs_ms, "rhs_mcell_updates_per_s": g.cells / (rhs_ms * 1e-3) / 1e6,
+                     "dual_time_lusgs_ms": dts, "pseudo_iteration_ms": rhs_ms + dts,
+                     "physical_step_s": LU_SUBITERATIONS * (rhs_ms + dts) * 1e-3,
+                     "subiterations_per_step": LU_SUBITERATIONS,
+                     "per_routine_ms": {k: round(v, 4) for k, v in per.items()}}
+    ctx.set_precision(prec0)
+    out["note"] = ("physical step = 10 LU-SGS sub-iterations x (RHS + Dual_time_stepping), the schedule of "
+                   "configs 0 and 1; the hyperplane sweep launches one kernel per plane")
+    return out
 
 
 def measure_e2e(ctx, g, host, w, torch, steps):
