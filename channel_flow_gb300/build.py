@@ -5,8 +5,8 @@ Three translation units, compiled in parallel with nvcc:
 * ``cf_variant.cu`` as namespace ``cf_exact`` with ``--fmad=false``: the FP64
   kernels without fused multiply-add, whose results equal the reference's
   bit for bit;
-* ``cf_variant.cu`` as namespace ``cf_fast`` with contraction on and the FP32
-  instantiations;
+* ``cf_variant.cu`` as namespace ``cf_fast`` with contraction on, the
+  reduced-division face fluxes (CF_FAST_MATH) and the FP32 instantiations;
 * ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h);
 * ``cf_noalloc.cu``: the allocation-free DPLUSGS entry point (its scratch is
   a file-scope device array).
@@ -59,7 +59,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         base += ["-Xptxas", "-v"]
     units = [
         ("cf_variant.cu", "cf_exact.o", ["-DCF_NS=cf_exact", "--fmad=false"]),
-        ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "--fmad=true"]),
+        ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "-DCF_FAST_MATH", "--fmad=true"]),
         ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
         ("cf_noalloc.cu", "cf_noalloc.o", ["-DCF_NS=cf_noalloc", "--fmad=false"]),
     ]

@@ -521,12 +521,39 @@ __device__ __forceinline__ void flux_roe(const T *mL, const T *mR, const T *m, i
     F[5] = T(0.5) * (n1 * (_P + P_) - Fav3 / insqr) / Jf;
 }
 
+}  // namespace CF_NS
+
+#ifdef CF_FAST_MATH
+#include "cf_flux_fast.cuh"
+#endif
+
+namespace CF_NS {
+
 // One thread per face of the box; DIR 0/1/2, LIMITED selects the scheme.
 template <int DIR, bool LIMITED, typename T>
 __global__ void __launch_bounds__(256) k_flux(cf_dims d, cf_flux_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     T mL[5], mR[5], m[9], F[6];
+#ifdef CF_FAST_MATH
+    if (DIR == 0) {
+        if (LIMITED) fast_states_x_limited<T>(d, a, i, j, k, mL, mR);
+        else fast_states_x_linear<T>(d, a, i, j, k, mL, mR);
+    } else if (DIR == 1) {
+        if (LIMITED) fast_states_y_limited<T>(d, a, i, j, k, mL, mR);
+        else fast_states_y_linear<T>(d, a, i, j, k, mL, mR);
+    } else {
+        if (LIMITED) fast_states_z_limited<T>(d, a, i, j, k, mL, mR);
+        else fast_states_z_linear<T>(d, a, i, j, k, mL, mR);
+    }
+    const size_t q = d.ix(i, j, k);
+#pragma unroll
+    for (int n = 0; n < 9; n++) m[n] = T(a.m[n][q]);
+    if (LIMITED)
+        fast_flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), T(d.K), T(d.e), F);
+    else
+        fast_flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), T(d.K), F);
+#else
     if (DIR == 0) {
         if (LIMITED) states_x_limited<T>(d, a, i, j, k, mL, mR);
         else states_x_linear<T>(d, a, i, j, k, mL, mR);
@@ -544,6 +571,7 @@ __global__ void __launch_bounds__(256) k_flux(cf_dims d, cf_flux_args a, cf_box 
         flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), T(d.K), T(d.e), F);
     else
         flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), T(d.K), F);
+#endif
     if (DIR == 1 && (j == 1 || j == d.ny)) {
         // wall faces keep the pressure term of the normal momentum only
         a.F[0][q] = 0;
