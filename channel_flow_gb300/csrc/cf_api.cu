@@ -29,6 +29,9 @@ struct cf_ctx {
     bool tables_checked = false;
     double *er_dev = nullptr;         // 5 doubles + device counter space
     double *er_host = nullptr;        // pinned
+    cudaStream_t cap = nullptr;       // private stream for graph capture
+    cudaGraphExec_t dts_exec = nullptr;               // Dual_time_stepping as one graph
+    std::vector<unsigned char> dts_key;               // arguments it was captured with
     std::string err;
 };
 
@@ -198,6 +201,8 @@ void cf_destroy(cf_ctx *c)
     if (c->ijk_dev) cudaFree(c->ijk_dev);
     if (c->er_dev) cudaFree(c->er_dev);
     if (c->er_host) cudaFreeHost(c->er_host);
+    if (c->dts_exec) cudaGraphExecDestroy(c->dts_exec);
+    if (c->cap) cudaStreamDestroy(c->cap);
     delete c;
 }
 
@@ -416,22 +421,23 @@ int cf_Filter(cf_ctx *c, int, double Roe_criterion, double E_high, double E_low,
     a.Yp = R(c, Y_point);
     a.J = R(c, J);
     a.Ep[0] = R(c, EpX); a.Ep[1] = R(c, EpY); a.Ep[2] = R(c, EpZ);
-    double *s = scratch(c, "filter", 27);
+    double *s = scratch(c, "filter", 16);
     if (!s) return fail(c, CF_ERR_NOMEM, "Filter: scratch allocation failed");
     const size_t n = c->d.total();
     int f = 0;
-    for (int v = 0; v < 5; v++) a.gx[v] = s + n * f++;
-    for (int v = 0; v < 5; v++) a.gy[v] = s + n * f++;
     for (int l = 0; l < 2; l++)
-        for (int v = 0; v < 5; v++) a.lev[l][v] = s + n * f++;
-    for (int v = 0; v < 5; v++) a.acc[v] = s + n * f++;
+        for (int v = 0; v < 4; v++) a.lev[l][v] = s + n * f++;
+    for (int v = 0; v < 4; v++) a.acc[v] = s + n * f++;
+    a.cA = s + n * f++;
+    a.cC = s + n * f++;
     a.Eh = s + n * f++;
     a.E2h = s + n * f++;
-    // the switch Ep is a threshold decision: the FP64 sensor always runs in
-    // the no-FMA build so that it takes the reference's decisions exactly
-    cudaError_t e = c->prec == CF_PREC_FP32
-                        ? cf_fast::filter(c->d, a, Roe_criterion, E_high, E_low, 1, c->stream)
-                        : cf_exact::filter(c->d, a, Roe_criterion, E_high, E_low, 0, c->stream);
+    // FP64 exact: the reference's expression trees (no FMA), so the switch
+    // takes the reference's decisions; FP64: contracted, reciprocal weights;
+    // FP32: float arithmetic and float scratch levels
+    cudaError_t e = c->prec == CF_PREC_FP64_EXACT
+                        ? cf_exact::filter(c->d, a, Roe_criterion, E_high, E_low, 0, c->stream)
+                        : cf_fast::filter(c->d, a, Roe_criterion, E_high, E_low, kprec(c), c->stream);
     return cuda_check(c, e, "Filter");
 }
 
@@ -508,16 +514,84 @@ static int lu_args(cf_ctx *c, double **p, const char *who, cf_lu_args &a)
     return CF_OK;
 }
 
-static int lu_finish_host(cf_ctx *c, const cf_lu_args &a, double *er[5], const char *who)
+static int lu_read_norms(cf_ctx *c, double *er[5], const char *who)
 {
-    cudaError_t e = exact(c) ? cf_exact::lu_finish(c->d, a, c->er_dev, c->stream)
-                             : cf_fast::lu_finish(c->d, a, c->er_dev, c->stream);
-    if (int rc = cuda_check(c, e, who)) return rc;
     if (int rc = cuda_check(c, cudaMemcpyAsync(c->er_host, c->er_dev, 5 * sizeof(double), cudaMemcpyDeviceToHost,
                                                c->stream), who)) return rc;
     if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), who)) return rc;
     for (int n = 0; n < 5; n++)
         if (er[n]) *er[n] = c->er_host[n];
+    return CF_OK;
+}
+
+static int lu_finish_host(cf_ctx *c, const cf_lu_args &a, double *er[5], const char *who)
+{
+    cudaError_t e = exact(c) ? cf_exact::lu_finish(c->d, a, c->er_dev, c->stream)
+                             : cf_fast::lu_finish(c->d, a, c->er_dev, c->stream);
+    if (int rc = cuda_check(c, e, who)) return rc;
+    return lu_read_norms(c, er, who);
+}
+
+// The whole Dual_time_stepping call on stream s: assembly, coefficient
+// pack, one forward and one backward hyperplane sweep (one launch per
+// plane), NL <- NR, update and norms into er_dev.
+//
+// The reference runs the forward/backward pair twice
+// (Dual_time_stepping.cpp:563-1275) so that, with several ranks, the
+// second pass sees the neighbours' interface planes of the first.  On one
+// domain the second pass reproduces the first bit for bit: the sweeps read
+// N only at ghost cells (zero, never written) and at cells the same sweep
+// has already recomputed from MR and the fixed pack.  It is run once.
+static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, double dt, cudaStream_t s)
+{
+    const cf_dims &d = c->d;
+    const bool ex = exact(c);
+    const int pr = ex ? 0 : kprec(c);
+    cudaError_t e = ex ? cf_exact::lu_prepare(d, a, dt, true, 0, s) : cf_fast::lu_prepare(d, a, dt, true, pr, s);
+    if (e == cudaSuccess) e = ex ? cf_exact::lu_pack(d, a, pack, dt, 0, s) : cf_fast::lu_pack(d, a, pack, dt, pr, s);
+    const int mlast = d.gend + d.ny + d.nz;
+    for (int m = 7; m <= mlast && e == cudaSuccess; m++) {
+        const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
+        e = ex ? cf_exact::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, true, 0, s)
+               : cf_fast::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, true, pr, s);
+    }
+    for (int m = mlast; m >= 7 && e == cudaSuccess; m--) {
+        const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
+        e = ex ? cf_exact::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, false, 0, s)
+               : cf_fast::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, false, pr, s);
+    }
+    if (e == cudaSuccess) e = cf_fast::lu_copy(d, a, s);
+    if (e == cudaSuccess) e = ex ? cf_exact::lu_finish(d, a, c->er_dev, s) : cf_fast::lu_finish(d, a, c->er_dev, s);
+    return e;
+}
+
+// capture enqueue_dts into c->dts_exec (kept while the arguments repeat)
+static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, double dt)
+{
+    if (!c->cap) {
+        if (int rc = cuda_check(c, cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking), "capture stream"))
+            return rc;
+    }
+    if (c->dts_exec) {
+        cudaGraphExecDestroy(c->dts_exec);
+        c->dts_exec = nullptr;
+    }
+    c->dts_key.clear();
+    if (int rc = cuda_check(c, cudaStreamBeginCapture(c->cap, cudaStreamCaptureModeThreadLocal), "graph capture"))
+        return rc;
+    const cudaError_t le = enqueue_dts(c, a, pack, dt, c->cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(c->cap, &g);
+    if (le != cudaSuccess || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_check(c, le != cudaSuccess ? le : ee, "Dual_time_stepping capture");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->dts_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        c->dts_exec = nullptr;
+        return cuda_check(c, ie, "Dual_time_stepping graph");
+    }
     return CF_OK;
 }
 
@@ -534,31 +608,22 @@ int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er
     }
     cf_lu_args a;
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
-    const cf_dims &d = c->d;
-    const bool ex = exact(c);
-    const int pr = ex ? 0 : kprec(c);
-    cudaError_t e = ex ? cf_exact::lu_prepare(d, a, deltaT, true, 0, c->stream)
-                       : cf_fast::lu_prepare(d, a, deltaT, true, pr, c->stream);
-    if (int rc = cuda_check(c, e, "Dual_time_stepping")) return rc;
-    const int mlast = d.gend + d.ny + d.nz;
-    for (int sweep = 1; sweep <= 2; sweep++) {
-        for (int m = 7; m <= mlast; m++) {
-            const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
-            e = ex ? cf_exact::lu_plane(d, a, c->ijk_dev, first, cnt, true, deltaT, 0, c->stream)
-                   : cf_fast::lu_plane(d, a, c->ijk_dev, first, cnt, true, deltaT, pr, c->stream);
-            if (e != cudaSuccess) return cuda_check(c, e, "Dual_time_stepping forward plane");
-        }
-        for (int m = mlast; m >= 7; m--) {
-            const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
-            e = ex ? cf_exact::lu_plane(d, a, c->ijk_dev, first, cnt, false, deltaT, 0, c->stream)
-                   : cf_fast::lu_plane(d, a, c->ijk_dev, first, cnt, false, deltaT, pr, c->stream);
-            if (e != cudaSuccess) return cuda_check(c, e, "Dual_time_stepping backward plane");
-        }
-        e = cf_fast::lu_copy(d, a, c->stream);
-        if (int rc = cuda_check(c, e, "Dual_time_stepping copy")) return rc;
+    double *pack = scratch(c, "lu_pack", CF_LU_PACK);
+    if (!pack) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: coefficient pack allocation failed");
+    // the graph bakes in every pointer and scalar: recapture when they change
+    std::vector<unsigned char> key(sizeof(cf_lu_args) + sizeof(double *) + sizeof(double) + sizeof(int), 0);
+    unsigned char *kp = key.data();
+    std::memcpy(kp, &a, sizeof a);
+    std::memcpy(kp + sizeof a, &pack, sizeof pack);
+    std::memcpy(kp + sizeof a + sizeof pack, &deltaT, sizeof deltaT);
+    std::memcpy(kp + sizeof a + sizeof pack + sizeof deltaT, &c->prec, sizeof c->prec);
+    if (!c->dts_exec || key != c->dts_key) {
+        if (int rc = capture_dts(c, a, pack, deltaT)) return rc;
+        c->dts_key = key;
     }
+    if (int rc = cuda_check(c, cudaGraphLaunch(c->dts_exec, c->stream), "Dual_time_stepping")) return rc;
     double *er[5] = {er1, er2, er3, er4, er5};
-    return lu_finish_host(c, a, er, "Dual_time_stepping");
+    return lu_read_norms(c, er, "Dual_time_stepping");
 }
 
 int cf_DPLUSGS(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,

@@ -2,111 +2,206 @@
 //
 // Per filter width (h: [1 6 1]/8, 2h: [1 2 1]/4) six levels, each an x pass,
 // a stretched-y pass and a z pass over the interior box i = 3..gend,
-// j = 2..ny, k = 2..nz.  Values read outside that box are the copies of U
-// the reference puts into every temporary (Filter.cpp:121-136): the shell
-// of each scratch field is filled with U once per call.  The deconvolved
-// field 6 G1p - 15 G1 + 20 GG - 15 GGG + 6 GGGG - GGGGG is accumulated in
-// the z pass level by level in the reference's summation order (the
-// roundings are identical), which replaces the reference's 55 temporaries
-// by 5 ping-pong level fields, the x/y pass fields and one accumulator.
+// j = 2..ny, k = 2..nz.  Every value a pass reads outside that box is the
+// cell's U: the reference fills each temporary with U before the passes
+// (Filter.cpp:121-136) and the passes write only the box.  The deconvolved
+// field 6 G1p - 15 G1 + 20 GG - 15 GGG + 6 GGGG - GGGGG (Filter.cpp:769) is
+// accumulated level by level in the reference's summation order.
+//
+// One launch per level (k_filter_level) runs the three passes in shared
+// memory: a block owns a 8 x 32 (j, k) tile and marches through a chunk of
+// x planes, holding the level's input on three planes in registers; x-pass
+// and y-pass results live in shared memory only.  Of the five variables
+// only rho, rho u, rho v, rho w are filtered: the sensor E (Filter.cpp:
+// 790-804) never reads the filtered energy.
+//
+// EXACT (no-FMA build) keeps the reference's expression trees, with the
+// metric ratios b/a and c/a of the y pass formed once per call; otherwise
+// the y pass uses per-cell weights A = (b/a) J(j-1)/J(j), C = (c/a)
+// J(j+1)/J(j) and no division.  ST is the storage type of the level and
+// accumulator fields (float in the FP32 build).
 #pragma once
 #include "cf_common.cuh"
 
 
 namespace CF_NS {
 
-// copy U into every scratch field outside the interior box
-__global__ void k_filter_shell(cf_dims d, cf_filter_args a, size_t n)
+constexpr int FT_J = 8, FT_K = 32, FT_I = 16;    // tile rows (j), columns (k), planes per block (i)
+constexpr int FT_HJ = FT_J + 2, FT_HK = FT_K + 2, FT_HALO = FT_HJ * FT_HK;
+
+template <typename ST>
+struct filt_fields {
+    const double *U[4];
+    const void *src[4];     // level input: U (level 0) or the previous level (ST)
+    ST *dst[4];             // level output (unused at the last level)
+    ST *acc[4];             // deconvolution sum
+    const ST *cA, *cC;      // y-pass coefficients (b/a, c/a when EXACT)
+    const double *J;
+};
+
+__device__ __forceinline__ bool filt_inside(const cf_dims &d, int i, int j, int k)
 {
-    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    const size_t plane = d.plane();
-    const int i = (int)(q / plane);
-    const size_t r = q - (size_t)i * plane;
-    const int j = (int)(r / (size_t)d.Zm);
-    const int k = (int)(r - (size_t)j * (size_t)d.Zm);
-    if (i >= 3 && i <= d.gend && j >= 2 && j <= d.ny && k >= 2 && k <= d.nz) return;
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-        const double u = a.U[v][q];
-        a.gx[v][q] = u;
-        a.gy[v][q] = u;
-        a.lev[0][v][q] = u;
-        a.lev[1][v][q] = u;
-    }
+    return i >= 3 && i <= d.gend && j >= 2 && j <= d.ny && k >= 2 && k <= d.nz;
 }
 
-// x pass (Filter.cpp:156-170, 835-849): level L -> gx
-template <typename T, bool WIDE>
-__global__ void k_filter_x(cf_dims d, cf_ptr5 src, cf_ptr5 dst, cf_box b)
-{
-    CF_BOX_INDEX(b, i, j, k);
-    const size_t q = d.ix(i, j, k), s = d.plane();
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-        const double *g = src.p[v];
-        T r = WIDE ? T(0.25) * (T(g[q - s]) + T(2) * T(g[q]) + T(g[q + s]))
-                   : T(0.125) * (T(g[q - s]) + T(6) * T(g[q]) + T(g[q + s]));
-        dst.p[v][q] = double(r);
-    }
-}
-
-// stretched y pass (Filter.cpp:186-208, 863-883): gx -> gy
-template <typename T, bool WIDE>
-__global__ void k_filter_y(cf_dims d, cf_ptr5 src, cf_ptr5 dst, const double *__restrict__ J,
-                           const double *__restrict__ Yp, cf_box b)
+// y-pass coefficients, once per call (Filter.cpp:186-208)
+template <typename T, typename ST, bool EXACT>
+__global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__restrict__ Yp,
+                                                     const double *__restrict__ J, ST *cA, ST *cC, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k), s = d.Zm;
-    T a_ = T(Yp[q + s]) - T(Yp[q - s]);
-    T b_ = T(Yp[q + s]) - T(Yp[q]);
-    T c_ = T(Yp[q]) - T(Yp[q - s]);
-    const T Jm = T(J[q - s]), J0 = T(J[q]), Jp = T(J[q + s]);
-#pragma unroll
-    for (int v = 0; v < 5; v++) {
-        const double *G = src.p[v];
-        T r = WIDE ? T(0.5) * (b_ / a_ * T(G[q - s]) * Jm + T(G[q]) * J0 + c_ / a_ * T(G[q + s]) * Jp) / J0
-                   : T(0.125) * (T(2) * b_ / a_ * T(G[q - s]) * Jm + T(6) * T(G[q]) * J0 + T(2) * c_ / a_ * T(G[q + s]) * Jp) / J0;
-        dst.p[v][q] = double(r);
+    if (EXACT) {
+        T a_ = T(Yp[q + s]) - T(Yp[q - s]);
+        T b_ = T(Yp[q + s]) - T(Yp[q]);
+        T c_ = T(Yp[q]) - T(Yp[q - s]);
+        cA[q] = ST(b_ / a_);
+        cC[q] = ST(c_ / a_);
+    } else {
+        const double a_ = Yp[q + s] - Yp[q - s];
+        const double b_ = Yp[q + s] - Yp[q];
+        const double c_ = Yp[q] - Yp[q - s];
+        const double iJ = 1.0 / J[q];
+        cA[q] = ST(b_ / a_ * (J[q - s] * iJ));
+        cC[q] = ST(c_ / a_ * (J[q + s] * iJ));
     }
 }
 
-// z pass (Filter.cpp:224-239, 896-910): gy -> level L+1, and the running
-// deconvolution sum of Filter.cpp:769 (weights 6, -15, 20, -15, 6, -1)
-template <typename T, bool WIDE>
-__global__ void k_filter_z(cf_dims d, cf_ptr5 src, cf_ptr5 dst, cf_ptr5 acc, cf_box b, int level)
+template <typename T, typename SRC>
+__device__ __forceinline__ T filt_load(const cf_dims &d, const double *U, const void *src, int i, int j, int k)
 {
-    CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
+    return filt_inside(d, i, j, k) ? T(static_cast<const SRC *>(src)[q]) : T(U[q]);
+}
+
+template <typename T, typename SRC, typename ST, bool WIDE, bool EXACT>
+__global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST> f, int level)
+{
+    __shared__ T sgx[4][FT_HJ][FT_HK];     // x pass, rows j0-1..j0+8, columns k0-1..k0+32
+    __shared__ T sgy[4][FT_J][FT_HK];      // y pass, rows j0..j0+7
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int k0 = 2 + (int)blockIdx.x * FT_K, j0 = 2 + (int)blockIdx.y * FT_J;
+    const int i0 = 3 + (int)blockIdx.z * FT_I;
+    const int i1 = min(i0 + FT_I - 1, d.gend);
+    // halo positions owned by this thread: tid and tid + 256
+    int pj[2], pk[2];
+    bool pv[2];
 #pragma unroll
-    for (int v = 0; v < 5; v++) {
-        const double *G = src.p[v];
-        T r = WIDE ? T(0.25) * (T(G[q - 1]) + T(2) * T(G[q]) + T(G[q + 1]))
-                   : T(0.125) * (T(G[q - 1]) + T(6) * T(G[q]) + T(G[q + 1]));
-        dst.p[v][q] = double(r);
-        T s;
-        switch (level) {
-        case 0: s = T(6) * r; break;
-        case 1: s = T(acc.p[v][q]) - T(15) * r; break;
-        case 2: s = T(acc.p[v][q]) + T(20) * r; break;
-        case 3: s = T(acc.p[v][q]) - T(15) * r; break;
-        case 4: s = T(acc.p[v][q]) + T(6) * r; break;
-        default: s = T(acc.p[v][q]) - r; break;
+    for (int o = 0; o < 2; o++) {
+        const int p = tid + 256 * o;
+        pj[o] = j0 - 1 + p / FT_HK;
+        pk[o] = k0 - 1 + p % FT_HK;
+        pv[o] = p < FT_HALO && pj[o] <= d.ny + 1 && pk[o] <= d.nz + 1;
+    }
+    T sm[4][2], s0[4][2], sp[4][2];
+#pragma unroll
+    for (int o = 0; o < 2; o++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            sm[v][o] = pv[o] ? filt_load<T, SRC>(d, f.U[v], f.src[v], i0 - 1, pj[o], pk[o]) : T(0);
+            s0[v][o] = pv[o] ? filt_load<T, SRC>(d, f.U[v], f.src[v], i0, pj[o], pk[o]) : T(0);
         }
-        acc.p[v][q] = double(s);
+    const int jy = j0 + ty;                  // y-pass / output row of this thread
+    const bool last = level == 5;
+    for (int i = i0; i <= i1; i++) {
+        // x pass (Filter.cpp:156-170, 835-849)
+#pragma unroll
+        for (int o = 0; o < 2; o++) {
+            if (!pv[o]) continue;
+            const bool in = filt_inside(d, i, pj[o], pk[o]);
+            const int r = (tid + 256 * o) / FT_HK, c = (tid + 256 * o) % FT_HK;
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                sp[v][o] = filt_load<T, SRC>(d, f.U[v], f.src[v], i + 1, pj[o], pk[o]);
+                T g = s0[v][o];
+                if (in)
+                    g = WIDE ? T(0.25) * (sm[v][o] + T(2) * s0[v][o] + sp[v][o])
+                             : T(0.125) * (sm[v][o] + T(6) * s0[v][o] + sp[v][o]);
+                sgx[v][r][c] = g;
+            }
+        }
+        __syncthreads();
+        // stretched y pass (Filter.cpp:186-208, 863-883)
+        if (jy <= d.ny) {
+#pragma unroll
+            for (int o = 0; o < 2; o++) {
+                const int c = tx + 32 * o;
+                const int kk = k0 - 1 + c;
+                if (c >= FT_HK || kk > d.nz + 1) continue;
+                if (kk < 2 || kk > d.nz) {
+#pragma unroll
+                    for (int v = 0; v < 4; v++) sgy[v][ty][c] = sgx[v][ty + 1][c];
+                    continue;
+                }
+                const size_t q = d.ix(i, jy, kk);
+                const T A = T(f.cA[q]), C = T(f.cC[q]);
+                if (EXACT) {
+                    const size_t s = d.Zm;
+                    const T Jm = T(f.J[q - s]), J0 = T(f.J[q]), Jp = T(f.J[q + s]);
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const T gm = sgx[v][ty][c], g0 = sgx[v][ty + 1][c], gp = sgx[v][ty + 2][c];
+                        sgy[v][ty][c] = WIDE ? T(0.5) * (A * gm * Jm + g0 * J0 + C * gp * Jp) / J0
+                                             : T(0.125) * (T(2) * A * gm * Jm + T(6) * g0 * J0 + T(2) * C * gp * Jp) / J0;
+                    }
+                } else {
+                    const T cw = WIDE ? T(0.5) : T(0.25), c0 = WIDE ? T(0.5) : T(0.75);
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const T gm = sgx[v][ty][c], g0 = sgx[v][ty + 1][c], gp = sgx[v][ty + 2][c];
+                        sgy[v][ty][c] = cw * (A * gm + C * gp) + c0 * g0;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // z pass (Filter.cpp:224-239, 896-910) and the deconvolution sum
+        const int kz = k0 + tx;
+        if (jy <= d.ny && kz <= d.nz) {
+            const size_t q = d.ix(i, jy, kz);
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const T gm = sgy[v][ty][tx], g0 = sgy[v][ty][tx + 1], gp = sgy[v][ty][tx + 2];
+                const T r = WIDE ? T(0.25) * (gm + T(2) * g0 + gp) : T(0.125) * (gm + T(6) * g0 + gp);
+                if (!last) f.dst[v][q] = ST(r);
+                T s;
+                switch (level) {
+                case 0: s = T(6) * r; break;
+                case 1: s = T(f.acc[v][q]) - T(15) * r; break;
+                case 2: s = T(f.acc[v][q]) + T(20) * r; break;
+                case 3: s = T(f.acc[v][q]) - T(15) * r; break;
+                case 4: s = T(f.acc[v][q]) + T(6) * r; break;
+                default: s = T(f.acc[v][q]) - r; break;
+                }
+                f.acc[v][q] = ST(s);
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < 2; o++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                sm[v][o] = s0[v][o];
+                s0[v][o] = sp[v][o];
+            }
+        // sgx is rewritten next plane only after every thread passed the
+        // second barrier (y pass done); sgy after the next first barrier
     }
 }
 
 // E = |u - u_deconvolved|^2 (Filter.cpp:790-804, 1465-1479)
-template <typename T>
-__global__ void k_filter_energy(cf_dims d, cf_filter_args a, double *E, cf_box b)
+template <typename ST>
+struct filt_ptr4 {
+    ST *p[4];
+};
+template <typename T, typename ST>
+__global__ void k_filter_energy4(cf_dims d, cf_ptr5 U, filt_ptr4<ST> acc, double *E, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
-    T u1 = T(a.U[0][q]), f1 = T(a.acc[0][q]);
-    T Ue = T(a.U[1][q]) / u1 - T(a.acc[1][q]) / f1;
-    T Ve = T(a.U[2][q]) / u1 - T(a.acc[2][q]) / f1;
-    T We = T(a.U[3][q]) / u1 - T(a.acc[3][q]) / f1;
+    T u1 = T(U.p[0][q]), f1 = T(acc.p[0][q]);
+    T Ue = T(U.p[1][q]) / u1 - T(acc.p[1][q]) / f1;
+    T Ve = T(U.p[2][q]) / u1 - T(acc.p[2][q]) / f1;
+    T We = T(U.p[3][q]) / u1 - T(acc.p[3][q]) / f1;
     E[q] = double(Ue * Ue + Ve * Ve + We * We);
 }
 
@@ -153,35 +248,49 @@ __global__ void k_filter_ep(cf_dims d, const double *__restrict__ Eh, const doub
     Ep[d.ix(i, j, k)] = Emax >= T(crit) ? hi : lo;
 }
 
-template <typename T>
+template <typename T, typename SRC, typename ST, bool EXACT>
+static void filter_level_launch(const cf_dims &d, const filt_fields<ST> &f, bool wide, int level, cudaStream_t s)
+{
+    const dim3 g((unsigned)((d.Z_out + FT_K - 1) / FT_K), (unsigned)((d.Y_out + FT_J - 1) / FT_J),
+                 (unsigned)((d.X_out + FT_I - 1) / FT_I));
+    const dim3 t(32, 8);
+    if (wide) k_filter_level<T, SRC, ST, true, EXACT><<<g, t, 0, s>>>(d, f, level);
+    else k_filter_level<T, SRC, ST, false, EXACT><<<g, t, 0, s>>>(d, f, level);
+}
+
+// T: arithmetic type, ST: storage of the scratch levels, EXACT: reference
+// expression trees.  Scratch (cf_filter_args): lev[2][4], acc[4], cA, cC
+// hold ST values; Eh, E2h doubles.
+template <typename T, typename ST, bool EXACT>
 cudaError_t launch_filter(const cf_dims &d, const cf_filter_args &a, double crit, double hi, double lo,
                           cudaStream_t s)
 {
-    const size_t n = d.total();
-    k_filter_shell<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
     const cf_box bi = make_box(3, d.gend, 2, d.ny, 2, d.nz);
     const dim3 g = box_grid(bi), t = box_block();
-    cf_ptr5 gx, gy, acc, l0, l1, U;
-    for (int v = 0; v < 5; v++) {
-        gx.p[v] = a.gx[v]; gy.p[v] = a.gy[v]; acc.p[v] = a.acc[v];
-        l0.p[v] = a.lev[0][v]; l1.p[v] = a.lev[1][v]; U.p[v] = const_cast<double *>(a.U[v]);
+    ST *cA = static_cast<ST *>(a.cA), *cC = static_cast<ST *>(a.cC);
+    k_filter_coef<T, ST, EXACT><<<g, t, 0, s>>>(d, a.Yp, a.J, cA, cC, bi);
+    filt_fields<ST> f;
+    for (int v = 0; v < 4; v++) {
+        f.U[v] = a.U[v];
+        f.acc[v] = static_cast<ST *>(a.acc[v]);
     }
+    f.cA = cA;
+    f.cC = cC;
+    f.J = a.J;
+    cf_ptr5 U;
+    filt_ptr4<ST> acc;
+    for (int v = 0; v < 5; v++) U.p[v] = const_cast<double *>(a.U[v]);
+    for (int v = 0; v < 4; v++) acc.p[v] = static_cast<ST *>(a.acc[v]);
     for (int wide = 0; wide < 2; wide++) {
-        cf_ptr5 src = U, dst = l0, other = l1;
         for (int lev = 0; lev < 6; lev++) {
-            if (wide) {
-                k_filter_x<T, true><<<g, t, 0, s>>>(d, src, gx, bi);
-                k_filter_y<T, true><<<g, t, 0, s>>>(d, gx, gy, a.J, a.Yp, bi);
-                k_filter_z<T, true><<<g, t, 0, s>>>(d, gy, dst, acc, bi, lev);
-            } else {
-                k_filter_x<T, false><<<g, t, 0, s>>>(d, src, gx, bi);
-                k_filter_y<T, false><<<g, t, 0, s>>>(d, gx, gy, a.J, a.Yp, bi);
-                k_filter_z<T, false><<<g, t, 0, s>>>(d, gy, dst, acc, bi, lev);
+            for (int v = 0; v < 4; v++) {
+                f.src[v] = lev == 0 ? static_cast<const void *>(a.U[v]) : a.lev[(lev - 1) & 1][v];
+                f.dst[v] = static_cast<ST *>(a.lev[lev & 1][v]);
             }
-            src = dst;
-            cf_ptr5 tmp = dst; dst = other; other = tmp;
+            if (lev == 0) filter_level_launch<T, double, ST, EXACT>(d, f, wide != 0, lev, s);
+            else filter_level_launch<T, ST, ST, EXACT>(d, f, wide != 0, lev, s);
         }
-        k_filter_energy<T><<<g, t, 0, s>>>(d, a, wide ? a.E2h : a.Eh, bi);
+        k_filter_energy4<T, ST><<<g, t, 0, s>>>(d, U, acc, wide ? a.E2h : a.Eh, bi);
     }
     cf_box bx = make_box(0, 1, 2, d.ny, 2, d.nz);
     k_filter_efill_x<<<box_grid(bx), t, 0, s>>>(d, a.Eh, a.E2h, bx);

@@ -12,11 +12,21 @@
 //   C, T, the metric norm, the matrix denominator and the face Jacobian.
 //
 // Results differ from the reference only by rounding (tests: within 1e-12
-// normwise in FP64).
+// normwise in FP64), except where two neighbouring values tie: the
+// reference's ratio is then 0/0 or x/0 and its state NaN; here the
+// reciprocal of a zero difference is taken as 0, which gives the limit
+// (no slope on that side).  Ties are rare in FP64 but frequent in FP32.
 #pragma once
 #include "cf_common.cuh"
 
 namespace CF_NS {
+
+// reciprocal of a neighbour difference, 0 for a tie
+template <typename T>
+__device__ __forceinline__ T ginv(T D)
+{
+    return D != T(0) ? T(1) / D : T(0);
+}
 
 // u[0..5] = cells c-2 .. c+3 of the face's stencil line; left state of cell
 // c (3rd or 5th order, slope sign S) and right state of cell c+1
@@ -24,7 +34,7 @@ template <typename T, int S>
 __device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, T jR, T &mL, T &mR)
 {
     const T D1 = u[2] - u[1], D2 = u[3] - u[2], D3 = u[4] - u[3];
-    const T inv1 = T(1) / D1, inv2 = T(1) / D2, inv3 = T(1) / D3;
+    const T inv1 = ginv(D1), inv2 = ginv(D2), inv3 = ginv(D3);
     const T rL = D2 * inv1;
     T bL;
     if (lo3) {
@@ -45,6 +55,50 @@ __device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, 
     }
     const T phiR = rmax(T(0), rmin(T(2), rmin(T(2) * rR, bR)));
     mR = (u[3] - T(0.5) * phiR * D3) * jR;
+}
+
+// left state alone: u[0..4] = cells c-2 .. c+2 (u[0] unused at 3rd order)
+template <typename T, int S>
+__device__ __forceinline__ T fast_left(const T *u, bool o3)
+{
+    const T D1 = u[2] - u[1], D2 = u[3] - u[2];
+    const T inv1 = ginv(D1);
+    const T rL = D2 * inv1;
+    T b;
+    if (o3) {
+        b = T(1.) / T(3) * (T(1) + T(2) * rL);
+    } else {
+        const T rLi = (u[4] - u[3]) * ginv(D2);
+        b = T(1.) / T(30) * (T(-2) * (u[1] - u[0]) * inv1 + T(11) + T(24) * rL - T(3) * rL * rLi);
+    }
+    const T phi = rmax(T(0), rmin(T(2), rmin(T(2) * rL, b)));
+    return S > 0 ? u[2] + T(0.5) * phi * D1 : u[2] - T(0.5) * phi * D1;
+}
+
+// right state alone: w[0..4] = cells c-2 .. c+2 of the right cell c
+// (w[4] unused at 3rd order)
+template <typename T>
+__device__ __forceinline__ T fast_right(const T *w, bool o3)
+{
+    const T Dm = w[2] - w[1], Dp = w[3] - w[2];
+    const T invp = ginv(Dp);
+    const T rR = Dm * invp;
+    T b;
+    if (o3) {
+        b = T(1.) / T(3) * (T(1) + T(2) * rR);
+    } else {
+        const T irR = (w[1] - w[0]) * ginv(Dm);
+        b = T(1.) / T(30) * (T(-2) * (w[4] - w[3]) * invp + T(11) + T(24) * rR - T(3) * rR * irR);
+    }
+    const T phi = rmax(T(0), rmin(T(2), rmin(T(2) * rR, b)));
+    return w[2] - T(0.5) * phi * Dp;
+}
+
+template <typename T>
+__device__ __forceinline__ void load5(const double *U, size_t qc, ptrdiff_t s, T *u)
+{
+#pragma unroll
+    for (int t = 0; t < 5; t++) u[t] = T(U[qc + (t - 2) * s]);
 }
 
 // loads the cells the selected orders need (others stay 0)
@@ -82,20 +136,63 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const cf
 {
     const ptrdiff_t s = d.Zm;
     const int ny = d.ny;
+    const T jf = T(a.Jf[d.ix(i, j, k)]);
+    const size_t qL = d.ix(i + 1, j, k + 1), qR = qL + s;
     const bool wallL = (j <= 2) || (j >= ny - 1);
     const bool wallR = (j + 1 <= 2) || (j + 1 >= ny - 1);
-    if (j == 1 || j == ny || wallL || wallR) {
-        // near-wall faces: the exact forms (two rows of each wall)
-        states_y_limited<T>(d, a, i, j, k, mL, mR);
+    if (j != 1 && j != ny && !wallL && !wallR) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            T u[6];
+            load6<T>(a.U[n], qL, s, false, false, u);
+            fast_pair<T, 1>(u, false, false, jf, jf, mL[n], mR[n]);
+        }
         return;
     }
-    const T jf = T(a.Jf[d.ix(i, j, k)]);
-    const size_t qc = d.ix(i + 1, j, k + 1);
+    // rows next to a wall (Flux_Y_limiter.cpp:115-477): wall averages on
+    // faces 1 and ny, the guarded ratio of variable 1 and 3rd order
+    if (j == 1) {
+        T temp = T(1.) / (T(1) / T(a.J[qL]) + T(1) / T(a.J[qL + s]));
 #pragma unroll
-    for (int n = 0; n < 5; n++) {
-        T u[6];
-        load6<T>(a.U[n], qc, s, false, false, u);
-        fast_pair<T, 1>(u, false, false, jf, jf, mL[n], mR[n]);
+        for (int n = 0; n < 5; n++) mL[n] = temp * (T(a.U[n][qL]) + T(a.U[n][qL + s]));
+    } else if (wallL) {
+        mL[0] = ywall_var1_left<T>(a.U[0], a.J, qL, s);
+#pragma unroll
+        for (int n = 1; n < 5; n++) {
+            T u[5];
+            u[0] = T(0);
+            u[1] = T(a.U[n][qL - s]); u[2] = T(a.U[n][qL]); u[3] = T(a.U[n][qL + s]); u[4] = T(0);
+            mL[n] = fast_left<T, 1>(u, true) * jf;
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            T u[5];
+            load5<T>(a.U[n], qL, s, u);
+            mL[n] = fast_left<T, 1>(u, false) * jf;
+        }
+    }
+    if (j == ny) {
+        const size_t q = d.ix(i + 1, ny, k + 1);
+        T temp = T(1.) / (T(1) / T(a.J[q]) + T(1) / T(a.J[q + s]));
+#pragma unroll
+        for (int n = 0; n < 5; n++) mR[n] = temp * (T(a.U[n][q]) + T(a.U[n][q + s]));
+    } else if (wallR) {
+        mR[0] = ywall_var1_right<T>(a.U[0], a.J, qR, s);
+#pragma unroll
+        for (int n = 1; n < 5; n++) {
+            T w[5];
+            w[0] = T(0);
+            w[1] = T(a.U[n][qR - s]); w[2] = T(a.U[n][qR]); w[3] = T(a.U[n][qR + s]); w[4] = T(0);
+            mR[n] = fast_right<T>(w, true) * jf;
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            T w[5];
+            load5<T>(a.U[n], qR, s, w);
+            mR[n] = fast_right<T>(w, false) * jf;
+        }
     }
 }
 
@@ -104,30 +201,61 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf
                                                       int k, T *mL, T *mR)
 {
     const int nz = d.nz, ny = d.ny;
-    if (k <= 2 || k >= nz - 1) {
-        // boundary rows: averages and linear 3rd-order states, exact forms
-        states_z_limited<T>(d, a, i, j, k, mL, mR);
+    const size_t qL = d.ix(i + 1, j + 1, k), qR = qL + 1;
+    const bool limL = k >= 3 && k <= nz - 1;          // cell k takes a limited state
+    const bool limR = k + 1 >= 3 && k + 1 <= nz - 1;  // cell k+1 takes a limited state
+    const bool lo3 = k >= ny, hi3 = k + 1 >= ny;      // the reference compares with the y extent
+    if (limL && limR) {
+        T iJ[6];
+        iJ[0] = lo3 ? T(0) : T(1) / T(a.J[qL - 2]);
+        iJ[1] = T(1) / T(a.J[qL - 1]);
+        iJ[2] = T(1) / T(a.J[qL]);
+        iJ[3] = T(1) / T(a.J[qL + 1]);
+        iJ[4] = T(1) / T(a.J[qL + 2]);
+        iJ[5] = hi3 ? T(0) : T(1) / T(a.J[qL + 3]);
+        const T jl = lo3 ? T(1.) / (T(-1) * iJ[1] + T(5) * iJ[2] + T(2) * iJ[3])
+                         : T(1.) / (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]);
+        const T jr = hi3 ? T(1.) / (T(2) * iJ[2] + T(5) * iJ[3] - T(1) * iJ[4])
+                         : T(1.) / (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            T u[6];
+            load6<T>(a.U[n], qL, 1, lo3, hi3, u);
+            fast_pair<T, -1>(u, lo3, hi3, jl, jr, mL[n], mR[n]);
+        }
         return;
     }
-    // cells k (left) and k+1 (right) are both in 3..nz-1
-    const size_t qc = d.ix(i + 1, j + 1, k);
-    const bool lo3 = k >= ny, hi3 = k + 1 >= ny;
-    T iJ[6];
-    iJ[0] = lo3 ? T(0) : T(1) / T(a.J[qc - 2]);
-    iJ[1] = T(1) / T(a.J[qc - 1]);
-    iJ[2] = T(1) / T(a.J[qc]);
-    iJ[3] = T(1) / T(a.J[qc + 1]);
-    iJ[4] = T(1) / T(a.J[qc + 2]);
-    iJ[5] = hi3 ? T(0) : T(1) / T(a.J[qc + 3]);
-    const T jl = lo3 ? T(1.) / (T(-1) * iJ[1] + T(5) * iJ[2] + T(2) * iJ[3])
-                     : T(1.) / (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]);
-    const T jr = hi3 ? T(1.) / (T(2) * iJ[2] + T(5) * iJ[3] - T(1) * iJ[4])
-                     : T(1.) / (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]);
+    // left state of face k from cell k (Flux_Z_limiter.cpp:120-330)
+    if (k == 1) {
 #pragma unroll
-    for (int n = 0; n < 5; n++) {
-        T u[6];
-        load6<T>(a.U[n], qc, 1, lo3, hi3, u);
-        fast_pair<T, -1>(u, lo3, hi3, jl, jr, mL[n], mR[n]);
+        for (int n = 0; n < 5; n++) mL[n] = avg2<T>(a.U[n], a.J, qL, 1);
+    } else if (!limL) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mL[n] = lin3L<T>(a.U[n], a.J, qL, 1);
+    } else {
+        const T jl = lo3 ? zjL3<T>(a.J, qL) : zjL5<T>(a.J, qL);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            T u[5];
+            load5<T>(a.U[n], qL, 1, u);
+            mL[n] = fast_left<T, -1>(u, lo3) * jl;
+        }
+    }
+    // right state of face k from cell k+1
+    if (k == nz) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mR[n] = avg2<T>(a.U[n], a.J, qL, 1);
+    } else if (!limR) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mR[n] = lin3R<T>(a.U[n], a.J, qR, 1);
+    } else {
+        const T jr = hi3 ? zjR3<T>(a.J, qR) : zjR5<T>(a.J, qR);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            T w[5];
+            load5<T>(a.U[n], qR, 1, w);
+            mR[n] = fast_right<T>(w, hi3) * jr;
+        }
     }
 }
 

@@ -6,6 +6,8 @@
 #pragma once
 #include "cf_types.h"
 
+constexpr int CF_LU_PACK = 52;   // doubles per cell of the sweep coefficient pack
+
 #define CF_DECLARE_LAUNCHERS(NS)                                                                        \
     namespace NS {                                                                                      \
     cudaError_t x_periodic(const cf_dims &d, const cf_ptr5 &U, cudaStream_t s);                         \
@@ -22,6 +24,10 @@
                            cudaStream_t s);                                                             \
     cudaError_t lu_plane(const cf_dims &d, const cf_lu_args &a, const int *ijk, int first, int count,  \
                          bool forward, double dt, int prec, cudaStream_t s);                            \
+    cudaError_t lu_pack(const cf_dims &d, const cf_lu_args &a, double *pack, double dt, int prec,       \
+                        cudaStream_t s);                                                                \
+    cudaError_t lu_plane_packed(const cf_dims &d, const cf_lu_args &a, const double *pack, const int *ijk, \
+                                int first, int count, bool forward, int prec, cudaStream_t s);          \
     cudaError_t lu_jacobi(const cf_dims &d, const cf_lu_args &a, double dt, int prec, cudaStream_t s); \
     cudaError_t lu_copy(const cf_dims &d, const cf_lu_args &a, cudaStream_t s);                        \
     cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, cudaStream_t s);     \

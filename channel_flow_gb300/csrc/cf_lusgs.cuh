@@ -189,7 +189,53 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     }
 }
 
-// L*N from cells i-1, j-1, k-1 (Dual_time_stepping.cpp:751-811)
+// L*N from the split Jacobians A, B, C of cells i-1, j-1, k-1 and their
+// N values a, b, c (Dual_time_stepping.cpp:751-811)
+template <typename T>
+__device__ __forceinline__ void lu_lower_sum(const lsplit<T> &A, const lsplit<T> &B, const lsplit<T> &C,
+                                             const T *a, const T *b, const T *c, T dXI, T dET, T dZT, T *LL)
+{
+    LL[0] = (-A.p11 * a[0] - A.p12 * a[1] - A.p13 * a[2] - A.p14 * a[3]) / dXI +
+            (-B.p11 * b[0] - B.p12 * b[1] - B.p13 * b[2] - B.p14 * b[3]) / dET +
+            (-C.p11 * c[0] - C.p12 * c[1] - C.p13 * c[2] - C.p14 * c[3]) / dZT;
+    LL[1] = (-A.p21 * a[0] - A.p22 * a[1]) / dXI + (-B.p21 * b[0] - B.p22 * b[1]) / dET +
+            (-C.p21 * c[0] - C.p22 * c[1]) / dZT;
+    LL[2] = (-A.p31 * a[0] - A.p33 * a[2]) / dXI + (-B.p31 * b[0] - B.p33 * b[2]) / dET +
+            (-C.p31 * c[0] - C.p33 * c[2]) / dZT;
+    LL[3] = (-A.p41 * a[0] - A.p44 * a[3]) / dXI + (-B.p41 * b[0] - B.p44 * b[3]) / dET +
+            (-C.p41 * c[0] - C.p44 * c[3]) / dZT;
+    LL[4] = (-A.p51 * a[0] - A.p52 * a[1] - A.p53 * a[2] - A.p54 * a[3] - A.p55 * a[4]) / dXI +
+            (-B.p51 * b[0] - B.p52 * b[1] - B.p53 * b[2] - B.p54 * b[3] - B.p55 * b[4]) / dET +
+            (-C.p51 * c[0] - C.p52 * c[1] - C.p53 * c[2] - C.p54 * c[3] - C.p55 * c[4]) / dZT;
+}
+
+// U*N from the split Jacobians of cells i+1, j+1, k+1 (Dual_time_stepping.cpp:1116-1177)
+template <typename T>
+__device__ __forceinline__ void lu_upper_sum(const lsplit<T> &A, const lsplit<T> &B, const lsplit<T> &C,
+                                             const T *a, const T *b, const T *c, T dXI, T dET, T dZT, T *UU)
+{
+    UU[0] = (+A.m11 * a[0] + A.p12 * a[1] + A.p13 * a[2] + A.p14 * a[3]) / dXI +
+            (+B.m11 * b[0] + B.p12 * b[1] + B.p13 * b[2] + B.p14 * b[3]) / dET +
+            (+C.m11 * c[0] + C.p12 * c[1] + C.p13 * c[2] + C.p14 * c[3]) / dZT;
+    UU[1] = (+A.p21 * a[0] + A.m22 * a[1]) / dXI + (+B.p21 * b[0] + B.m22 * b[1]) / dET +
+            (+C.p21 * c[0] + C.m22 * c[1]) / dZT;
+    UU[2] = (+A.p31 * a[0] + A.m22 * a[2]) / dXI + (+B.p31 * b[0] + B.m22 * b[2]) / dET +
+            (+C.p31 * c[0] + C.m22 * c[2]) / dZT;
+    UU[3] = (+A.p41 * a[0] + A.m22 * a[3]) / dXI + (+B.p41 * b[0] + B.m22 * b[3]) / dET +
+            (+C.p41 * c[0] + C.m22 * c[3]) / dZT;
+    UU[4] = (+A.p51 * a[0] + A.p52 * a[1] + A.p53 * a[2] + A.p54 * a[3] + A.m22 * a[4]) / dXI +
+            (+B.p51 * b[0] + B.p52 * b[1] + B.p53 * b[2] + B.p54 * b[3] + B.m22 * b[4]) / dET +
+            (+C.p51 * c[0] + C.p52 * c[1] + C.p53 * c[2] + C.p54 * c[3] + C.m22 * c[4]) / dZT;
+}
+
+template <typename T>
+__device__ __forceinline__ void lu_load5(double *const *N, size_t q, T *v)
+{
+#pragma unroll
+    for (int n = 0; n < 5; n++) v[n] = T(N[n][q]);
+}
+
+// L*N with the splits formed from the neighbours' states
 template <typename T>
 __device__ __forceinline__ void lu_lower(const cf_dims &d, const cf_lu_args &a, double *const *N, int i, int j,
                                          int k, T *LL)
@@ -199,22 +245,14 @@ __device__ __forceinline__ void lu_lower(const cf_dims &d, const cf_lu_args &a, 
     lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
     lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
     lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), T(a.m[6][qc]), T(a.m[7][qc]), T(a.m[8][qc]), false, K);
-    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
-    T a0 = T(N[0][qa]), a1 = T(N[1][qa]), a2 = T(N[2][qa]), a3 = T(N[3][qa]), a4 = T(N[4][qa]);
-    T b0 = T(N[0][qb]), b1 = T(N[1][qb]), b2 = T(N[2][qb]), b3 = T(N[3][qb]), b4 = T(N[4][qb]);
-    T c0 = T(N[0][qc]), c1 = T(N[1][qc]), c2 = T(N[2][qc]), c3 = T(N[3][qc]), c4 = T(N[4][qc]);
-    LL[0] = (-A.p11 * a0 - A.p12 * a1 - A.p13 * a2 - A.p14 * a3) / dXI +
-            (-B.p11 * b0 - B.p12 * b1 - B.p13 * b2 - B.p14 * b3) / dET +
-            (-C.p11 * c0 - C.p12 * c1 - C.p13 * c2 - C.p14 * c3) / dZT;
-    LL[1] = (-A.p21 * a0 - A.p22 * a1) / dXI + (-B.p21 * b0 - B.p22 * b1) / dET + (-C.p21 * c0 - C.p22 * c1) / dZT;
-    LL[2] = (-A.p31 * a0 - A.p33 * a2) / dXI + (-B.p31 * b0 - B.p33 * b2) / dET + (-C.p31 * c0 - C.p33 * c2) / dZT;
-    LL[3] = (-A.p41 * a0 - A.p44 * a3) / dXI + (-B.p41 * b0 - B.p44 * b3) / dET + (-C.p41 * c0 - C.p44 * c3) / dZT;
-    LL[4] = (-A.p51 * a0 - A.p52 * a1 - A.p53 * a2 - A.p54 * a3 - A.p55 * a4) / dXI +
-            (-B.p51 * b0 - B.p52 * b1 - B.p53 * b2 - B.p54 * b3 - B.p55 * b4) / dET +
-            (-C.p51 * c0 - C.p52 * c1 - C.p53 * c2 - C.p54 * c3 - C.p55 * c4) / dZT;
+    T va[5], vb[5], vc[5];
+    lu_load5<T>(N, qa, va);
+    lu_load5<T>(N, qb, vb);
+    lu_load5<T>(N, qc, vc);
+    lu_lower_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), LL);
 }
 
-// U*N from cells i+1, j+1, k+1 (Dual_time_stepping.cpp:1116-1177)
+// U*N with the splits formed from the neighbours' states
 template <typename T>
 __device__ __forceinline__ void lu_upper(const cf_dims &d, const cf_lu_args &a, double *const *N, int i, int j,
                                          int k, T *UU)
@@ -224,19 +262,133 @@ __device__ __forceinline__ void lu_upper(const cf_dims &d, const cf_lu_args &a, 
     lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
     lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
     lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), T(a.m[6][qc]), T(a.m[7][qc]), T(a.m[8][qc]), false, K);
-    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
-    T a0 = T(N[0][qa]), a1 = T(N[1][qa]), a2 = T(N[2][qa]), a3 = T(N[3][qa]), a4 = T(N[4][qa]);
-    T b0 = T(N[0][qb]), b1 = T(N[1][qb]), b2 = T(N[2][qb]), b3 = T(N[3][qb]), b4 = T(N[4][qb]);
-    T c0 = T(N[0][qc]), c1 = T(N[1][qc]), c2 = T(N[2][qc]), c3 = T(N[3][qc]), c4 = T(N[4][qc]);
-    UU[0] = (+A.m11 * a0 + A.p12 * a1 + A.p13 * a2 + A.p14 * a3) / dXI +
-            (+B.m11 * b0 + B.p12 * b1 + B.p13 * b2 + B.p14 * b3) / dET +
-            (+C.m11 * c0 + C.p12 * c1 + C.p13 * c2 + C.p14 * c3) / dZT;
-    UU[1] = (+A.p21 * a0 + A.m22 * a1) / dXI + (+B.p21 * b0 + B.m22 * b1) / dET + (+C.p21 * c0 + C.m22 * c1) / dZT;
-    UU[2] = (+A.p31 * a0 + A.m22 * a2) / dXI + (+B.p31 * b0 + B.m22 * b2) / dET + (+C.p31 * c0 + C.m22 * c2) / dZT;
-    UU[3] = (+A.p41 * a0 + A.m22 * a3) / dXI + (+B.p41 * b0 + B.m22 * b3) / dET + (+C.p41 * c0 + C.m22 * c3) / dZT;
-    UU[4] = (+A.p51 * a0 + A.p52 * a1 + A.p53 * a2 + A.p54 * a3 + A.m22 * a4) / dXI +
-            (+B.p51 * b0 + B.p52 * b1 + B.p53 * b2 + B.p54 * b3 + B.m22 * b4) / dET +
-            (+C.p51 * c0 + C.p52 * c1 + C.p53 * c2 + C.p54 * c3 + C.m22 * c4) / dZT;
+    T va[5], vb[5], vc[5];
+    lu_load5<T>(N, qa, va);
+    lu_load5<T>(N, qb, vb);
+    lu_load5<T>(N, qc, vc);
+    lu_upper_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), UU);
+}
+
+// ---------------------------------------------------------------------------
+// coefficient pack of the hyperplane sweeps
+// ---------------------------------------------------------------------------
+// The split Jacobians and the diagonal inverse of a cell depend only on its
+// own state and metrics, which the sweeps do not change.  k_lu_pack forms
+// them once per call for every cell and its ghost neighbours, so a plane
+// step only gathers them.  Per cell LU_PACK doubles: for x, y, z (16 each)
+// p11 p22 m11 m22 p12 p13 p14 p21 p31 p41 p51 p52 p53 p54 (2 unused), then
+// d11 d22 d51 (1 unused).  Same expressions as the unpacked path, so the
+// values are the same bits.
+constexpr int LU_PACK = 52;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lu_pack(cf_dims d, cf_lu_args a, double *__restrict__ pack, cf_box b,
+                                                 double dt)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const size_t q = d.ix(i, j, k);
+    const T K = T(d.K);
+    const lstate<T> s = lu_state<T>(d, a, q);
+    double *P = pack + q * LU_PACK;
+#pragma unroll
+    for (int dir = 0; dir < 3; dir++) {
+        const lsplit<T> A = lu_split<T>(s, T(a.m[3 * dir][q]), T(a.m[3 * dir + 1][q]), T(a.m[3 * dir + 2][q]),
+                                        dir == 0, K);
+        double2 *o = reinterpret_cast<double2 *>(P + 16 * dir);
+        o[0] = make_double2(double(A.p11), double(A.p22));
+        o[1] = make_double2(double(A.m11), double(A.m22));
+        o[2] = make_double2(double(A.p12), double(A.p13));
+        o[3] = make_double2(double(A.p14), double(A.p21));
+        o[4] = make_double2(double(A.p31), double(A.p41));
+        o[5] = make_double2(double(A.p51), double(A.p52));
+        o[6] = make_double2(double(A.p53), double(A.p54));
+    }
+    const ldiag<T> g = lu_diag<T>(d, a, q, s, T(dt));
+    double2 *o = reinterpret_cast<double2 *>(P + 48);
+    o[0] = make_double2(double(g.d11), double(g.d22));
+    o[1] = make_double2(double(g.d51), 0.0);
+}
+
+// split of one direction from the pack; UPPER selects m11/m22 in place of p11/p22
+template <typename T, bool UPPER>
+__device__ __forceinline__ lsplit<T> lu_unpack(const double *__restrict__ P)
+{
+    const double2 *v = reinterpret_cast<const double2 *>(P);
+    lsplit<T> A;
+    const double2 d0 = UPPER ? v[1] : v[0], d2 = v[2], d3 = v[3], d4 = v[4], d5 = v[5], d6 = v[6];
+    if (UPPER) {
+        A.m11 = T(d0.x); A.m22 = T(d0.y);
+    } else {
+        A.p11 = T(d0.x); A.p22 = T(d0.y);
+        A.p33 = A.p22; A.p44 = A.p22; A.p55 = A.p22;
+    }
+    A.p12 = T(d2.x); A.p13 = T(d2.y); A.p14 = T(d3.x); A.p21 = T(d3.y);
+    A.p31 = T(d4.x); A.p41 = T(d4.y); A.p51 = T(d5.x); A.p52 = T(d5.y);
+    A.p53 = T(d6.x); A.p54 = T(d6.y);
+    return A;
+}
+
+template <typename T>
+__device__ __forceinline__ ldiag<T> lu_unpack_diag(const double *__restrict__ P)
+{
+    const double2 *v = reinterpret_cast<const double2 *>(P + 48);
+    const double2 a0 = v[0], a1 = v[1];
+    ldiag<T> g;
+    g.d11 = T(a0.x); g.d22 = T(a0.y); g.d51 = T(a1.x);
+    return g;
+}
+
+// forward plane from the pack: NL = D^-1 (MR - L NL)
+template <typename T>
+__global__ void k_lu_forward_packed(cf_dims d, cf_lu_args a, const double *__restrict__ pack,
+                                    const int *__restrict__ ijk, int first, int count)
+{
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= count) return;
+    const int *c = ijk + 3 * (size_t)(first + t);
+    const size_t q = d.ix(c[0], c[1], c[2]);
+    const size_t qa = q - d.plane(), qb = q - (size_t)d.Zm, qc = q - 1;
+    const lsplit<T> A = lu_unpack<T, false>(pack + qa * LU_PACK);
+    const lsplit<T> B = lu_unpack<T, false>(pack + qb * LU_PACK + 16);
+    const lsplit<T> C = lu_unpack<T, false>(pack + qc * LU_PACK + 32);
+    const ldiag<T> g = lu_unpack_diag<T>(pack + q * LU_PACK);
+    T va[5], vb[5], vc[5], LL[5];
+    lu_load5<T>(a.NL, qa, va);
+    lu_load5<T>(a.NL, qb, vb);
+    lu_load5<T>(a.NL, qc, vc);
+    lu_lower_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), LL);
+    T r0 = T(a.MR[0][q]) - LL[0];
+    a.NL[0][q] = double(g.d11 * r0);
+    a.NL[1][q] = double(g.d22 * (T(a.MR[1][q]) - LL[1]));
+    a.NL[2][q] = double(g.d22 * (T(a.MR[2][q]) - LL[2]));
+    a.NL[3][q] = double(g.d22 * (T(a.MR[3][q]) - LL[3]));
+    a.NL[4][q] = double(g.d51 * r0 + g.d22 * (T(a.MR[4][q]) - LL[4]));
+}
+
+// backward plane from the pack: NR = NL - D^-1 U NR
+template <typename T>
+__global__ void k_lu_backward_packed(cf_dims d, cf_lu_args a, const double *__restrict__ pack,
+                                     const int *__restrict__ ijk, int first, int count)
+{
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= count) return;
+    const int *c = ijk + 3 * (size_t)(first + t);
+    const size_t q = d.ix(c[0], c[1], c[2]);
+    const size_t qa = q + d.plane(), qb = q + (size_t)d.Zm, qc = q + 1;
+    const lsplit<T> A = lu_unpack<T, true>(pack + qa * LU_PACK);
+    const lsplit<T> B = lu_unpack<T, true>(pack + qb * LU_PACK + 16);
+    const lsplit<T> C = lu_unpack<T, true>(pack + qc * LU_PACK + 32);
+    const ldiag<T> g = lu_unpack_diag<T>(pack + q * LU_PACK);
+    T va[5], vb[5], vc[5], UU[5];
+    lu_load5<T>(a.NR, qa, va);
+    lu_load5<T>(a.NR, qb, vb);
+    lu_load5<T>(a.NR, qc, vc);
+    lu_upper_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), UU);
+    a.NR[0][q] = double(T(a.NL[0][q]) - g.d11 * UU[0]);
+    a.NR[1][q] = double(T(a.NL[1][q]) - g.d22 * UU[1]);
+    a.NR[2][q] = double(T(a.NL[2][q]) - g.d22 * UU[2]);
+    a.NR[3][q] = double(T(a.NL[3][q]) - g.d22 * UU[3]);
+    a.NR[4][q] = double(T(a.NL[4][q]) - (g.d51 * UU[0] + g.d22 * UU[4]));
 }
 
 // forward plane: NL = D^-1 (MR - L NL) (Dual_time_stepping.cpp:594-877)

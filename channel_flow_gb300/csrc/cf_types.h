@@ -77,8 +77,11 @@ struct cf_filter_args {
     const double *Yp;       // Y_point
     const double *J;
     double *Ep[3];          // EpX, EpY, EpZ
-    double *gx[5], *gy[5], *lev[2][5], *acc[5];   // scratch
-    double *Eh, *E2h;                               // scratch
+    // scratch: two level fields and the deconvolution sum per filtered
+    // variable, the y-pass coefficients (double, or float in the FP32
+    // build), and the sensor energies
+    void *lev[2][4], *acc[4], *cA, *cC;
+    double *Eh, *E2h;
 };
 
 struct cf_lu_args {

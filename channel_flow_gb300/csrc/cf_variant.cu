@@ -53,8 +53,13 @@ cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStrea
 cudaError_t filter(const cf_dims &d, const cf_filter_args &a, double crit, double hi, double lo, int prec,
                    cudaStream_t s)
 {
-    return CF_DISPATCH(prec, launch_filter<double>(d, a, crit, hi, lo, s),
-                       launch_filter<float>(d, a, crit, hi, lo, s));
+#ifdef CF_FAST_MATH
+    constexpr bool exact = false;
+#else
+    constexpr bool exact = true;
+#endif
+    return CF_DISPATCH(prec, (launch_filter<double, double, exact>(d, a, crit, hi, lo, s)),
+                       (launch_filter<float, float, false>(d, a, crit, hi, lo, s)));
 }
 
 template <typename T>
@@ -98,6 +103,36 @@ cudaError_t lu_plane(const cf_dims &d, const cf_lu_args &a, const int *ijk, int 
 {
     return CF_DISPATCH(prec, lu_plane_t<double>(d, a, ijk, first, count, forward, dt, s),
                        lu_plane_t<float>(d, a, ijk, first, count, forward, dt, s));
+}
+
+template <typename T>
+static cudaError_t lu_pack_t(const cf_dims &d, const cf_lu_args &a, double *pack, double dt, cudaStream_t s)
+{
+    // every interior cell and its face-neighbour ghosts
+    cf_box b = make_box(2, d.gend + 1, 1, d.ny + 1, 1, d.nz + 1);
+    k_lu_pack<T><<<box_grid(b), box_block(), 0, s>>>(d, a, pack, b, dt);
+    return cudaGetLastError();
+}
+cudaError_t lu_pack(const cf_dims &d, const cf_lu_args &a, double *pack, double dt, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_pack_t<double>(d, a, pack, dt, s), lu_pack_t<float>(d, a, pack, dt, s));
+}
+
+template <typename T>
+static cudaError_t lu_plane_packed_t(const cf_dims &d, const cf_lu_args &a, const double *pack, const int *ijk,
+                                     int first, int count, bool forward, cudaStream_t s)
+{
+    if (count <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((count + 127) / 128);
+    if (forward) k_lu_forward_packed<T><<<blocks, 128, 0, s>>>(d, a, pack, ijk, first, count);
+    else k_lu_backward_packed<T><<<blocks, 128, 0, s>>>(d, a, pack, ijk, first, count);
+    return cudaGetLastError();
+}
+cudaError_t lu_plane_packed(const cf_dims &d, const cf_lu_args &a, const double *pack, const int *ijk, int first,
+                            int count, bool forward, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_plane_packed_t<double>(d, a, pack, ijk, first, count, forward, s),
+                       lu_plane_packed_t<float>(d, a, pack, ijk, first, count, forward, s));
 }
 
 template <typename T>
