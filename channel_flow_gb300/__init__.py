@@ -73,6 +73,25 @@ class Context:
     def set_stream(self, stream):
         self._ok(self.lib.cf_set_stream(self.h, stream if isinstance(stream, int) else int(stream)))
 
+    def set_lu_schedule(self, schedule: str):
+        """'wavefront' (default) or 'planes': how the hyperplane sweeps of
+        Dual_time_stepping are launched; both give the same results."""
+        self._ok(self.lib.cf_set_lu_schedule(self.h, {"wavefront": _lib.CF_LU_WAVEFRONT,
+                                                      "planes": _lib.CF_LU_PLANES}[schedule]))
+
+    def lu_trace(self, enable: bool = True):
+        """Record per-tile timer stamps of the wavefront sweeps."""
+        self._ok(self.lib.cf_lu_trace(self.h, 1 if enable else 0))
+
+    def lu_trace_read(self) -> np.ndarray:
+        """Stamps of the last Dual_time_stepping call, shape (2, tiles, 4):
+        forward/backward sweep; claimed, inputs ready, staged, done (ns)."""
+        g = self.grid
+        tiles = -(-g.X_out // 4) * -(-g.Y_out // 8) * -(-g.Z_out // 8)
+        out = np.zeros((2, tiles, 4), np.int64)
+        self._ok(self.lib.cf_lu_trace_read(self.h, out.ctypes.data, out.size))
+        return out
+
     def set_precision(self, precision: str):
         self._ok(self.lib.cf_set_precision(self.h, _lib.PREC[precision]))
         self.precision = precision

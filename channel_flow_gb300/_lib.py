@@ -11,7 +11,8 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libcfgb300.so"
 
-CF_OK, CF_ERR_ARG, CF_ERR_CUDA, CF_ERR_NONFINITE, CF_ERR_NOMEM, CF_ERR_STATE = range(6)
+CF_OK, CF_ERR_ARG, CF_ERR_CUDA, CF_ERR_NONFINITE, CF_ERR_NOMEM, CF_ERR_STATE, CF_ERR_TIMEOUT = range(7)
+CF_LU_WAVEFRONT, CF_LU_PLANES = 0, 1
 PREC = {"fp64_exact": 0, "fp64": 1, "fp32": 2}
 
 
@@ -43,6 +44,9 @@ _SIGS = {
     "cf_set_precision": ([P, C.c_int], C.c_int),
     "cf_set_stream": ([P, P], C.c_int),
     "cf_set_stretching": ([P, C.c_double], C.c_int),
+    "cf_set_lu_schedule": ([P, C.c_int], C.c_int),
+    "cf_lu_trace": ([P, C.c_int], C.c_int),
+    "cf_lu_trace_read": ([P, P, C.c_size_t], C.c_int),
     "cf_synchronize": ([P], C.c_int),
     "cf_field_count": ([P], C.c_size_t),
     "cf_register": ([P, P], C.c_int),

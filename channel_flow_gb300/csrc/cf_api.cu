@@ -30,6 +30,10 @@ struct cf_ctx {
     double *er_dev = nullptr;         // 5 doubles + device counter space
     double *er_host = nullptr;        // pinned
     cudaStream_t cap = nullptr;       // private stream for graph capture
+    int lu_schedule = CF_LU_WAVEFRONT;                // hyperplane sweep schedule
+    int *tile_order = nullptr;        // wavefront tiles sorted by plane (device)
+    long long *trace = nullptr;       // wavefront trace: [2 sweeps][tiles][4] stamps, when enabled
+    size_t trace_tiles = 0;
     cudaGraphExec_t dts_exec = nullptr;               // Dual_time_stepping as one graph
     std::vector<unsigned char> dts_key;               // arguments it was captured with
     std::string err;
@@ -71,10 +75,9 @@ int check_ptrs(cf_ctx *c, const double *const *p, int n, const char *who)
     return CF_OK;
 }
 
-// scratch of nfields fields, owned by the context (allocated on first use)
-double *scratch(cf_ctx *c, const char *key, int nfields)
+// scratch of a number of bytes, owned by the context (allocated on first use)
+void *scratch_bytes(cf_ctx *c, const char *key, size_t bytes)
 {
-    const size_t bytes = (size_t)nfields * c->d.total() * sizeof(double);
     auto &e = c->scratch[key];
     if (e.first && e.second >= bytes) return e.first;
     if (e.first) cudaFree(e.first);
@@ -86,6 +89,12 @@ double *scratch(cf_ctx *c, const char *key, int nfields)
     }
     e.second = bytes;
     return e.first;
+}
+
+// scratch of nfields fields
+double *scratch(cf_ctx *c, const char *key, int nfields)
+{
+    return static_cast<double *>(scratch_bytes(c, key, (size_t)nfields * c->d.total() * sizeof(double)));
 }
 
 // cells of plane m = i+j+k in i-major order, exactly the tables of
@@ -144,6 +153,7 @@ const char *cf_error_string(int code)
     case CF_ERR_NONFINITE: return "non-finite value";
     case CF_ERR_NOMEM: return "device allocation failed";
     case CF_ERR_STATE: return "call out of order";
+    case CF_ERR_TIMEOUT: return "a bounded device wait ran out";
     default: return "unknown error";
     }
 }
@@ -202,6 +212,8 @@ void cf_destroy(cf_ctx *c)
     if (c->er_dev) cudaFree(c->er_dev);
     if (c->er_host) cudaFreeHost(c->er_host);
     if (c->dts_exec) cudaGraphExecDestroy(c->dts_exec);
+    if (c->tile_order) cudaFree(c->tile_order);
+    if (c->trace) cudaFree(c->trace);
     if (c->cap) cudaStreamDestroy(c->cap);
     delete c;
 }
@@ -218,6 +230,37 @@ int cf_set_stream(cf_ctx *c, void *stream)
     if (!c) return CF_ERR_ARG;
     c->stream = (cudaStream_t)stream;
     return CF_OK;
+}
+
+int cf_set_lu_schedule(cf_ctx *c, int schedule)
+{
+    if (!c || (schedule != CF_LU_WAVEFRONT && schedule != CF_LU_PLANES)) return CF_ERR_ARG;
+    c->lu_schedule = schedule;
+    return CF_OK;
+}
+
+int cf_lu_trace(cf_ctx *c, int enable)
+{
+    if (!c) return CF_ERR_ARG;
+    if (!enable) {
+        if (c->trace) cudaFree(c->trace);
+        c->trace = nullptr;
+        c->trace_tiles = 0;
+    } else if (!c->trace_tiles) {
+        c->trace_tiles = 1;     // sized by the next Dual_time_stepping call
+    }
+    return CF_OK;
+}
+
+int cf_lu_trace_read(cf_ctx *c, long long *out, size_t count)
+{
+    if (!c || !out) return CF_ERR_ARG;
+    if (!c->trace) return fail(c, CF_ERR_STATE, "cf_lu_trace_read: no trace recorded");
+    const size_t n = 2 * 4 * c->trace_tiles;
+    if (count < n) return fail(c, CF_ERR_ARG, "cf_lu_trace_read: %zu values needed", n);
+    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "cf_lu_trace_read")) return rc;
+    return cuda_check(c, cudaMemcpy(out, c->trace, n * sizeof(long long), cudaMemcpyDeviceToHost),
+                      "cf_lu_trace_read");
 }
 
 int cf_set_stretching(cf_ctx *c, double gamma)
@@ -532,33 +575,119 @@ static int lu_finish_host(cf_ctx *c, const cf_lu_args &a, double *er[5], const c
     return lu_read_norms(c, er, who);
 }
 
-// The whole Dual_time_stepping call on stream s: assembly, coefficient
-// pack, one forward and one backward hyperplane sweep (one launch per
-// plane), NL <- NR, update and norms into er_dev.
+// tiling and scratch of the wavefront sweeps (cf_wave.cuh)
+static int wave_setup(cf_ctx *c, cf_wave_args &w)
+{
+    const cf_dims &d = c->d;
+    w.d = d;
+    w.nti = (d.X_out + CF_WAVE_TI - 1) / CF_WAVE_TI;
+    w.ntj = (d.Y_out + CF_WAVE_TJ - 1) / CF_WAVE_TJ;
+    w.ntk = (d.Z_out + CF_WAVE_TK - 1) / CF_WAVE_TK;
+    w.ntiles = w.nti * w.ntj * w.ntk;
+    if (!c->tile_order) {
+        // topological order of both sweeps: tiles by ti + tj + tk
+        std::vector<int> order;
+        order.reserve((size_t)w.ntiles);
+        for (int p = 0; p <= w.nti + w.ntj + w.ntk - 3; p++)
+            for (int a = 0; a < w.nti; a++)
+                for (int b = 0; b < w.ntj; b++) {
+                    const int k = p - a - b;
+                    if (k >= 0 && k < w.ntk) order.push_back((a * w.ntj + b) * w.ntk + k);
+                }
+        if (cudaMalloc(&c->tile_order, order.size() * sizeof(int)) != cudaSuccess) {
+            c->tile_order = nullptr;
+            return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: tile table allocation failed");
+        }
+        if (int rc = cuda_check(c, cudaMemcpy(c->tile_order, order.data(), order.size() * sizeof(int),
+                                              cudaMemcpyHostToDevice), "tile table")) return rc;
+    }
+    w.order = c->tile_order;
+    const size_t cells = (size_t)CF_WAVE_TI * CF_WAVE_TJ * CF_WAVE_TK;
+    const size_t T8 = sizeof(double);       // sized for double; the FP32 kernels use half
+    const size_t pack = (size_t)w.ntiles * cells * CF_WAVE_PACK * T8;
+    const size_t fx = (size_t)w.ntiles * 5 * CF_WAVE_TJ * CF_WAVE_TK * T8;
+    const size_t fy = (size_t)w.ntiles * 5 * CF_WAVE_TI * CF_WAVE_TK * T8;
+    const size_t fz = (size_t)w.ntiles * 5 * CF_WAVE_TI * CF_WAVE_TJ * T8;
+    const size_t nl = (size_t)w.ntiles * 5 * cells * T8;
+    const size_t flags = (((size_t)w.ntiles + 2) * sizeof(int) + 255) / 256 * 256;
+    unsigned char *base = static_cast<unsigned char *>(
+        scratch_bytes(c, "lu_wave", 2 * pack + fx + fy + fz + nl + flags));
+    if (!base) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: wavefront scratch allocation failed");
+    w.packF = base;
+    w.packB = base + pack;
+    w.inx = base + 2 * pack;
+    w.iny = base + 2 * pack + fx;
+    w.inz = base + 2 * pack + fx + fy;
+    w.nl = base + 2 * pack + fx + fy + fz;
+    unsigned char *f = base + 2 * pack + fx + fy + fz + nl;
+    w.flags = reinterpret_cast<int *>(f);
+    w.counter = w.flags + w.ntiles;
+    w.err = w.flags + w.ntiles + 1;
+    w.trace = nullptr;
+    if (c->trace_tiles) {
+        if (c->trace_tiles != (size_t)w.ntiles) {
+            if (c->trace) cudaFree(c->trace);
+            c->trace = nullptr;
+            if (cudaMalloc(&c->trace, 2 * 4 * (size_t)w.ntiles * sizeof(long long)) != cudaSuccess) {
+                c->trace = nullptr;
+                c->trace_tiles = 0;
+                return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: trace allocation failed");
+            }
+            c->trace_tiles = (size_t)w.ntiles;
+        }
+        w.trace = c->trace;
+    }
+    return CF_OK;
+}
+
+// The whole Dual_time_stepping call on stream s: assembly, one forward and
+// one backward hyperplane sweep, NL <- NR, update and norms into er_dev.
 //
 // The reference runs the forward/backward pair twice
 // (Dual_time_stepping.cpp:563-1275) so that, with several ranks, the
 // second pass sees the neighbours' interface planes of the first.  On one
 // domain the second pass reproduces the first bit for bit: the sweeps read
 // N only at ghost cells (zero, never written) and at cells the same sweep
-// has already recomputed from MR and the fixed pack.  It is run once.
-static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, double dt, cudaStream_t s)
+// has already recomputed from MR and fixed coefficients.  It is run once.
+//
+// Schedules: CF_LU_WAVEFRONT, one persistent tiled launch per sweep
+// (cf_wave.cuh); CF_LU_PLANES, one launch per hyperplane from a per-cell
+// coefficient pack.  Both give the same bits.
+static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, const cf_wave_args &w, double dt,
+                               cudaStream_t s)
 {
     const cf_dims &d = c->d;
     const bool ex = exact(c);
     const int pr = ex ? 0 : kprec(c);
     cudaError_t e = ex ? cf_exact::lu_prepare(d, a, dt, true, 0, s) : cf_fast::lu_prepare(d, a, dt, true, pr, s);
-    if (e == cudaSuccess) e = ex ? cf_exact::lu_pack(d, a, pack, dt, 0, s) : cf_fast::lu_pack(d, a, pack, dt, pr, s);
-    const int mlast = d.gend + d.ny + d.nz;
-    for (int m = 7; m <= mlast && e == cudaSuccess; m++) {
-        const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
-        e = ex ? cf_exact::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, true, 0, s)
-               : cf_fast::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, true, pr, s);
-    }
-    for (int m = mlast; m >= 7 && e == cudaSuccess; m--) {
-        const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
-        e = ex ? cf_exact::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, false, 0, s)
-               : cf_fast::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, false, pr, s);
+    if (c->lu_schedule == CF_LU_WAVEFRONT) {
+        const size_t fl = ((size_t)w.ntiles + 1) * sizeof(int);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.err, 0, sizeof(int), s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, false, 0, s)
+                                     : cf_fast::lu_wave_pack(d, a, w, dt, false, pr, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, w, true, 0, s)
+                                     : cf_fast::lu_wave_sweep(a, w, true, pr, s);
+        cf_wave_args wb = w;
+        if (w.trace) wb.trace = w.trace + 4 * (size_t)w.ntiles;
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, 0, s)
+                                     : cf_fast::lu_wave_pack(d, a, w, dt, true, pr, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, wb, false, 0, s)
+                                     : cf_fast::lu_wave_sweep(a, wb, false, pr, s);
+    } else {
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_pack(d, a, pack, dt, 0, s) : cf_fast::lu_pack(d, a, pack, dt, pr, s);
+        const int mlast = d.gend + d.ny + d.nz;
+        for (int m = 7; m <= mlast && e == cudaSuccess; m++) {
+            const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
+            e = ex ? cf_exact::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, true, 0, s)
+                   : cf_fast::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, true, pr, s);
+        }
+        for (int m = mlast; m >= 7 && e == cudaSuccess; m--) {
+            const int cnt = c->nijk[2 * (size_t)m + 1], first = c->nijk[2 * (size_t)m] - cnt + 1;
+            e = ex ? cf_exact::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, false, 0, s)
+                   : cf_fast::lu_plane_packed(d, a, pack, c->ijk_dev, first, cnt, false, pr, s);
+        }
     }
     if (e == cudaSuccess) e = cf_fast::lu_copy(d, a, s);
     if (e == cudaSuccess) e = ex ? cf_exact::lu_finish(d, a, c->er_dev, s) : cf_fast::lu_finish(d, a, c->er_dev, s);
@@ -566,7 +695,7 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, dou
 }
 
 // capture enqueue_dts into c->dts_exec (kept while the arguments repeat)
-static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, double dt)
+static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, const cf_wave_args &w, double dt)
 {
     if (!c->cap) {
         if (int rc = cuda_check(c, cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking), "capture stream"))
@@ -579,7 +708,7 @@ static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, double dt)
     c->dts_key.clear();
     if (int rc = cuda_check(c, cudaStreamBeginCapture(c->cap, cudaStreamCaptureModeThreadLocal), "graph capture"))
         return rc;
-    const cudaError_t le = enqueue_dts(c, a, pack, dt, c->cap);
+    const cudaError_t le = enqueue_dts(c, a, pack, w, dt, c->cap);
     cudaGraph_t g = nullptr;
     const cudaError_t ee = cudaStreamEndCapture(c->cap, &g);
     if (le != cudaSuccess || ee != cudaSuccess) {
@@ -608,22 +737,46 @@ int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er
     }
     cf_lu_args a;
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
-    double *pack = scratch(c, "lu_pack", CF_LU_PACK);
-    if (!pack) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: coefficient pack allocation failed");
+    double *pack = nullptr;
+    cf_wave_args w{};
+    if (c->lu_schedule == CF_LU_WAVEFRONT) {
+        if (int rc = wave_setup(c, w)) return rc;
+    } else {
+        pack = scratch(c, "lu_pack", CF_LU_PACK);
+        if (!pack) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: coefficient pack allocation failed");
+    }
     // the graph bakes in every pointer and scalar: recapture when they change
-    std::vector<unsigned char> key(sizeof(cf_lu_args) + sizeof(double *) + sizeof(double) + sizeof(int), 0);
+    std::vector<unsigned char> key(sizeof(cf_lu_args) + sizeof(double *) + sizeof(void *) + sizeof(double) +
+                                   2 * sizeof(int), 0);
     unsigned char *kp = key.data();
     std::memcpy(kp, &a, sizeof a);
-    std::memcpy(kp + sizeof a, &pack, sizeof pack);
-    std::memcpy(kp + sizeof a + sizeof pack, &deltaT, sizeof deltaT);
-    std::memcpy(kp + sizeof a + sizeof pack + sizeof deltaT, &c->prec, sizeof c->prec);
+    kp += sizeof a;
+    std::memcpy(kp, &pack, sizeof pack);
+    kp += sizeof pack;
+    std::memcpy(kp, &w.packF, sizeof w.packF);
+    kp += sizeof w.packF;
+    std::memcpy(kp, &deltaT, sizeof deltaT);
+    kp += sizeof deltaT;
+    std::memcpy(kp, &c->prec, sizeof c->prec);
+    kp += sizeof c->prec;
+    std::memcpy(kp, &c->lu_schedule, sizeof c->lu_schedule);
+    key.insert(key.end(), reinterpret_cast<const unsigned char *>(&w.trace),
+               reinterpret_cast<const unsigned char *>(&w.trace) + sizeof w.trace);
     if (!c->dts_exec || key != c->dts_key) {
-        if (int rc = capture_dts(c, a, pack, deltaT)) return rc;
+        if (int rc = capture_dts(c, a, pack, w, deltaT)) return rc;
         c->dts_key = key;
     }
     if (int rc = cuda_check(c, cudaGraphLaunch(c->dts_exec, c->stream), "Dual_time_stepping")) return rc;
+    int *err_host = reinterpret_cast<int *>(c->er_host + 12);
+    *err_host = 0;
+    if (c->lu_schedule == CF_LU_WAVEFRONT)
+        if (int rc = cuda_check(c, cudaMemcpyAsync(err_host, w.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+                                "Dual_time_stepping")) return rc;
     double *er[5] = {er1, er2, er3, er4, er5};
-    return lu_read_norms(c, er, "Dual_time_stepping");
+    if (int rc = lu_read_norms(c, er, "Dual_time_stepping")) return rc;
+    if (*err_host)
+        return fail(c, CF_ERR_TIMEOUT, "Dual_time_stepping: a wavefront wait ran out (code %d)", *err_host);
+    return CF_OK;
 }
 
 int cf_DPLUSGS(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,

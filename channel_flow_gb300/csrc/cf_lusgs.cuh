@@ -189,43 +189,62 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     }
 }
 
+// x / den of the sweep sums: the division itself in the no-FMA build,
+// a multiplication by the reciprocal in the contracted and FP32 builds
+template <typename T>
+struct lu_den {
+    T den, rden;
+    __device__ __forceinline__ explicit lu_den(T d) : den(d), rden(T(1) / d) {}
+};
+template <typename T>
+__device__ __forceinline__ T lu_div(T x, const lu_den<T> &d)
+{
+#ifdef CF_FAST_MATH
+    return x * d.rden;
+#else
+    return x / d.den;
+#endif
+}
+
 // L*N from the split Jacobians A, B, C of cells i-1, j-1, k-1 and their
 // N values a, b, c (Dual_time_stepping.cpp:751-811)
 template <typename T>
 __device__ __forceinline__ void lu_lower_sum(const lsplit<T> &A, const lsplit<T> &B, const lsplit<T> &C,
-                                             const T *a, const T *b, const T *c, T dXI, T dET, T dZT, T *LL)
+                                             const T *a, const T *b, const T *c, T dXI_, T dET_, T dZT_, T *LL)
 {
-    LL[0] = (-A.p11 * a[0] - A.p12 * a[1] - A.p13 * a[2] - A.p14 * a[3]) / dXI +
-            (-B.p11 * b[0] - B.p12 * b[1] - B.p13 * b[2] - B.p14 * b[3]) / dET +
-            (-C.p11 * c[0] - C.p12 * c[1] - C.p13 * c[2] - C.p14 * c[3]) / dZT;
-    LL[1] = (-A.p21 * a[0] - A.p22 * a[1]) / dXI + (-B.p21 * b[0] - B.p22 * b[1]) / dET +
-            (-C.p21 * c[0] - C.p22 * c[1]) / dZT;
-    LL[2] = (-A.p31 * a[0] - A.p33 * a[2]) / dXI + (-B.p31 * b[0] - B.p33 * b[2]) / dET +
-            (-C.p31 * c[0] - C.p33 * c[2]) / dZT;
-    LL[3] = (-A.p41 * a[0] - A.p44 * a[3]) / dXI + (-B.p41 * b[0] - B.p44 * b[3]) / dET +
-            (-C.p41 * c[0] - C.p44 * c[3]) / dZT;
-    LL[4] = (-A.p51 * a[0] - A.p52 * a[1] - A.p53 * a[2] - A.p54 * a[3] - A.p55 * a[4]) / dXI +
-            (-B.p51 * b[0] - B.p52 * b[1] - B.p53 * b[2] - B.p54 * b[3] - B.p55 * b[4]) / dET +
-            (-C.p51 * c[0] - C.p52 * c[1] - C.p53 * c[2] - C.p54 * c[3] - C.p55 * c[4]) / dZT;
+    const lu_den<T> dXI(dXI_), dET(dET_), dZT(dZT_);
+    LL[0] = lu_div(-A.p11 * a[0] - A.p12 * a[1] - A.p13 * a[2] - A.p14 * a[3], dXI) +
+            lu_div(-B.p11 * b[0] - B.p12 * b[1] - B.p13 * b[2] - B.p14 * b[3], dET) +
+            lu_div(-C.p11 * c[0] - C.p12 * c[1] - C.p13 * c[2] - C.p14 * c[3], dZT);
+    LL[1] = lu_div(-A.p21 * a[0] - A.p22 * a[1], dXI) + lu_div(-B.p21 * b[0] - B.p22 * b[1], dET) +
+            lu_div(-C.p21 * c[0] - C.p22 * c[1], dZT);
+    LL[2] = lu_div(-A.p31 * a[0] - A.p33 * a[2], dXI) + lu_div(-B.p31 * b[0] - B.p33 * b[2], dET) +
+            lu_div(-C.p31 * c[0] - C.p33 * c[2], dZT);
+    LL[3] = lu_div(-A.p41 * a[0] - A.p44 * a[3], dXI) + lu_div(-B.p41 * b[0] - B.p44 * b[3], dET) +
+            lu_div(-C.p41 * c[0] - C.p44 * c[3], dZT);
+    LL[4] = lu_div(-A.p51 * a[0] - A.p52 * a[1] - A.p53 * a[2] - A.p54 * a[3] - A.p55 * a[4], dXI) +
+            lu_div(-B.p51 * b[0] - B.p52 * b[1] - B.p53 * b[2] - B.p54 * b[3] - B.p55 * b[4], dET) +
+            lu_div(-C.p51 * c[0] - C.p52 * c[1] - C.p53 * c[2] - C.p54 * c[3] - C.p55 * c[4], dZT);
 }
 
 // U*N from the split Jacobians of cells i+1, j+1, k+1 (Dual_time_stepping.cpp:1116-1177)
 template <typename T>
 __device__ __forceinline__ void lu_upper_sum(const lsplit<T> &A, const lsplit<T> &B, const lsplit<T> &C,
-                                             const T *a, const T *b, const T *c, T dXI, T dET, T dZT, T *UU)
+                                             const T *a, const T *b, const T *c, T dXI_, T dET_, T dZT_, T *UU)
 {
-    UU[0] = (+A.m11 * a[0] + A.p12 * a[1] + A.p13 * a[2] + A.p14 * a[3]) / dXI +
-            (+B.m11 * b[0] + B.p12 * b[1] + B.p13 * b[2] + B.p14 * b[3]) / dET +
-            (+C.m11 * c[0] + C.p12 * c[1] + C.p13 * c[2] + C.p14 * c[3]) / dZT;
-    UU[1] = (+A.p21 * a[0] + A.m22 * a[1]) / dXI + (+B.p21 * b[0] + B.m22 * b[1]) / dET +
-            (+C.p21 * c[0] + C.m22 * c[1]) / dZT;
-    UU[2] = (+A.p31 * a[0] + A.m22 * a[2]) / dXI + (+B.p31 * b[0] + B.m22 * b[2]) / dET +
-            (+C.p31 * c[0] + C.m22 * c[2]) / dZT;
-    UU[3] = (+A.p41 * a[0] + A.m22 * a[3]) / dXI + (+B.p41 * b[0] + B.m22 * b[3]) / dET +
-            (+C.p41 * c[0] + C.m22 * c[3]) / dZT;
-    UU[4] = (+A.p51 * a[0] + A.p52 * a[1] + A.p53 * a[2] + A.p54 * a[3] + A.m22 * a[4]) / dXI +
-            (+B.p51 * b[0] + B.p52 * b[1] + B.p53 * b[2] + B.p54 * b[3] + B.m22 * b[4]) / dET +
-            (+C.p51 * c[0] + C.p52 * c[1] + C.p53 * c[2] + C.p54 * c[3] + C.m22 * c[4]) / dZT;
+    const lu_den<T> dXI(dXI_), dET(dET_), dZT(dZT_);
+    UU[0] = lu_div(+A.m11 * a[0] + A.p12 * a[1] + A.p13 * a[2] + A.p14 * a[3], dXI) +
+            lu_div(+B.m11 * b[0] + B.p12 * b[1] + B.p13 * b[2] + B.p14 * b[3], dET) +
+            lu_div(+C.m11 * c[0] + C.p12 * c[1] + C.p13 * c[2] + C.p14 * c[3], dZT);
+    UU[1] = lu_div(+A.p21 * a[0] + A.m22 * a[1], dXI) + lu_div(+B.p21 * b[0] + B.m22 * b[1], dET) +
+            lu_div(+C.p21 * c[0] + C.m22 * c[1], dZT);
+    UU[2] = lu_div(+A.p31 * a[0] + A.m22 * a[2], dXI) + lu_div(+B.p31 * b[0] + B.m22 * b[2], dET) +
+            lu_div(+C.p31 * c[0] + C.m22 * c[2], dZT);
+    UU[3] = lu_div(+A.p41 * a[0] + A.m22 * a[3], dXI) + lu_div(+B.p41 * b[0] + B.m22 * b[3], dET) +
+            lu_div(+C.p41 * c[0] + C.m22 * c[3], dZT);
+    UU[4] = lu_div(+A.p51 * a[0] + A.p52 * a[1] + A.p53 * a[2] + A.p54 * a[3] + A.m22 * a[4], dXI) +
+            lu_div(+B.p51 * b[0] + B.p52 * b[1] + B.p53 * b[2] + B.p54 * b[3] + B.m22 * b[4], dET) +
+            lu_div(+C.p51 * c[0] + C.p52 * c[1] + C.p53 * c[2] + C.p54 * c[3] + C.m22 * c[4], dZT);
 }
 
 template <typename T>

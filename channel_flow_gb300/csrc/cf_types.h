@@ -95,6 +95,22 @@ struct cf_lu_args {
     double *partial;         // scratch: per-block partial norm sums (5 per block)
 };
 
+// tiled wavefront of the hyperplane sweeps (cf_wave.cuh)
+constexpr int CF_WAVE_TI = 4, CF_WAVE_TJ = 8, CF_WAVE_TK = 8, CF_WAVE_PACK = 44;
+struct cf_wave_args {
+    cf_dims d;
+    int nti, ntj, ntk, ntiles;
+    const int *order;        // tile ids sorted by ti + tj + tk
+    void *packF, *packB;     // [ntiles][tile cells][CF_WAVE_PACK] of the kernel's type
+    void *inx, *iny, *inz;   // terms arriving at a tile's x, y, z face: [ntiles][5][64 | 32 | 32]
+    void *nl;                // forward N of every tile, [ntiles][5][tile cells]
+    int *flags;              // per tile: 1 when done; [ntiles] = claim counter, [ntiles+1] = error word
+    int *counter;
+    int *err;                // bit 0: dependency wait ran out, bit 1: pack copy wait ran out
+    long long *trace;        // optional: per tile 4 global-timer stamps (claimed, inputs ready,
+                             // pack landed, done); NULL when tracing is off
+};
+
 struct cf_rk3_args {
     double *U_[5];
     const double *U[5];

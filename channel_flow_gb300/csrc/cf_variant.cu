@@ -1,11 +1,14 @@
 // One build variant of the hot-path kernels (see cf_launch.h).  The build
 // compiles this file twice, with -DCF_NS=cf_exact --fmad=false and with
 // -DCF_NS=cf_fast -DCF_WITH_FLOAT.
+#include <algorithm>
+
 #include "cf_flux.cuh"
 #include "cf_bc.cuh"
 #include "cf_visc.cuh"
 #include "cf_filter.cuh"
 #include "cf_lusgs.cuh"
+#include "cf_wave.cuh"
 #include "cf_launch.h"
 
 #ifdef CF_WITH_FLOAT
@@ -133,6 +136,49 @@ cudaError_t lu_plane_packed(const cf_dims &d, const cf_lu_args &a, const double 
 {
     return CF_DISPATCH(prec, lu_plane_packed_t<double>(d, a, pack, ijk, first, count, forward, s),
                        lu_plane_packed_t<float>(d, a, pack, ijk, first, count, forward, s));
+}
+
+template <typename T>
+static cudaError_t lu_wave_pack_t(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt,
+                                  bool upper, cudaStream_t s)
+{
+    if (upper) {
+        cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+        k_lu_tile_ghost_upper<T><<<box_grid(b), box_block(), 0, s>>>(a, w, b);
+        return cudaGetLastError();
+    }
+    const size_t smem = (size_t)WV_CELLS * WV_PACK * sizeof(T);
+    cudaError_t e = cudaFuncSetAttribute(k_lu_tile_pack<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_lu_tile_pack<T><<<w.ntiles, WV_CELLS, smem, s>>>(a, w, dt);
+    return cudaGetLastError();
+}
+cudaError_t lu_wave_pack(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt, bool upper,
+                         int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_wave_pack_t<double>(d, a, w, dt, upper, s),
+                       lu_wave_pack_t<float>(d, a, w, dt, upper, s));
+}
+
+template <typename T>
+static cudaError_t lu_wave_sweep_t(const cf_lu_args &a, const cf_wave_args &w, bool fwd, cudaStream_t s)
+{
+    const size_t smem = (size_t)WV_SM_TOTAL * sizeof(T);
+    void (*kf)(cf_lu_args, wave_args) = fwd ? k_lu_wave<T, true> : k_lu_wave<T, false>;
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, occ = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int threads = 32 * WV_WARPS;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, threads, smem)) != cudaSuccess) return e;
+    const int blocks = std::min(w.ntiles, std::max(1, occ) * sms);
+    kf<<<blocks, threads, smem, s>>>(a, w);
+    return cudaGetLastError();
+}
+cudaError_t lu_wave_sweep(const cf_lu_args &a, const cf_wave_args &w, bool fwd, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_wave_sweep_t<double>(a, w, fwd, s), lu_wave_sweep_t<float>(a, w, fwd, s));
 }
 
 template <typename T>

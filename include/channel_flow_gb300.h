@@ -37,6 +37,7 @@ extern "C" {
 #define CF_ERR_NONFINITE 3   /* cf_check_finite found a NaN or Inf */
 #define CF_ERR_NOMEM 4       /* device allocation failed */
 #define CF_ERR_STATE 5       /* call out of order (e.g. sweep before Hyperplane) */
+#define CF_ERR_TIMEOUT 6     /* a bounded device-side wait ran out (results invalid) */
 
 /* arithmetic modes of the flux, viscous, filter and LU-SGS kernels */
 #define CF_PREC_FP64_EXACT 0 /* FP64, no fused multiply-add: equals the reference bit for bit */
@@ -75,6 +76,19 @@ int cf_set_stream(cf_ctx *ctx, void *cuda_stream); /* cudaStream_t; NULL = legac
 /* Wall-normal stretching parameter of the analytic metrics (Jacobian_u/v/w):
  * the reference hard-codes 1.5 (Jacobian_u.cpp:19). */
 int cf_set_stretching(cf_ctx *ctx, double gamma);
+/* Schedule of the hyperplane sweeps of Dual_time_stepping (same results):
+ * CF_LU_WAVEFRONT (default) runs each sweep as one persistent launch over
+ * 4x8x8-cell tiles; CF_LU_PLANES launches one kernel per hyperplane. */
+#define CF_LU_WAVEFRONT 0
+#define CF_LU_PLANES 1
+int cf_set_lu_schedule(cf_ctx *ctx, int schedule);
+/* Wavefront trace (profiling): when enabled, each Dual_time_stepping call
+ * records per tile four device global-timer stamps in ns (claimed, inputs
+ * ready, coefficients staged, done), forward sweep then backward sweep.
+ * cf_lu_trace_read copies 2*4*tiles values, tiles = ceil(cells_x/4) *
+ * ceil(cells_y/8) * ceil(cells_z/8), tile id (ti*ntj + tj)*ntk + tk. */
+int cf_lu_trace(cf_ctx *ctx, int enable);
+int cf_lu_trace_read(cf_ctx *ctx, long long *out, size_t count);
 int cf_synchronize(cf_ctx *ctx);
 const char *cf_last_error(const cf_ctx *ctx);
 const char *cf_error_string(int code);

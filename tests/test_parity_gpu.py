@@ -159,3 +159,50 @@ def test_gpu_fp32_filter_switch(port, ctx_factory):
     for i in r.outputs:
         frac = np.count_nonzero(want[i] != got[i]) / want[i].size
         assert frac <= 0.01, (i, frac)
+
+
+@pytest.mark.parametrize("schedule", ["wavefront", "planes"])
+@pytest.mark.parametrize("dims", cases.GRIDS + [(13, 9, 17)])
+def test_gpu_dts_schedules_exact(dims, schedule, port, cuda_lib):
+    """Both sweep schedules of Dual_time_stepping (tiled wavefront, one
+    launch per hyperplane) equal the oracle bit for bit, on grids with
+    partial tiles."""
+    import channel_flow_gb300 as cf
+    r = routines.BY_NAME["Dual_time_stepping"]
+    g = cases.grid(dims)
+    ctx = cf.Context(g, precision="fp64_exact")
+    try:
+        ctx.set_lu_schedule(schedule)
+        want, got, e_want, e_got = _run_both(port, ctx, r, g, seed=11)
+        diff = routines.compare(r, g, got, want)
+        assert max(diff.values()) == 0, diff
+        np.testing.assert_allclose(e_got, e_want, rtol=1e-12, atol=0)
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gpu_dts_schedules_agree(precision, cuda_lib):
+    """The two schedules agree in the contracted and FP32 builds to the
+    rounding of those builds (FMA contraction may pair the per-direction
+    sums differently in the two kernels)."""
+    import channel_flow_gb300 as cf
+    r = routines.BY_NAME["Dual_time_stepping"]
+    dims = (13, 9, 17)
+    g = cases.grid(dims)
+    outs = []
+    for schedule in ("wavefront", "planes"):
+        ctx = cf.Context(g, precision=precision)
+        try:
+            ctx.set_lu_schedule(schedule)
+            a = cases.copy_case(r.build(g, 4))
+            er = routines.run_gpu(ctx, r, a)
+            outs.append((a, er))
+        finally:
+            ctx.close()
+    (a0, e0), (a1, e1) = outs
+    tol = RTOL_FP64 if precision == "fp64" else 1e-5
+    for i in r.outputs:
+        scale = max(float(np.max(np.abs(a1[i]))), 1e-300)
+        assert float(np.max(np.abs(a0[i] - a1[i]))) / scale <= tol, i
+    np.testing.assert_allclose(np.asarray(e0), np.asarray(e1), rtol=tol * 10, atol=0)
