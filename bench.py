@@ -134,9 +134,9 @@ def rhs_calls(ctx, w, ptr):
 
 
 # kernels launched per step: x halo 1, y wall 1, z periodic 1, Filter
-# (1 shell + 2 x 6 x 3 passes + 2 energy + 3 ghost fills + 3 thresholds = 45),
-# 3 flux kernels, viscous 3
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 45 + 3 + 3
+# (1 coefficients + 2 x 6 fused levels + 2 energy + 3 ghost fills + 3
+# thresholds = 21), 3 flux kernels, viscous 3
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 21 + 3 + 3
 
 
 def run_calls(ctx, calls):
@@ -270,12 +270,13 @@ def time_cpu(g, host, steps, warmup):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_exact", "fp32"])
     ap.add_argument("--grid", default="x".join(map(str, GRID)))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
 
@@ -424,13 +425,10 @@ def timed_steps(ctx, calls, steps, stream, torch):
     return t_start.elapsed_time(t_end), per
 
 
-def secondary(ctx, g, w, calls, stream, torch, args):
-    """FP32 RHS on the same workload, and the dual-time LU-SGS
-    pseudo-iteration (RHS + Dual_time_stepping) in FP64 and FP32."""
+def pseudo_iteration(ctx, g, w, calls, stream, torch, steps):
+    """RHS and Dual_time_stepping timings of one context, in its current
+    precision; the state is restored between the LU-SGS calls."""
     from channel_flow_gb300 import _lib
-    out = {}
-    steps = max(2, min(args.steps, 5))
-    prec0 = ctx.precision
     z = lambda: torch.zeros(g.shape, dtype=torch.float64, device="cuda")
     U0 = [u.clone() for u in w.U]
     Un = [u.clone() for u in w.U]
@@ -440,40 +438,68 @@ def secondary(ctx, g, w, calls, stream, torch, args):
     ptrs = _lib.ptr_array([a.data_ptr() for a in arrays])
     er = np.zeros(5)
     e = [er[n:].ctypes.data for n in range(5)]
-    Nijk, ijk = ctx.Hyperplane()
     dt = 0.00000005
-    for prec in ("fp64", "fp32"):
-        ctx.set_precision(prec)
-        for _ in range(2):
-            run_calls(ctx, calls)
-        torch.cuda.synchronize()
-        tot, per = timed_steps(ctx, calls, steps, stream, torch)
-        rhs_ms = tot / steps
-        # one pseudo-iteration's LU-SGS; the state is restored between calls
-        lu_ms = []
-        for it in range(3):
-            for u, u0 in zip(w.U, U0):
-                u.copy_(u0)
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            t0.record(stream)
-            rc = ctx.lib.cf_Dual_time_stepping(ctx.h, 0, dt, *e, Nijk.ctypes.data, ijk.ctypes.data, ptrs)
-            t1.record(stream)
-            torch.cuda.synchronize()
-            _lib.check(ctx.lib, ctx.h, rc)
-            if it > 0:
-                lu_ms.append(t0.elapsed_time(t1))
+    for _ in range(2):
+        run_calls(ctx, calls)
+    torch.cuda.synchronize()
+    tot, per = timed_steps(ctx, calls, steps, stream, torch)
+    rhs_ms = tot / steps
+    lu_ms = []
+    for it in range(3):
         for u, u0 in zip(w.U, U0):
             u.copy_(u0)
-        dts = sum(lu_ms) / len(lu_ms)
-        out[prec] = {"rhs_ms": rhs_ms, "rhs_mcell_updates_per_s": g.cells / (rhs_ms * 1e-3) / 1e6,
-                     "dual_time_lusgs_ms": dts, "pseudo_iteration_ms": rhs_ms + dts,
-                     "physical_step_s": LU_SUBITERATIONS * (rhs_ms + dts) * 1e-3,
-                     "subiterations_per_step": LU_SUBITERATIONS,
-                     "per_routine_ms": {k: round(v, 4) for k, v in per.items()}}
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        rc = ctx.lib.cf_Dual_time_stepping(ctx.h, 0, dt, *e, None, None, ptrs)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        _lib.check(ctx.lib, ctx.h, rc)
+        if it > 0:
+            lu_ms.append(t0.elapsed_time(t1))
+    for u, u0 in zip(w.U, U0):
+        u.copy_(u0)
+    del Un, Uq, lu, arrays
+    dts = sum(lu_ms) / len(lu_ms)
+    return {"rhs_ms": rhs_ms, "rhs_mcell_updates_per_s": g.cells / (rhs_ms * 1e-3) / 1e6,
+            "dual_time_lusgs_ms": dts, "pseudo_iteration_ms": rhs_ms + dts,
+            "physical_step_s": LU_SUBITERATIONS * (rhs_ms + dts) * 1e-3,
+            "per_routine_ms": {k: round(v, 4) for k, v in per.items()}}
+
+
+def secondary(ctx, g, w, calls, stream, torch, args):
+    """Per precision: the RHS and one dual-time pseudo-iteration (RHS +
+    hyperplane LU-SGS) on the benchmark grid, and on the 256 x 192 x 192
+    mixed-precision channel (9.4 M cells)."""
+    import channel_flow_gb300 as cf
+    from channel_flow_gb300 import synthetic as syn
+    out = {}
+    steps = max(2, min(args.steps, 5))
+    prec0 = ctx.precision
+    key = "x".join(str(v) for v in (g.X_out, g.Y_out, g.Z_out))
+    out[key] = {}
+    for prec in ("fp64", "fp32"):
+        ctx.set_precision(prec)
+        out[key][prec] = pseudo_iteration(ctx, g, w, calls, stream, torch, steps)
     ctx.set_precision(prec0)
+    if (g.X_out, g.Y_out, g.Z_out) != (256, 192, 192) and not args.no_large:
+        g2 = syn.channel_grid(256, 192, 192)
+        ctx2 = cf.Context(g2, precision="fp64", gamma=GAMMA)
+        w2 = DeviceWorkload(ctx2, g2, make_host_workload(g2), torch)
+        calls2 = rhs_calls(ctx2, w2, lambda x: x.data_ptr())
+        out["256x192x192"] = {}
+        for prec in ("fp64", "fp32"):
+            ctx2.set_precision(prec)
+            out["256x192x192"][prec] = pseudo_iteration(ctx2, g2, w2, calls2, stream, torch, 3)
+        ctx2.close()
+        del w2, calls2
+        torch.cuda.empty_cache()
+    for k, v in out.items():
+        if "fp64" in v and "fp32" in v:
+            v["physical_step_fp64_over_fp32"] = v["fp64"]["physical_step_s"] / v["fp32"]["physical_step_s"]
     out["note"] = ("physical step = 10 LU-SGS sub-iterations x (RHS + Dual_time_stepping), the schedule of "
-                   "configs 0 and 1; the hyperplane sweep launches one kernel per plane")
+                   "configs 0 and 1; FP32 = flux/viscous/filter/LU-SGS sweeps in FP32, state update and "
+                   "norms FP64; no learned initial guess")
     return out
 
 
