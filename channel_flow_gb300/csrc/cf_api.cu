@@ -392,6 +392,13 @@ static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double
     for (int n = 0; n < 9; n++) a.m[n] = R(c, p32[17 + n]);
     for (int n = 0; n < 5; n++) a.F[n] = R(c, p32[26 + n]);
     a.Ep = p32[31] ? R(c, p32[31]) : nullptr;
+    a.wz[0] = a.wz[1] = nullptr;
+    if (dir == 2 && limited) {
+        double *wz = scratch(c, "flux_zweights", 2);
+        if (!wz) return fail(c, CF_ERR_NOMEM, "%s: scratch allocation failed", who);
+        a.wz[0] = wz;
+        a.wz[1] = wz + c->d.total();
+    }
     cudaError_t e = exact(c) ? cf_exact::flux(c->d, a, dir, limited, 0, c->stream)
                              : cf_fast::flux(c->d, a, dir, limited, kprec(c), c->stream);
     return cuda_check(c, e, who);

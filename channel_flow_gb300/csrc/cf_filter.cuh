@@ -21,12 +21,14 @@
 // J(j+1)/J(j) and no division.  ST is the storage type of the level and
 // accumulator fields (float in the FP32 build).
 #pragma once
+#include <algorithm>
+
 #include "cf_common.cuh"
 
 
 namespace CF_NS {
 
-constexpr int FT_J = 8, FT_K = 32, FT_I = 16;    // tile rows (j), columns (k), planes per block (i)
+constexpr int FT_J = 8, FT_K = 32;    // tile rows (j), columns (k); planes per block set at launch
 constexpr int FT_HJ = FT_J + 2, FT_HK = FT_K + 2, FT_HALO = FT_HJ * FT_HK;
 
 template <typename ST>
@@ -75,14 +77,14 @@ __device__ __forceinline__ T filt_load(const cf_dims &d, const double *U, const 
 }
 
 template <typename T, typename SRC, typename ST, bool WIDE, bool EXACT>
-__global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST> f, int level)
+__global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST> f, int level, int fti)
 {
     __shared__ T sgx[4][FT_HJ][FT_HK];     // x pass, rows j0-1..j0+8, columns k0-1..k0+32
     __shared__ T sgy[4][FT_J][FT_HK];      // y pass, rows j0..j0+7
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
     const int k0 = 2 + (int)blockIdx.x * FT_K, j0 = 2 + (int)blockIdx.y * FT_J;
-    const int i0 = 3 + (int)blockIdx.z * FT_I;
-    const int i1 = min(i0 + FT_I - 1, d.gend);
+    const int i0 = 3 + (int)blockIdx.z * fti;
+    const int i1 = min(i0 + fti - 1, d.gend);
     // halo positions owned by this thread: tid and tid + 256
     int pj[2], pk[2];
     bool pv[2];
@@ -251,11 +253,21 @@ __global__ void k_filter_ep(cf_dims d, const double *__restrict__ Eh, const doub
 template <typename T, typename SRC, typename ST, bool EXACT>
 static void filter_level_launch(const cf_dims &d, const filt_fields<ST> &f, bool wide, int level, cudaStream_t s)
 {
-    const dim3 g((unsigned)((d.Z_out + FT_K - 1) / FT_K), (unsigned)((d.Y_out + FT_J - 1) / FT_J),
-                 (unsigned)((d.X_out + FT_I - 1) / FT_I));
+    // planes per block: enough blocks for about four per SM
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 132;
+    }
+    const int tk = (d.Z_out + FT_K - 1) / FT_K, tj = (d.Y_out + FT_J - 1) / FT_J;
+    const int chunks = std::max(1, std::min(d.X_out, (4 * sms + tk * tj - 1) / (tk * tj)));
+    const int fti = (d.X_out + chunks - 1) / chunks;
+    const dim3 g((unsigned)tk, (unsigned)tj, (unsigned)((d.X_out + fti - 1) / fti));
     const dim3 t(32, 8);
-    if (wide) k_filter_level<T, SRC, ST, true, EXACT><<<g, t, 0, s>>>(d, f, level);
-    else k_filter_level<T, SRC, ST, false, EXACT><<<g, t, 0, s>>>(d, f, level);
+    if (wide) k_filter_level<T, SRC, ST, true, EXACT><<<g, t, 0, s>>>(d, f, level, fti);
+    else k_filter_level<T, SRC, ST, false, EXACT><<<g, t, 0, s>>>(d, f, level, fti);
 }
 
 // T: arithmetic type, ST: storage of the scratch levels, EXACT: reference

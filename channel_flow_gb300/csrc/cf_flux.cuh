@@ -239,12 +239,12 @@ __device__ __forceinline__ void states_z_limited(const cf_dims &d, const cf_flux
 #pragma unroll
         for (int n = 0; n < 5; n++) mL[n] = lin3L<T>(a.U[n], a.J, qL, 1);
     } else if (k >= ny) {
-        T jl = zjL3<T>(a.J, qL);
+        T jl = T(a.wz[0][qL]);
 #pragma unroll
         for (int n = 0; n < 5; n++)
             mL[n] = left3<T, -1>(T(a.U[n][qL - 1]), T(a.U[n][qL]), T(a.U[n][qL + 1])) * jl;
     } else {
-        T jl = zjL5<T>(a.J, qL);
+        T jl = T(a.wz[0][qL]);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             const double *U = a.U[n];
@@ -260,12 +260,12 @@ __device__ __forceinline__ void states_z_limited(const cf_dims &d, const cf_flux
 #pragma unroll
         for (int n = 0; n < 5; n++) mR[n] = lin3R<T>(a.U[n], a.J, qR, 1);
     } else if (kc >= ny) {
-        T jr = zjR3<T>(a.J, qR);
+        T jr = T(a.wz[1][qR]);
 #pragma unroll
         for (int n = 0; n < 5; n++)
             mR[n] = right3<T>(T(a.U[n][qR - 1]), T(a.U[n][qR]), T(a.U[n][qR + 1])) * jr;
     } else {
-        T jr = zjR5<T>(a.J, qR);
+        T jr = T(a.wz[1][qR]);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             const double *U = a.U[n];
@@ -593,12 +593,41 @@ static inline cf_box flux_box(const cf_dims &d, int dir)
     return make_box(2, d.gend - 1, 1, d.ny - 1, 1, d.nz);                    // Flux_Z*.cpp
 }
 
+// The z limiter's state weights 1/sum(w/J) depend on J alone.  The no-FMA
+// build forms them once per cell with the reference's expressions
+// (Flux_Z_limiter.cpp:190-196, 3rd order where k >= ny) into wz[0], wz[1];
+// the contracted and FP32 builds store 1/J in wz[0] and form the weights
+// from it in the flux kernel (two divisions per face instead of eight).
+__global__ void __launch_bounds__(256) k_flux_zweights(cf_dims d, const double *__restrict__ J, double *wl,
+                                                       double *wr, cf_box b)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const size_t q = d.ix(i, j, k);
+#ifdef CF_FAST_MATH
+    (void)wr;
+    wl[q] = 1.0 / J[q];
+#else
+    const bool o3 = k >= d.ny;
+    wl[q] = o3 ? zjL3<double>(J, q) : zjL5<double>(J, q);
+    wr[q] = o3 ? zjR3<double>(J, q) : zjR5<double>(J, q);
+#endif
+}
+
 template <typename T>
 cudaError_t launch_flux(const cf_dims &d, const cf_flux_args &a, int dir, bool limited, cudaStream_t s)
 {
     cf_box b = flux_box(d, dir);
     if (b.ni == 0 || b.nj == 0 || b.nk == 0) return cudaSuccess;
     dim3 g = box_grid(b), t = box_block();
+    if (dir == 2 && limited) {
+        if (!a.wz[0] || !a.wz[1]) return cudaErrorInvalidValue;
+#ifdef CF_FAST_MATH
+        cf_box bw = make_box(3, d.gend, 2, d.ny, 1, d.nz + 1);      // 1/J of every cell a stencil reads
+#else
+        cf_box bw = make_box(3, d.gend, 2, d.ny, 3, d.nz - 1);
+#endif
+        if (bw.nk > 0) k_flux_zweights<<<box_grid(bw), t, 0, s>>>(d, a.J, a.wz[0], a.wz[1], bw);
+    }
     if (limited) {
         if (dir == 0) k_flux<0, true, T><<<g, t, 0, s>>>(d, a, b);
         else if (dir == 1) k_flux<1, true, T><<<g, t, 0, s>>>(d, a, b);

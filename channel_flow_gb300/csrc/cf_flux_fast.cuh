@@ -205,14 +205,15 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf
     const bool limL = k >= 3 && k <= nz - 1;          // cell k takes a limited state
     const bool limR = k + 1 >= 3 && k + 1 <= nz - 1;  // cell k+1 takes a limited state
     const bool lo3 = k >= ny, hi3 = k + 1 >= ny;      // the reference compares with the y extent
+    const double *iJp = a.wz[0];      // 1/J per cell
     if (limL && limR) {
         T iJ[6];
-        iJ[0] = lo3 ? T(0) : T(1) / T(a.J[qL - 2]);
-        iJ[1] = T(1) / T(a.J[qL - 1]);
-        iJ[2] = T(1) / T(a.J[qL]);
-        iJ[3] = T(1) / T(a.J[qL + 1]);
-        iJ[4] = T(1) / T(a.J[qL + 2]);
-        iJ[5] = hi3 ? T(0) : T(1) / T(a.J[qL + 3]);
+        iJ[0] = lo3 ? T(0) : T(iJp[qL - 2]);
+        iJ[1] = T(iJp[qL - 1]);
+        iJ[2] = T(iJp[qL]);
+        iJ[3] = T(iJp[qL + 1]);
+        iJ[4] = T(iJp[qL + 2]);
+        iJ[5] = hi3 ? T(0) : T(iJp[qL + 3]);
         const T jl = lo3 ? T(1.) / (T(-1) * iJ[1] + T(5) * iJ[2] + T(2) * iJ[3])
                          : T(1.) / (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]);
         const T jr = hi3 ? T(1.) / (T(2) * iJ[2] + T(5) * iJ[3] - T(1) * iJ[4])
@@ -233,7 +234,9 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf
 #pragma unroll
         for (int n = 0; n < 5; n++) mL[n] = lin3L<T>(a.U[n], a.J, qL, 1);
     } else {
-        const T jl = lo3 ? zjL3<T>(a.J, qL) : zjL5<T>(a.J, qL);
+        const T jl = lo3 ? T(1.) / (T(-1) * T(iJp[qL - 1]) + T(5) * T(iJp[qL]) + T(2) * T(iJp[qL + 1]))
+                         : T(1.) / (T(2) * T(iJp[qL - 2]) - T(13) * T(iJp[qL - 1]) + T(47) * T(iJp[qL]) +
+                                    T(27) * T(iJp[qL + 1]) - T(3) * T(iJp[qL + 2]));
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T u[5];
@@ -249,7 +252,9 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf
 #pragma unroll
         for (int n = 0; n < 5; n++) mR[n] = lin3R<T>(a.U[n], a.J, qR, 1);
     } else {
-        const T jr = hi3 ? zjR3<T>(a.J, qR) : zjR5<T>(a.J, qR);
+        const T jr = hi3 ? T(1.) / (T(2) * T(iJp[qR - 1]) + T(5) * T(iJp[qR]) - T(1) * T(iJp[qR + 1]))
+                         : T(1.) / (T(-3) * T(iJp[qR - 2]) + T(27) * T(iJp[qR - 1]) + T(47) * T(iJp[qR]) -
+                                    T(13) * T(iJp[qR + 1]) + T(2) * T(iJp[qR + 2]));
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T w[5];

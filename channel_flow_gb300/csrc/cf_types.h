@@ -60,6 +60,7 @@ struct cf_flux_args {
     const double *m[9];   // face metrics xidx..ztdz of the same face set
     const double *Ep;     // sensor EpX / EpY / EpZ (limited fluxes only)
     double *F[5];         // inF1..inF5
+    double *wz[2];        // scratch of the z limiter: per-cell 1/sum(w/J) of the left and right states
 };
 
 struct cf_visc_args {

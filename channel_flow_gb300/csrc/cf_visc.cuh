@@ -123,11 +123,23 @@ __device__ __forceinline__ vcross<T> ccross(T p0, T p1, T p2, T q0, T q1, T q2)
     return c;
 }
 
-template <typename T>
+// FACE 0/1/2: the x, y or z face of every cell (one launch each keeps the
+// FP64 register footprint of one face, without spills); FACE 3: all three
+// in one pass (FP32, where the registers suffice)
+template <typename T, int FACE>
 __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const T K = T(d.K), Cv = T(d.Cv), mu_E = T(d.mu_L), Pr_E = T(d.Pr_L);
+#ifdef CF_FAST_MATH
+    // the contracted and FP32 builds multiply by reciprocals of Pr and J_f
+    const T iPr = T(1) / Pr_E;
+#define CF_VPR(x) ((x) * iPr)
+#define CF_VJF(x) ((x) * iJf)
+#else
+#define CF_VPR(x) ((x) / (Pr_E))
+#define CF_VJF(x) ((x) / Jf)
+#endif
     const T invXI = T(1.) / T(d.dXI), invET = T(1.) / T(d.dET), invZT = T(1.) / T(d.dZT);
     const T inv4XI = T(1.) / (T(4) * T(d.dXI)), inv4ET = T(1.) / (T(4) * T(d.dET)),
             inv4ZT = T(1.) / (T(4) * T(d.dZT));
@@ -135,16 +147,13 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
     const vcell<T> c = ld<T>(a, q);
     const vcell<T> im = ld<T>(a, d.ix(i - 1, j, k)), jm = ld<T>(a, d.ix(i, j - 1, k)),
                    km = ld<T>(a, d.ix(i, j, k - 1));
-    const vcell<T> ip = ld<T>(a, d.ix(i + 1, j, k)), jp = ld<T>(a, d.ix(i, j + 1, k)),
-                   kp = ld<T>(a, d.ix(i, j, k + 1));
-    const vcell<T> imjp = ld<T>(a, d.ix(i - 1, j + 1, k)), imkp = ld<T>(a, d.ix(i - 1, j, k + 1));
-    const vcell<T> ipjm = ld<T>(a, d.ix(i + 1, j - 1, k)), ipkm = ld<T>(a, d.ix(i + 1, j, k - 1));
-    const vcell<T> jmkp = ld<T>(a, d.ix(i, j - 1, k + 1)), jpkm = ld<T>(a, d.ix(i, j + 1, k - 1));
-    const vcell<T> imjm = ld<T>(a, d.ix(i - 1, j - 1, k)), jmkm = ld<T>(a, d.ix(i, j - 1, k - 1)),
-                   imkm = ld<T>(a, d.ix(i - 1, j, k - 1));
-
+    const vcell<T> ip = FACE != 0 ? ld<T>(a, d.ix(i + 1, j, k)) : c;
+    const vcell<T> jp = FACE != 1 ? ld<T>(a, d.ix(i, j + 1, k)) : c;
+    const vcell<T> kp = FACE != 2 ? ld<T>(a, d.ix(i, j, k + 1)) : c;
     // ---- x face (Viscous_terms.cpp:398-547) ----
-    {
+    if (FACE == 0 || FACE == 3) {
+        const vcell<T> imjp = ld<T>(a, d.ix(i - 1, j + 1, k)), imkp = ld<T>(a, d.ix(i - 1, j, k + 1));
+        const vcell<T> imjm = ld<T>(a, d.ix(i - 1, j - 1, k)), imkm = ld<T>(a, d.ix(i - 1, j, k - 1));
         vgrad<T> X = g2<T>(c, im, invXI);
         vgrad<T> Y = g4<T>(jp, imjp, jm, imjm, imjp, inv4ET);
         vgrad<T> Z = g4<T>(kp, imkp, km, imkm, imkp, inv4ZT);
@@ -155,15 +164,20 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         vcross<T> E = ccross<T>(m0, m1, m2, T(m[6][f]), T(m[7][f]), T(m[8][f]));
         T Ux = T(0.5) * (c.u + im.u), Vx = T(0.5) * (c.v + im.v), Wx = T(0.5) * (c.w + im.w);
         T Jf = T(a.Jf[0][f]);
-        a.LL[0][q] = double(mu_E * (A.s1 * X.du + A.s5 * X.dv + A.s7 * X.dw + D.x1 * Y.du + D.x7 * Y.dv + D.x9 * Y.dw + E.x1 * Z.du + E.x7 * Z.dv + E.x9 * Z.dw) / Jf);
-        a.LL[1][q] = double(mu_E * (A.s5 * X.du + A.s2 * X.dv + A.s6 * X.dw + D.x5 * Y.du + D.x2 * Y.dv + D.x10 * Y.dw + E.x5 * Z.du + E.x2 * Z.dv + E.x10 * Z.dw) / Jf);
-        a.LL[2][q] = double(mu_E * (A.s7 * X.du + A.s6 * X.dv + A.s3 * X.dw + D.x6 * Y.du + D.x8 * Y.dv + D.x3 * Y.dw + E.x6 * Z.du + E.x8 * Z.dv + E.x3 * Z.dw) / Jf);
-        a.LL[3][q] = double(mu_E * (T(0.5) * A.s1 * X.du2 + T(0.5) * A.s2 * X.dv2 + T(0.5) * A.s3 * X.dw2 + A.s5 * X.duv + A.s6 * X.dvw + A.s7 * X.duw + Cv * K * A.s4 * X.dT / (Pr_E) +
-            T(0.5) * D.x1 * Y.du2 + T(0.5) * D.x2 * Y.dv2 + T(0.5) * D.x3 * Y.dw2 + D.x5 * Vx * Y.du + D.x6 * Wx * Y.du + D.x7 * Ux * Y.dv + D.x8 * Wx * Y.dv + D.x9 * Ux * Y.dw + D.x10 * Vx * Y.dw + Cv * K * D.x4 * Y.dT / (Pr_E) +
-            T(0.5) * E.x1 * Z.du2 + T(0.5) * E.x2 * Z.dv2 + T(0.5) * E.x3 * Z.dw2 + E.x5 * Vx * Z.du + E.x6 * Wx * Z.du + E.x7 * Ux * Z.dv + E.x8 * Wx * Z.dv + E.x9 * Ux * Z.dw + E.x10 * Vx * Z.dw + Cv * K * E.x4 * Z.dT / (Pr_E)) / Jf);
+#ifdef CF_FAST_MATH
+        const T iJf = T(1) / Jf;
+#endif
+        a.LL[0][q] = double(CF_VJF(mu_E * (A.s1 * X.du + A.s5 * X.dv + A.s7 * X.dw + D.x1 * Y.du + D.x7 * Y.dv + D.x9 * Y.dw + E.x1 * Z.du + E.x7 * Z.dv + E.x9 * Z.dw)));
+        a.LL[1][q] = double(CF_VJF(mu_E * (A.s5 * X.du + A.s2 * X.dv + A.s6 * X.dw + D.x5 * Y.du + D.x2 * Y.dv + D.x10 * Y.dw + E.x5 * Z.du + E.x2 * Z.dv + E.x10 * Z.dw)));
+        a.LL[2][q] = double(CF_VJF(mu_E * (A.s7 * X.du + A.s6 * X.dv + A.s3 * X.dw + D.x6 * Y.du + D.x8 * Y.dv + D.x3 * Y.dw + E.x6 * Z.du + E.x8 * Z.dv + E.x3 * Z.dw)));
+        a.LL[3][q] = double(CF_VJF(mu_E * (T(0.5) * A.s1 * X.du2 + T(0.5) * A.s2 * X.dv2 + T(0.5) * A.s3 * X.dw2 + A.s5 * X.duv + A.s6 * X.dvw + A.s7 * X.duw + CF_VPR(Cv * K * A.s4 * X.dT) +
+            T(0.5) * D.x1 * Y.du2 + T(0.5) * D.x2 * Y.dv2 + T(0.5) * D.x3 * Y.dw2 + D.x5 * Vx * Y.du + D.x6 * Wx * Y.du + D.x7 * Ux * Y.dv + D.x8 * Wx * Y.dv + D.x9 * Ux * Y.dw + D.x10 * Vx * Y.dw + CF_VPR(Cv * K * D.x4 * Y.dT) +
+            T(0.5) * E.x1 * Z.du2 + T(0.5) * E.x2 * Z.dv2 + T(0.5) * E.x3 * Z.dw2 + E.x5 * Vx * Z.du + E.x6 * Wx * Z.du + E.x7 * Ux * Z.dv + E.x8 * Wx * Z.dv + E.x9 * Ux * Z.dw + E.x10 * Vx * Z.dw + CF_VPR(Cv * K * E.x4 * Z.dT))));
     }
     // ---- y face (Viscous_terms.cpp:550-695) ----
-    {
+    if (FACE == 1 || FACE == 3) {
+        const vcell<T> ipjm = ld<T>(a, d.ix(i + 1, j - 1, k)), imjm = ld<T>(a, d.ix(i - 1, j - 1, k));
+        const vcell<T> jmkp = ld<T>(a, d.ix(i, j - 1, k + 1)), jmkm = ld<T>(a, d.ix(i, j - 1, k - 1));
         vgrad<T> X = g4<T>(ip, ipjm, im, imjm, ipjm, inv4XI);
         vgrad<T> Y = g2<T>(c, jm, invET);
         vgrad<T> Z = g4<T>(kp, jmkp, km, jmkm, jmkp, inv4ZT);
@@ -175,15 +189,21 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         vcross<T> F = ccross<T>(e0, e1, e2, T(m[6][f]), T(m[7][f]), T(m[8][f]));
         T Uy = T(0.5) * (c.u + jm.u), Vy = T(0.5) * (c.v + jm.v), Wy = T(0.5) * (c.w + jm.w);
         T Jf = T(a.Jf[1][f]);
-        a.ML[0][q] = double(mu_E * (D.x1 * X.du + D.x5 * X.dv + D.x6 * X.dw + B.s1 * Y.du + B.s5 * Y.dv + B.s7 * Y.dw + F.x1 * Z.du + F.x7 * Z.dv + F.x9 * Z.dw) / Jf);
-        a.ML[1][q] = double(mu_E * (D.x7 * X.du + D.x2 * X.dv + D.x8 * X.dw + B.s5 * Y.du + B.s2 * Y.dv + B.s6 * Y.dw + F.x5 * Z.du + F.x2 * Z.dv + F.x10 * Z.dw) / Jf);
-        a.ML[2][q] = double(mu_E * (D.x9 * X.du + D.x10 * X.dv + D.x3 * X.dw + B.s7 * Y.du + B.s6 * Y.dv + B.s3 * Y.dw + F.x6 * Z.du + F.x8 * Z.dv + F.x3 * Z.dw) / Jf);
-        a.ML[3][q] = double(mu_E * (T(0.5) * B.s1 * Y.du2 + T(0.5) * B.s2 * Y.dv2 + T(0.5) * B.s3 * Y.dw2 + B.s5 * Y.duv + B.s6 * Y.dvw + B.s7 * Y.duw + Cv * K * B.s4 * Y.dT / (Pr_E) +
-            T(0.5) * D.x1 * X.du2 + T(0.5) * D.x2 * X.dv2 + T(0.5) * D.x3 * X.dw2 + D.x5 * Uy * X.dv + D.x6 * Uy * X.dw + D.x7 * Vy * X.du + D.x8 * Vy * X.dw + D.x9 * Wy * X.du + D.x10 * Wy * X.dv + Cv * K * D.x4 * X.dT / (Pr_E) +
-            T(0.5) * F.x1 * Z.du2 + T(0.5) * F.x2 * Z.dv2 + T(0.5) * F.x3 * Z.dw2 + F.x5 * Vy * Z.du + F.x6 * Wy * Z.du + F.x7 * Uy * Z.dv + F.x8 * Wy * Z.dv + F.x9 * Uy * Z.dw + F.x10 * Vy * Z.dw + Cv * K * F.x4 * Z.dT / (Pr_E)) / Jf);
+#ifdef CF_FAST_MATH
+        const T iJf = T(1) / Jf;
+#endif
+        a.ML[0][q] = double(CF_VJF(mu_E * (D.x1 * X.du + D.x5 * X.dv + D.x6 * X.dw + B.s1 * Y.du + B.s5 * Y.dv + B.s7 * Y.dw + F.x1 * Z.du + F.x7 * Z.dv + F.x9 * Z.dw)));
+        a.ML[1][q] = double(CF_VJF(mu_E * (D.x7 * X.du + D.x2 * X.dv + D.x8 * X.dw + B.s5 * Y.du + B.s2 * Y.dv + B.s6 * Y.dw + F.x5 * Z.du + F.x2 * Z.dv + F.x10 * Z.dw)));
+        a.ML[2][q] = double(CF_VJF(mu_E * (D.x9 * X.du + D.x10 * X.dv + D.x3 * X.dw + B.s7 * Y.du + B.s6 * Y.dv + B.s3 * Y.dw + F.x6 * Z.du + F.x8 * Z.dv + F.x3 * Z.dw)));
+        a.ML[3][q] = double(CF_VJF(mu_E * (T(0.5) * B.s1 * Y.du2 + T(0.5) * B.s2 * Y.dv2 + T(0.5) * B.s3 * Y.dw2 + B.s5 * Y.duv + B.s6 * Y.dvw + B.s7 * Y.duw + CF_VPR(Cv * K * B.s4 * Y.dT) +
+            T(0.5) * D.x1 * X.du2 + T(0.5) * D.x2 * X.dv2 + T(0.5) * D.x3 * X.dw2 + D.x5 * Uy * X.dv + D.x6 * Uy * X.dw + D.x7 * Vy * X.du + D.x8 * Vy * X.dw + D.x9 * Wy * X.du + D.x10 * Wy * X.dv + CF_VPR(Cv * K * D.x4 * X.dT) +
+            T(0.5) * F.x1 * Z.du2 + T(0.5) * F.x2 * Z.dv2 + T(0.5) * F.x3 * Z.dw2 + F.x5 * Vy * Z.du + F.x6 * Wy * Z.du + F.x7 * Uy * Z.dv + F.x8 * Wy * Z.dv + F.x9 * Uy * Z.dw + F.x10 * Vy * Z.dw + CF_VPR(Cv * K * F.x4 * Z.dT))));
     }
     // ---- z face (Viscous_terms.cpp:698-841) ----
-    {
+    if (FACE == 2 || FACE == 3) {
+        const vcell<T> ipkm = ld<T>(a, d.ix(i + 1, j, k - 1)), imkm = ld<T>(a, d.ix(i - 1, j, k - 1));
+        const vcell<T> jpkm = ld<T>(a, d.ix(i, j + 1, k - 1)), jmkm = ld<T>(a, d.ix(i, j - 1, k - 1));
+        const vcell<T> imjp = ld<T>(a, d.ix(i - 1, j + 1, k));
         vgrad<T> X = g4<T>(ip, ipkm, im, imkm, ipkm, inv4XI);
         vgrad<T> Y = g4<T>(jp, jpkm, jm, jmkm, imjp, inv4ET);
         vgrad<T> Z = g2<T>(c, km, invZT);
@@ -194,14 +214,20 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         vcross<T> F = ccross<T>(T(m[3][f]), T(m[4][f]), T(m[5][f]), z0, z1, z2);
         T Uz = T(0.5) * (c.u + km.u), Vz = T(0.5) * (c.v + km.v), Wz = T(0.5) * (c.w + km.w);
         T Jf = T(a.Jf[2][f]);
-        a.NL[0][q] = double(mu_E * (E.x1 * X.du + E.x5 * X.dv + E.x6 * X.dw + F.x1 * Y.du + F.x5 * Y.dv + F.x6 * Y.dw + Cc.s1 * Z.du + Cc.s5 * Z.dv + Cc.s7 * Z.dw) / Jf);
-        a.NL[1][q] = double(mu_E * (E.x7 * X.du + E.x2 * X.dv + E.x8 * X.dw + F.x7 * Y.du + F.x2 * Y.dv + F.x8 * Y.dw + Cc.s5 * Z.du + Cc.s2 * Z.dv + Cc.s6 * Z.dw) / Jf);
-        a.NL[2][q] = double(mu_E * (E.x9 * X.du + E.x10 * X.dv + E.x3 * X.dw + F.x9 * Y.du + F.x10 * Y.dv + F.x3 * Y.dw + Cc.s7 * Z.du + Cc.s6 * Z.dv + Cc.s3 * Z.dw) / Jf);
-        a.NL[3][q] = double(mu_E * (T(0.5) * Cc.s1 * Z.du2 + T(0.5) * Cc.s2 * Z.dv2 + T(0.5) * Cc.s3 * Z.dw2 + Cc.s5 * Z.duv + Cc.s6 * Z.dvw + Cc.s7 * Z.duw + Cv * K * Cc.s4 * Z.dT / (Pr_E) +
-            T(0.5) * E.x1 * X.du2 + T(0.5) * E.x2 * X.dv2 + T(0.5) * E.x3 * X.dw2 + E.x5 * Uz * X.dv + E.x6 * Uz * X.dw + E.x7 * Vz * X.du + E.x8 * Vz * X.dw + E.x9 * Wz * X.du + E.x10 * Wz * X.dv + Cv * K * E.x4 * X.dT / (Pr_E) +
-            T(0.5) * F.x1 * Y.du2 + T(0.5) * F.x2 * Y.dv2 + T(0.5) * F.x3 * Y.dw2 + F.x5 * Uz * Y.dv + F.x6 * Uz * Y.dw + F.x7 * Vz * Y.du + F.x8 * Vz * Y.dw + F.x9 * Wz * Y.du + F.x10 * Wz * Y.dv + Cv * K * F.x4 * Y.dT / (Pr_E)) / Jf);
+#ifdef CF_FAST_MATH
+        const T iJf = T(1) / Jf;
+#endif
+        a.NL[0][q] = double(CF_VJF(mu_E * (E.x1 * X.du + E.x5 * X.dv + E.x6 * X.dw + F.x1 * Y.du + F.x5 * Y.dv + F.x6 * Y.dw + Cc.s1 * Z.du + Cc.s5 * Z.dv + Cc.s7 * Z.dw)));
+        a.NL[1][q] = double(CF_VJF(mu_E * (E.x7 * X.du + E.x2 * X.dv + E.x8 * X.dw + F.x7 * Y.du + F.x2 * Y.dv + F.x8 * Y.dw + Cc.s5 * Z.du + Cc.s2 * Z.dv + Cc.s6 * Z.dw)));
+        a.NL[2][q] = double(CF_VJF(mu_E * (E.x9 * X.du + E.x10 * X.dv + E.x3 * X.dw + F.x9 * Y.du + F.x10 * Y.dv + F.x3 * Y.dw + Cc.s7 * Z.du + Cc.s6 * Z.dv + Cc.s3 * Z.dw)));
+        a.NL[3][q] = double(CF_VJF(mu_E * (T(0.5) * Cc.s1 * Z.du2 + T(0.5) * Cc.s2 * Z.dv2 + T(0.5) * Cc.s3 * Z.dw2 + Cc.s5 * Z.duv + Cc.s6 * Z.dvw + Cc.s7 * Z.duw + CF_VPR(Cv * K * Cc.s4 * Z.dT) +
+            T(0.5) * E.x1 * X.du2 + T(0.5) * E.x2 * X.dv2 + T(0.5) * E.x3 * X.dw2 + E.x5 * Uz * X.dv + E.x6 * Uz * X.dw + E.x7 * Vz * X.du + E.x8 * Vz * X.dw + E.x9 * Wz * X.du + E.x10 * Wz * X.dv + CF_VPR(Cv * K * E.x4 * X.dT) +
+            T(0.5) * F.x1 * Y.du2 + T(0.5) * F.x2 * Y.dv2 + T(0.5) * F.x3 * Y.dw2 + F.x5 * Uz * Y.dv + F.x6 * Uz * Y.dw + F.x7 * Vz * Y.du + F.x8 * Vz * Y.dw + F.x9 * Wz * Y.du + F.x10 * Wz * Y.dv + CF_VPR(Cv * K * F.x4 * Y.dT))));
     }
 }
+
+#undef CF_VPR
+#undef CF_VJF
 
 // Viscous_terms.cpp:854-883
 template <typename T>
@@ -222,7 +248,13 @@ cudaError_t launch_viscous(const cf_dims &d, const cf_visc_args &a, cudaStream_t
     const size_t n = d.total();
     k_visc_prim<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
     cf_box bf = make_box(3, d.gend + 1, 2, d.ny + 1, 2, d.nz + 1);
-    k_visc_faces<T><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+    if constexpr (sizeof(T) == sizeof(double)) {
+        k_visc_faces<T, 0><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+        k_visc_faces<T, 1><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+        k_visc_faces<T, 2><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+    } else {
+        k_visc_faces<T, 3><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+    }
     cf_box bd = make_box(3, d.gend, 2, d.ny, 2, d.nz);
     k_visc_div<T><<<box_grid(bd), box_block(), 0, s>>>(d, a, bd);
     return cudaGetLastError();
