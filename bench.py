@@ -277,6 +277,9 @@ def main():
     ap.add_argument("--grid", default="x".join(map(str, GRID)))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
+    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs"],
+                    help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
+                         "(one LU-SGS pseudo-iteration per step, for profiling)")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
 
@@ -329,6 +332,12 @@ def main():
     for _ in range(max(args.warmup, 3)):
         run_calls(ctx, calls)
     torch.cuda.synchronize()
+    if args.step == "lusgs":
+        r = pseudo_iteration(ctx, g, w, calls, stream, torch, max(2, args.steps))
+        print(json.dumps({"step": "lusgs", "metric": "ms per Dual_time_stepping", "value": r["dual_time_lusgs_ms"],
+                          "unit": "ms", "higher_is_better": False, "config": cfg, "detail": r}))
+        ctx.close()
+        return 0
 
     # timed region: K steps, events around every routine for the roofline
     if dist:
