@@ -41,8 +41,7 @@ class Context:
     def __init__(self, grid: Grid, precision: str = "fp64", stream=None, gamma: float = 1.5):
         self.lib = _lib.load()
         self.grid = grid
-        g = _lib.cf_grid(grid.X_out, grid.Y_out, grid.Z_out, grid.deltaXI, grid.deltaET, grid.deltaZT,
-                         grid.K, grid.R, grid.e, grid.Cv, grid.mu_L, grid.Pr_L, grid.f, grid.high)
+        g = _lib.grid_struct(grid)
         h = C.c_void_p()
         rc = self.lib.cf_create(C.byref(g), _lib.PREC[precision], C.byref(h))
         _lib.check(self.lib, None, rc)
@@ -91,6 +90,74 @@ class Context:
         out = np.zeros((2, tiles, 4), np.int64)
         self._ok(self.lib.cf_lu_trace_read(self.h, out.ctypes.data, out.size))
         return out
+
+    def set_output_dir(self, path):
+        """Directory of Statistic's, Output's and Initial_condition's files."""
+        self._ok(self.lib.cf_set_output_dir(self.h, None if path is None else str(path).encode()))
+
+    def Driven_force(self, U2_, J, myid=0):
+        """Bulk-flow integral: returns (Q, ER_Q)."""
+        q = np.zeros(2)
+        self._ok(self.lib.cf_Driven_force(self.h, myid, _ptr(U2_), _ptr(J), q[0:].ctypes.data,
+                                          q[1:].ctypes.data))
+        return float(q[0]), float(q[1])
+
+    def Statistic(self, step, iteration, statistic_step, *arrays, myid=0):
+        if len(arrays) != 27:
+            raise ValueError("Statistic takes 27 arrays")
+        self._ok(self.lib.cf_Statistic(self.h, myid, step, iteration, statistic_step,
+                                       _lib.ptr_array([_ptr(a) for a in arrays])))
+
+    def statistic_read(self) -> np.ndarray:
+        out = np.zeros(17 * (self.grid.Y_out + 4) + 2)
+        self._ok(self.lib.cf_statistic_read(self.h, out.ctypes.data))
+        return out
+
+    def statistic_reset(self):
+        self._ok(self.lib.cf_statistic_reset(self.h))
+
+    def Output(self, step, *arrays, myid=0):
+        """U1..U5, U1q..U5q, J -> LES%05d.bin"""
+        if len(arrays) != 11:
+            raise ValueError("Output takes 11 arrays")
+        self._ok(self.lib.cf_Output(self.h, step, myid, *[_ptr(a) for a in arrays]))
+
+    def Initial_condition(self, *arrays, myid=0):
+        """U1_..U5_, U1..U5, U1q..U5q, J <- initial.bin"""
+        if len(arrays) != 16:
+            raise ValueError("Initial_condition takes 16 arrays")
+        self._ok(self.lib.cf_Initial_condition(self.h, myid, *[_ptr(a) for a in arrays]))
+
+    def step(self, fields: dict, step: int = 1, deltaT: float = 0.00000005, max_iterations: int = 200,
+             tolerance: float = 0.001, limiter: bool = True, filter: bool = True, roe_criterion: float = 0.007,
+             e_high: float = 1.0, e_low: float = 0.0, statistic_step: int = 0):
+        """One physical time step (cf_step).  ``fields`` maps the cf_fields
+        member names to device tensors (lists for the multi-array members,
+        a list of three lists for face_metric and inF).  Returns
+        (iterations, er[5], Q)."""
+        f = _lib.cf_fields()
+        for name, val in fields.items():
+            slot = getattr(f, name)
+            if isinstance(val, (list, tuple)):
+                for i, v in enumerate(val):
+                    if isinstance(v, (list, tuple)):
+                        for k, x in enumerate(v):
+                            slot[i][k] = _ptr(x)
+                    else:
+                        slot[i] = _ptr(v)
+            else:
+                setattr(f, name, _ptr(val))
+        prm = _lib.cf_step_params(deltaT, max_iterations, tolerance, int(limiter), int(filter), roe_criterion,
+                                  e_high, e_low, statistic_step)
+        it = C.c_int(0)
+        er = np.zeros(5)
+        q = np.zeros(1)
+        self._ok(self.lib.cf_step(self.h, C.byref(prm), step, C.byref(f), C.byref(it), er.ctypes.data,
+                                  q.ctypes.data))
+        return it.value, er, float(q[0])
+
+    def step_reset(self):
+        self._ok(self.lib.cf_step_reset(self.h))
 
     def set_precision(self, precision: str):
         self._ok(self.lib.cf_set_precision(self.h, _lib.PREC[precision]))
@@ -207,8 +274,7 @@ def dplusgs_noalloc(grid: Grid, deltaT, *arrays, stream=None):
     if stream is None:
         import torch
         stream = torch.cuda.current_stream().cuda_stream
-    g = _lib.cf_grid(grid.X_out, grid.Y_out, grid.Z_out, grid.deltaXI, grid.deltaET, grid.deltaZT,
-                     grid.K, grid.R, grid.e, grid.Cv, grid.mu_L, grid.Pr_L, grid.f, grid.high)
+    g = _lib.grid_struct(grid)
     er = np.zeros(5)
     e = [er[n:].ctypes.data for n in range(5)]
     rc = lib.cf_DPLUSGS_noalloc(C.byref(g), stream, deltaT, *e, _lib.ptr_array([_ptr(a) for a in arrays]))

@@ -21,7 +21,28 @@ class cf_grid(C.Structure):
                 ("d_xi", C.c_double), ("d_eta", C.c_double), ("d_zeta", C.c_double),
                 ("gamma_gas", C.c_double), ("r_gas", C.c_double), ("beta_min", C.c_double),
                 ("cv", C.c_double), ("mu", C.c_double), ("prandtl", C.c_double),
-                ("body_force", C.c_double), ("height", C.c_double)]
+                ("body_force", C.c_double), ("height", C.c_double), ("bulk_flux", C.c_double)]
+
+
+_VP = C.c_void_p
+
+
+class cf_fields(C.Structure):
+    _fields_ = [("U_", _VP * 5), ("U", _VP * 5), ("Uq", _VP * 5), ("J", _VP), ("Y_point", _VP),
+                ("cell_metric", _VP * 9), ("face_J", _VP * 3), ("face_metric", (_VP * 9) * 3), ("Ep", _VP * 3),
+                ("inF", (_VP * 5) * 3), ("vF", _VP * 4), ("LL", _VP * 4), ("ML", _VP * 4),
+                ("MR", _VP * 5), ("NR", _VP * 5), ("NL", _VP * 5), ("Residual", _VP * 5)]
+
+
+class cf_step_params(C.Structure):
+    _fields_ = [("deltaT", C.c_double), ("max_iterations", C.c_int), ("tolerance", C.c_double),
+                ("limiter", C.c_int), ("filter", C.c_int), ("roe_criterion", C.c_double),
+                ("e_high", C.c_double), ("e_low", C.c_double), ("statistic_step", C.c_int)]
+
+
+def grid_struct(grid) -> "cf_grid":
+    return cf_grid(grid.X_out, grid.Y_out, grid.Z_out, grid.deltaXI, grid.deltaET, grid.deltaZT,
+                   grid.K, grid.R, grid.e, grid.Cv, grid.mu_L, grid.Pr_L, grid.f, grid.high, grid.Q0)
 
 
 class CFError(RuntimeError):
@@ -68,6 +89,15 @@ _SIGS = {
     "cf_Jacobian_u": ([P, C.c_int, C.POINTER(P)], C.c_int),
     "cf_Jacobian_v": ([P, C.c_int, C.POINTER(P)], C.c_int),
     "cf_Jacobian_w": ([P, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_set_output_dir": ([P, C.c_char_p], C.c_int),
+    "cf_Driven_force": ([P, C.c_int, P, P, P, P], C.c_int),
+    "cf_Statistic": ([P, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_statistic_read": ([P, P], C.c_int),
+    "cf_statistic_reset": ([P], C.c_int),
+    "cf_Output": ([P, C.c_int, C.c_int] + [P] * 11, C.c_int),
+    "cf_Initial_condition": ([P, C.c_int] + [P] * 16, C.c_int),
+    "cf_step": ([P, P, C.c_int, P, P, P, P], C.c_int),
+    "cf_step_reset": ([P], C.c_int),
 }
 for _n in ("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter", "Flux_X", "Flux_Y", "Flux_Z"):
     _SIGS["cf_" + _n] = ([P, C.c_int] + [P] * 32, C.c_int)

@@ -3,6 +3,7 @@
 // (declarations and contracts: include/channel_flow_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -21,6 +22,11 @@ struct cf_ctx {
     int prec = CF_PREC_FP64;
     cudaStream_t stream = nullptr;
     double gamma = 1.5;
+    double q0 = 20.464969232814912;   // target bulk flux Q0 (prm.h)
+    std::string out_dir = ".";        // where Statistic / Output / Initial_condition put their files
+    double *stat_acc = nullptr;       // Statistic accumulators, 17 rows of Y_m (device)
+    double sxy_bottom = 0, sxy_up = 0;
+    double E[5] = {0, 0, 0, 0, 0};    // running maxima of the residual norms (main.cpp:63, 387-391)
     std::unordered_map<const double *, double *> mirrors;
     std::unordered_map<std::string, std::pair<double *, size_t>> scratch;
     std::vector<int> nijk;            // plane tables, Hyperplane layout (host)
@@ -172,6 +178,7 @@ int cf_grid_reference(cf_grid *g, int cells_x, int cells_y, int cells_z)
     g->gamma_gas = 1.4; g->r_gas = 287; g->beta_min = 0.0001;
     g->cv = 717.5; g->mu = 0.0000185; g->prandtl = 0.72;
     g->body_force = 599.29876710; g->height = 0.005;
+    g->bulk_flux = 20.464969232814912;
     return CF_OK;
 }
 
@@ -189,6 +196,7 @@ int cf_create(const cf_grid *g, int precision, cf_ctx **out)
     d.dXI = g->d_xi; d.dET = g->d_eta; d.dZT = g->d_zeta;
     d.K = g->gamma_gas; d.R = g->r_gas; d.e = g->beta_min; d.Cv = g->cv; d.mu_L = g->mu; d.Pr_L = g->prandtl;
     d.f = g->body_force; d.high = g->height;
+    c->q0 = g->bulk_flux;
     c->prec = precision;
     build_tables(c);
     cudaError_t e = cudaMalloc(&c->ijk_dev, c->ijk.size() * sizeof(int));
@@ -212,6 +220,7 @@ void cf_destroy(cf_ctx *c)
     if (c->er_dev) cudaFree(c->er_dev);
     if (c->er_host) cudaFreeHost(c->er_host);
     if (c->dts_exec) cudaGraphExecDestroy(c->dts_exec);
+    if (c->stat_acc) cudaFree(c->stat_acc);
     if (c->tile_order) cudaFree(c->tile_order);
     if (c->trace) cudaFree(c->trace);
     if (c->cap) cudaStreamDestroy(c->cap);
@@ -828,5 +837,297 @@ static int jacobian_common(cf_ctx *c, double **p, int which, const char *who)
 int cf_Jacobian_u(cf_ctx *c, int, double **p) { return jacobian_common(c, p, 0, "Jacobian_u"); }
 int cf_Jacobian_v(cf_ctx *c, int, double **p) { return jacobian_common(c, p, 1, "Jacobian_v"); }
 int cf_Jacobian_w(cf_ctx *c, int, double **p) { return jacobian_common(c, p, 2, "Jacobian_w"); }
+
+// ---------------------------------------------------------------------------
+// reductions and IO around the step (FP64 in every precision mode)
+
+static std::string out_path(const cf_ctx *c, const char *name)
+{
+    return c->out_dir.empty() ? std::string(name) : c->out_dir + "/" + name;
+}
+
+int cf_set_output_dir(cf_ctx *c, const char *dir)
+{
+    if (!c) return CF_ERR_ARG;
+    c->out_dir = dir ? dir : "";
+    return CF_OK;
+}
+
+int cf_Driven_force(cf_ctx *c, int, double *U2_, double *J, double *Q, double *ER_Q)
+{
+    if (!c || !U2_ || !J) return CF_ERR_ARG;
+    const cf_dims &d = c->d;
+    double *rows = scratch(c, "bulk_rows", 1);            // Y_m row sums + Jsum, inside one field
+    const size_t plen = (size_t)4 * 152 * 9 + (size_t)d.Ym * 64;
+    double *partial = static_cast<double *>(scratch_bytes(c, "stat_partial", plen * sizeof(double)));
+    if (!rows || !partial) return fail(c, CF_ERR_NOMEM, "Driven_force: scratch allocation failed");
+    double *jsum = rows + d.Ym;
+    cudaError_t e = cf_fast::bulk_rows(d, R(c, U2_), R(c, J), jsum, rows, partial, plen, c->stream);
+    if (int rc = cuda_check(c, e, "Driven_force")) return rc;
+    std::vector<double> h((size_t)d.Ym);
+    if (int rc = cuda_check(c, cudaMemcpyAsync(h.data(), rows, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                               c->stream), "Driven_force")) return rc;
+    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "Driven_force")) return rc;
+    double q = 0;
+    for (int j = 2; j <= d.ny; j++) q += h[(size_t)j];
+    q = q / d.X_out / d.Z_out;
+    if (Q) *Q = q;
+    if (ER_Q) *ER_Q = std::fabs(c->q0 - q) / c->q0;
+    return CF_OK;
+}
+
+static int stat_alloc(cf_ctx *c)
+{
+    if (c->stat_acc) return CF_OK;
+    const size_t n = (size_t)17 * c->d.Ym;
+    if (cudaMalloc(&c->stat_acc, n * sizeof(double)) != cudaSuccess) {
+        c->stat_acc = nullptr;
+        return fail(c, CF_ERR_NOMEM, "Statistic: accumulator allocation failed");
+    }
+    return cuda_check(c, cudaMemset(c->stat_acc, 0, n * sizeof(double)), "Statistic");
+}
+
+int cf_statistic_reset(cf_ctx *c)
+{
+    if (!c) return CF_ERR_ARG;
+    if (int rc = stat_alloc(c)) return rc;
+    c->sxy_bottom = c->sxy_up = 0;
+    return cuda_check(c, cudaMemsetAsync(c->stat_acc, 0, (size_t)17 * c->d.Ym * sizeof(double), c->stream),
+                      "cf_statistic_reset");
+}
+
+int cf_statistic_read(cf_ctx *c, double *out)
+{
+    if (!c || !out) return CF_ERR_ARG;
+    if (int rc = stat_alloc(c)) return rc;
+    const size_t n = (size_t)17 * c->d.Ym;
+    if (int rc = cuda_check(c, cudaMemcpyAsync(out, c->stat_acc, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                               c->stream), "cf_statistic_read")) return rc;
+    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "cf_statistic_read")) return rc;
+    out[n] = c->sxy_bottom;
+    out[n + 1] = c->sxy_up;
+    return CF_OK;
+}
+
+int cf_Statistic(cf_ctx *c, int, int step, int, int statistic_step, double **p)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    if (statistic_step <= 0) return fail(c, CF_ERR_ARG, "Statistic: statistic_step must be positive");
+    for (int i = 0; i < 16; i++)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "Statistic: array argument %d is NULL", i);
+    if (int rc = stat_alloc(c)) return rc;
+    const cf_dims &d = c->d;
+    cf_stat_args a;
+    for (int n = 0; n < 5; n++) a.U[n] = R(c, p[n]);
+    a.J = R(c, p[5]);
+    a.Jv = R(c, p[6]);
+    for (int n = 0; n < 9; n++) a.m[n] = R(c, p[7 + n]);
+    const size_t plen = (size_t)4 * 152 * 9 + (size_t)d.Ym * 64;
+    double *partial = static_cast<double *>(scratch_bytes(c, "stat_partial", plen * sizeof(double)));
+    if (!partial) return fail(c, CF_ERR_NOMEM, "Statistic: scratch allocation failed");
+    cudaError_t e = exact(c) ? cf_exact::statistic(d, a, c->stat_acc, partial, plen, c->stream)
+                             : cf_fast::statistic(d, a, c->stat_acc, partial, plen, c->stream);
+    if (int rc = cuda_check(c, e, "Statistic")) return rc;
+    const int Ym = d.Ym, ny = d.ny;
+    std::vector<double> h((size_t)17 * Ym);
+    if (int rc = cuda_check(c, cudaMemcpyAsync(h.data(), c->stat_acc, h.size() * sizeof(double),
+                                               cudaMemcpyDeviceToHost, c->stream), "Statistic")) return rc;
+    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "Statistic")) return rc;
+    const double XZ = (double)d.X_out, ZZ = (double)d.Z_out;
+    // wall shear-stress increments (Statistic.cpp:900-920)
+    const double s1 = h[(size_t)7 * Ym + 1] / XZ / ZZ, sn = h[(size_t)7 * Ym + ny] / XZ / ZZ;
+    {
+        FILE *f = std::fopen(out_path(c, "Shear_stress.dat").c_str(), "a");
+        if (!f) return fail(c, CF_ERR_ARG, "Statistic: cannot open Shear_stress.dat in '%s'", c->out_dir.c_str());
+        std::fprintf(f, "%f\t%f\n", s1 - c->sxy_bottom, sn - c->sxy_up);
+        std::fclose(f);
+    }
+    c->sxy_bottom = s1;
+    c->sxy_up = sn;
+    if (step % statistic_step == 0) {
+        const double inv = 1. / statistic_step / XZ / ZZ;
+        char name[64];
+        std::snprintf(name, sizeof name, "ND%05d.dat", step);
+        FILE *f = std::fopen(out_path(c, name).c_str(), "w");
+        if (!f) return fail(c, CF_ERR_ARG, "Statistic: cannot write %s", name);
+        for (int r = 0; r < 10; r++)
+            for (int j = 1; j <= ny; j++) std::fprintf(f, "%.16f\n", h[(size_t)r * Ym + j] * inv);
+        std::fclose(f);
+        std::snprintf(name, sizeof name, "st%05d.dat", step);
+        f = std::fopen(out_path(c, name).c_str(), "w");
+        if (!f) return fail(c, CF_ERR_ARG, "Statistic: cannot write %s", name);
+        for (int r = 10; r < 17; r++)
+            for (int j = 2; j <= ny; j++) std::fprintf(f, "%.16f\n", h[(size_t)r * Ym + j] * inv);
+        std::fclose(f);
+        c->sxy_bottom = c->sxy_up = 0;
+        if (int rc = cuda_check(c, cudaMemsetAsync(c->stat_acc, 0, h.size() * sizeof(double), c->stream),
+                                "Statistic")) return rc;
+    }
+    return CF_OK;
+}
+
+static int restart_args(cf_ctx *c, double *const *U, double *const *Uq, const double *J, cf_ptr5 &u, cf_ptr5 &uq,
+                        const char *who)
+{
+    for (int n = 0; n < 5; n++) {
+        if (!U[n] || !Uq[n]) return fail(c, CF_ERR_ARG, "%s: NULL array", who);
+        u.p[n] = R(c, U[n]);
+        uq.p[n] = R(c, Uq[n]);
+    }
+    if (!J) return fail(c, CF_ERR_ARG, "%s: NULL J", who);
+    return CF_OK;
+}
+
+int cf_Output(cf_ctx *c, int step, int, double *U1, double *U2, double *U3, double *U4, double *U5, double *U1q,
+              double *U2q, double *U3q, double *U4q, double *U5q, double *J)
+{
+    if (!c) return CF_ERR_ARG;
+    double *U[5] = {U1, U2, U3, U4, U5}, *Uq[5] = {U1q, U2q, U3q, U4q, U5q};
+    cf_ptr5 u, uq;
+    if (int rc = restart_args(c, U, Uq, J, u, uq, "Output")) return rc;
+    const cf_dims &d = c->d;
+    const size_t N = (size_t)d.X_out * d.Y_out * d.Z_out;
+    double *img = static_cast<double *>(scratch_bytes(c, "restart", 10 * N * sizeof(double)));
+    if (!img) return fail(c, CF_ERR_NOMEM, "Output: scratch allocation failed");
+    if (int rc = cuda_check(c, cf_fast::restart_pack(d, u, uq, R(c, J), img, c->stream), "Output")) return rc;
+    std::vector<double> h(10 * N);
+    if (int rc = cuda_check(c, cudaMemcpyAsync(h.data(), img, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                               c->stream), "Output")) return rc;
+    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "Output")) return rc;
+    char name[64];
+    std::snprintf(name, sizeof name, "LES%05d.bin", step);
+    FILE *f = std::fopen(out_path(c, name).c_str(), "wb");
+    if (!f) return fail(c, CF_ERR_ARG, "Output: cannot write %s", name);
+    const size_t w = std::fwrite(h.data(), sizeof(double), h.size(), f);
+    std::fclose(f);
+    return w == h.size() ? CF_OK : fail(c, CF_ERR_ARG, "Output: short write of %s", name);
+}
+
+int cf_Initial_condition(cf_ctx *c, int, double *, double *, double *, double *, double *, double *U1, double *U2,
+                         double *U3, double *U4, double *U5, double *U1q, double *U2q, double *U3q, double *U4q,
+                         double *U5q, double *J)
+{
+    if (!c) return CF_ERR_ARG;
+    double *U[5] = {U1, U2, U3, U4, U5}, *Uq[5] = {U1q, U2q, U3q, U4q, U5q};
+    cf_ptr5 u, uq;
+    if (int rc = restart_args(c, U, Uq, J, u, uq, "Initial_condition")) return rc;
+    const cf_dims &d = c->d;
+    const size_t N = (size_t)d.X_out * d.Y_out * d.Z_out;
+    std::vector<double> h(10 * N);
+    FILE *f = std::fopen(out_path(c, "initial.bin").c_str(), "rb");
+    if (!f) return fail(c, CF_ERR_ARG, "Initial_condition: cannot open initial.bin in '%s'", c->out_dir.c_str());
+    const size_t r = std::fread(h.data(), sizeof(double), h.size(), f);
+    std::fclose(f);
+    if (r != h.size()) return fail(c, CF_ERR_ARG, "Initial_condition: initial.bin holds %zu of %zu values", r, h.size());
+    double *img = static_cast<double *>(scratch_bytes(c, "restart", 10 * N * sizeof(double)));
+    if (!img) return fail(c, CF_ERR_NOMEM, "Initial_condition: scratch allocation failed");
+    if (int rc = cuda_check(c, cudaMemcpyAsync(img, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                               c->stream), "Initial_condition")) return rc;
+    if (int rc = cuda_check(c, cf_fast::restart_unpack(d, img, u, uq, R(c, J), c->stream), "Initial_condition"))
+        return rc;
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "Initial_condition");
+}
+
+// ---------------------------------------------------------------------------
+// physical time step driver (main.cpp:143-480)
+
+int cf_step_reset(cf_ctx *c)
+{
+    if (!c) return CF_ERR_ARG;
+    for (double &e : c->E) e = 0;
+    return CF_OK;
+}
+
+int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, int *iterations, double *er_out,
+            double *Q)
+{
+    if (!c || !pp || !f) return CF_ERR_ARG;
+    if (pp->max_iterations < 1) return fail(c, CF_ERR_ARG, "cf_step: max_iterations must be >= 1");
+    double *const *U_ = f->U_;
+    double *visc[79] = {nullptr};
+    for (int n = 0; n < 5; n++) visc[n] = U_[n];
+    for (int n = 0; n < 4; n++) visc[5 + n] = f->vF[n];
+    visc[9] = f->J;
+    for (int n = 0; n < 9; n++) visc[10 + n] = f->cell_metric[n];
+    for (int s = 0; s < 3; s++) {
+        visc[19 + 10 * s] = f->face_J[s];
+        for (int n = 0; n < 9; n++) visc[20 + 10 * s + n] = f->face_metric[s][n];
+    }
+    for (int n = 0; n < 4; n++) {
+        visc[55 + n] = f->LL[n];
+        visc[65 + n] = f->ML[n];
+        visc[75 + n] = f->NL[1 + n];
+    }
+    double *dts[64];
+    for (int n = 0; n < 5; n++) {
+        dts[n] = U_[n];
+        dts[5 + n] = f->U[n];
+        dts[10 + n] = f->Uq[n];
+        dts[25 + n] = f->inF[0][n];
+        dts[30 + n] = f->inF[1][n];
+        dts[35 + n] = f->inF[2][n];
+        dts[44 + n] = f->MR[n];
+        dts[49 + n] = f->NR[n];
+        dts[54 + n] = f->NL[n];
+        dts[59 + n] = f->Residual[n];
+    }
+    dts[15] = f->J;
+    for (int n = 0; n < 9; n++) dts[16 + n] = f->cell_metric[n];
+    for (int n = 0; n < 4; n++) dts[40 + n] = f->vF[n];
+    double er[5] = {0, 0, 0, 0, 0};
+    int it = 1;
+    for (;; it++) {
+        if (int rc = cf_X_periodic(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4])) return rc;
+        if (int rc = cf_Y_boundary_condition(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4], f->J)) return rc;
+        if (int rc = cf_Z_boundary_condition(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4], f->J)) return rc;
+        if (pp->filter)
+            if (int rc = cf_Filter(c, 0, pp->roe_criterion, pp->e_high, pp->e_low, U_[0], U_[1], U_[2], U_[3],
+                                   U_[4], f->Y_point, f->Ep[0], f->Ep[1], f->Ep[2], f->J)) return rc;
+        for (int dir = 0; dir < 3; dir++) {
+            double *p32[32] = {nullptr};
+            for (int n = 0; n < 5; n++) {
+                p32[n] = U_[n];
+                p32[26 + n] = f->inF[dir][n];
+            }
+            p32[15] = f->J;
+            p32[16] = f->face_J[dir];
+            for (int n = 0; n < 9; n++) p32[17 + n] = f->face_metric[dir][n];
+            p32[31] = f->Ep[dir];
+            static const char *names[2][3] = {{"Flux_X", "Flux_Y", "Flux_Z"},
+                                              {"Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter"}};
+            if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32)) return rc;
+        }
+        if (int rc = cf_Viscous_terms(c, 0, visc)) return rc;
+        if (int rc = cf_Dual_time_stepping(c, 0, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr,
+                                           nullptr, dts)) return rc;
+        for (int n = 0; n < 5; n++) {
+            c->E[n] = std::max(c->E[n], er[n]);
+            er[n] = er[n] / c->E[n];
+        }
+        const double tol = pp->tolerance;
+        if ((er[0] < tol && er[1] < tol && er[2] < tol && er[3] < tol) || it >= pp->max_iterations) break;
+    }
+    if (int rc = cf_Driven_force(c, 0, f->U[1], f->J, Q, nullptr)) return rc;
+    if (pp->statistic_step > 0) {
+        double *st[27] = {nullptr};
+        for (int n = 0; n < 5; n++) st[n] = U_[n];
+        st[5] = f->J;
+        st[6] = f->face_J[1];
+        for (int n = 0; n < 9; n++) st[7 + n] = f->face_metric[1][n];
+        st[26] = f->Ep[1];
+        if (int rc = cf_Statistic(c, 0, step, it, pp->statistic_step, st)) return rc;
+    }
+    cf_ptr5 u_, u, uq;
+    for (int n = 0; n < 5; n++) {
+        u_.p[n] = R(c, U_[n]);
+        u.p[n] = R(c, f->U[n]);
+        uq.p[n] = R(c, f->Uq[n]);
+    }
+    if (int rc = cuda_check(c, cf_fast::advance_levels(c->d, u_, u, uq, c->stream), "cf_step")) return rc;
+    if (iterations) *iterations = it;
+    if (er_out)
+        for (int n = 0; n < 5; n++) er_out[n] = er[n];
+    return CF_OK;
+}
 
 }  // extern "C"

@@ -36,6 +36,16 @@ constexpr int CF_LU_PACK = 52;   // doubles per cell of the sweep coefficient pa
     cudaError_t lu_copy(const cf_dims &d, const cf_lu_args &a, cudaStream_t s);                        \
     cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, cudaStream_t s);     \
     size_t lu_partial_count(const cf_dims &d);                                                          \
+    cudaError_t statistic(const cf_dims &d, const cf_stat_args &a, double *acc, double *partial,         \
+                          size_t partial_len, cudaStream_t s);                                          \
+    cudaError_t bulk_rows(const cf_dims &d, const double *U2, const double *J, double *jsum_dev,        \
+                          double *rows, double *partial, size_t partial_len, cudaStream_t s);           \
+    cudaError_t restart_pack(const cf_dims &d, const cf_ptr5 &U, const cf_ptr5 &Uq, const double *J,   \
+                             double *img, cudaStream_t s);                                              \
+    cudaError_t restart_unpack(const cf_dims &d, const double *img, const cf_ptr5 &U, const cf_ptr5 &Uq, \
+                               const double *J, cudaStream_t s);                                        \
+    cudaError_t advance_levels(const cf_dims &d, const cf_ptr5 &U_, const cf_ptr5 &U, const cf_ptr5 &Uq, \
+                               cudaStream_t s);                                                         \
     cudaError_t face_metrics(const cf_dims &d, const cf_metric_args &a, int which, double gamma,       \
                              cudaStream_t s);                                                           \
     }

@@ -112,6 +112,13 @@ struct cf_wave_args {
                              // pack landed, done); NULL when tracing is off
 };
 
+struct cf_stat_args {
+    const double *U[5];      // U1_..U5_
+    const double *J;         // cell Jacobian
+    const double *Jv;        // y-face Jacobian J_v
+    const double *m[9];      // y-face metrics xidx_v..ztdz_v
+};
+
 struct cf_rk3_args {
     double *U_[5];
     const double *U[5];

@@ -9,6 +9,7 @@
 #include "cf_filter.cuh"
 #include "cf_lusgs.cuh"
 #include "cf_wave.cuh"
+#include "cf_stats.cuh"
 #include "cf_launch.h"
 
 #ifdef CF_WITH_FLOAT
@@ -214,6 +215,81 @@ cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, cud
     k_lu_update<<<g, box_block(), 0, s>>>(d, a, b);
     const double DN = 1. / (d.X_out * d.Y_out * d.Z_out);
     k_lu_norm<<<1, 256, 0, s>>>(a.partial, lu_partial_count(d), DN, er_dev);
+    return cudaGetLastError();
+}
+
+template <int KIND>
+static cudaError_t stat_kind(const cf_dims &d, const cf_stat_args &a, double *partial, size_t partial_len,
+                             double *out, int Ym, st_qmap qm, int j0, int nrows, int accumulate,
+                             const double *jsum, cudaStream_t s)
+{
+    constexpr int NQ = st_kind<KIND>::NQ;
+    if (nrows <= 0) return cudaSuccess;
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 132;
+    }
+    int nchunk = std::max(1, std::min(d.X_out, (4 * sms + nrows - 1) / nrows));
+    while ((size_t)nrows * nchunk * NQ > partial_len && nchunk > 1) nchunk--;
+    if ((size_t)nrows * nchunk * NQ > partial_len) return cudaErrorInvalidValue;
+    k_stat_rows<KIND><<<dim3((unsigned)nrows, (unsigned)nchunk), ST_THREADS, 0, s>>>(d, a, partial, nchunk, jsum);
+    const int n = nrows * NQ;
+    k_stat_finish<NQ><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(partial, nrows, nchunk, j0, out, Ym, qm, accumulate);
+    return cudaGetLastError();
+}
+
+// Statistic's per-call accumulation into acc (17 rows of Ym): y-face Roe
+// quantities (rows 0..6, 8, 9), wall-normal shear (row 7), cell moments
+// (rows 10..16)
+cudaError_t statistic(const cf_dims &d, const cf_stat_args &a, double *acc, double *partial, size_t partial_len,
+                      cudaStream_t s)
+{
+    const int Ym = d.Ym;
+    st_qmap qf{{0, 1, 2, 3, 4, 5, 6, 8, 9}}, qs{{7}}, qm{{10, 11, 12, 13, 14, 15, 16}};
+    cudaError_t e = stat_kind<ST_FACE>(d, a, partial, partial_len, acc, Ym, qf, 1, d.ny, 1, nullptr, s);
+    if (e == cudaSuccess) e = stat_kind<ST_SHEAR>(d, a, partial, partial_len, acc, Ym, qs, 1, d.ny, 1, nullptr, s);
+    if (e == cudaSuccess)
+        e = stat_kind<ST_MOMENT>(d, a, partial, partial_len, acc, Ym, qm, 2, d.ny - 1, 1, nullptr, s);
+    return e;
+}
+
+// Driven_force's bulk-flow integral: rows[j] = row sums (j = 2..ny) into
+// out (Ym doubles), jsum_dev receives Jsum
+cudaError_t bulk_rows(const cf_dims &d, const double *U2, const double *J, double *jsum_dev, double *rows,
+                      double *partial, size_t partial_len, cudaStream_t s)
+{
+    k_bulk_jsum<<<1, 32, 0, s>>>(d, J, jsum_dev);
+    cf_stat_args a{};
+    a.U[1] = U2;
+    a.J = J;
+    st_qmap q0{{0}};
+    return stat_kind<ST_BULK>(d, a, partial, partial_len, rows, d.Ym, q0, 2, d.ny - 1, 0, jsum_dev, s);
+}
+
+cudaError_t restart_pack(const cf_dims &d, const cf_ptr5 &U, const cf_ptr5 &Uq, const double *J, double *img,
+                         cudaStream_t s)
+{
+    const size_t N = (size_t)d.X_out * d.Y_out * d.Z_out;
+    k_restart_pack<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(d, U, Uq, J, img);
+    return cudaGetLastError();
+}
+
+cudaError_t restart_unpack(const cf_dims &d, const double *img, const cf_ptr5 &U, const cf_ptr5 &Uq,
+                           const double *J, cudaStream_t s)
+{
+    const size_t N = (size_t)d.X_out * d.Y_out * d.Z_out;
+    k_restart_unpack<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(d, img, U, Uq, J);
+    return cudaGetLastError();
+}
+
+cudaError_t advance_levels(const cf_dims &d, const cf_ptr5 &U_, const cf_ptr5 &U, const cf_ptr5 &Uq,
+                           cudaStream_t s)
+{
+    cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+    k_advance_levels<<<box_grid(b), box_block(), 0, s>>>(d, U_, U, Uq, b);
     return cudaGetLastError();
 }
 

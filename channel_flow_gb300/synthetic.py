@@ -24,6 +24,7 @@ MU_L = 0.0000185
 PR_L = 0.72
 F_BODY = 599.29876710   # prm.h:14
 HIGH = 0.005            # prm.h:19, channel height 2h
+Q0_BULK = 20.464969232814912   # prm.h:15, Driven_force's target bulk flux
 T_WALL = 298.0592       # Y_boundary_condition.cpp:87
 RHO_REF = 1.1842        # main.cpp:382 normalisation density
 
@@ -47,6 +48,7 @@ class Grid:
     Pr_L: float = PR_L
     f: float = F_BODY
     high: float = HIGH
+    Q0: float = Q0_BULK
 
     @property
     def shape(self):

@@ -49,7 +49,7 @@ typedef struct cf_ctx cf_ctx;
 /* Grid and constants.  The reference fixes these at compile time:
  * Resolution.h (cell counts X_out, Y_out, Z_out and spacings deltaXI,
  * deltaET, deltaZT), prm.h (K = 1.4, R = 287, e = 1e-4, f = 599.29876710,
- * high = 0.005) and Viscous_terms.h (Cv = 717.5, mu_L = 1.85e-5,
+ * high = 0.005, Q0 = 20.464969232814912) and Viscous_terms.h (Cv = 717.5, mu_L = 1.85e-5,
  * Pr_L = 0.72).  The field names differ from those macro names so that this
  * header can be included after the reference's headers. */
 typedef struct {
@@ -58,6 +58,7 @@ typedef struct {
     double gamma_gas, r_gas, beta_min;      /* K, R, e */
     double cv, mu, prandtl;                 /* Cv, mu_L, Pr_L */
     double body_force, height;              /* f, high */
+    double bulk_flux;                       /* Q0 (prm.h), the Driven_force target */
 } cf_grid;
 
 /* ------------------------------------------------------------------ */
@@ -215,6 +216,87 @@ int cf_Jacobian_w(cf_ctx *ctx, int myid, double **arrays10);
 /* replaces Jacobian_v (Jacobian_v.cpp:17): J_v + 9 face metrics, then J +
  * 9 cell metrics (read for the wall rows) */
 int cf_Jacobian_v(cf_ctx *ctx, int myid, double **arrays20);
+
+
+/* ------------------------------------------------------------------ */
+/* reductions and IO around the step (FP64 in every precision mode)      */
+/* ------------------------------------------------------------------ */
+
+/* Directory for the files of Statistic (Shear_stress.dat, ND%05d.dat,
+ * st%05d.dat), Output (LES%05d.bin) and Initial_condition (initial.bin);
+ * default ".", the reference's current directory. */
+int cf_set_output_dir(cf_ctx *ctx, const char *dir);
+
+/* Driven_force.cpp:14 (U2_, J): the bulk-flow integral Q and
+ * ER_Q = |Q0 - Q| / Q0 (the reference prints them; either pointer may be
+ * NULL).  Deterministic FP64 reduction. */
+int cf_Driven_force(cf_ctx *ctx, int myid, double *U2_, double *J, double *Q, double *ER_Q);
+
+/* Statistic.cpp:16.  Arrays in the reference's order (27): U1_..U5_, J,
+ * J_v, xidx_v..ztdz_v, MR1..5, ML1..5, EpY; only the first 16 are read (the
+ * MR/ML scratch the reference overwrites is left untouched).  Adds this
+ * call's y-row sums to accumulators kept in the context, appends the wall
+ * shear increments to Shear_stress.dat and, when step % statistic_step == 0,
+ * writes ND%05d.dat and st%05d.dat in the reference's format and clears the
+ * accumulators. */
+int cf_Statistic(cf_ctx *ctx, int myid, int step, int iteration, int statistic_step, double **arrays27);
+/* accumulators: 17 rows of Y_m doubles (ULm URm VLm VRm rhoLm rhoRm RUVm
+ * SXYm Roe_Dm dRLm Um Vm Wm UUm VVm WWm UVm, raw sums) then SXY_bottom,
+ * SXY_up: 17*Y_m + 2 values */
+int cf_statistic_read(cf_ctx *ctx, double *out);
+int cf_statistic_reset(cf_ctx *ctx);
+
+/* Output.cpp:14 / Initial_condition.cpp:10: the restart image LES%05d.bin
+ * (ten float64 blocks [X_out][Y_out][Z_out] of U1..U5, U1q..U5q times J)
+ * written from, and initial.bin read into, the device fields.
+ * Initial_condition fills U1..U5 and U1q..U5q; U1_..U5_ are not read. */
+int cf_Output(cf_ctx *ctx, int step, int myid, double *U1, double *U2, double *U3, double *U4, double *U5,
+              double *U1q, double *U2q, double *U3q, double *U4q, double *U5q, double *J);
+int cf_Initial_condition(cf_ctx *ctx, int myid, double *U1_, double *U2_, double *U3_, double *U4_, double *U5_,
+                         double *U1, double *U2, double *U3, double *U4, double *U5, double *U1q, double *U2q,
+                         double *U3q, double *U4q, double *U5q, double *J);
+
+
+/* ------------------------------------------------------------------ */
+/* physical time step driver (main.cpp:143-480)                          */
+/* ------------------------------------------------------------------ */
+
+/* The device fields of a run (one per reference array; arrays the
+ * routines treat as scratch may be shared). */
+typedef struct {
+    double *U_[5], *U[5], *Uq[5];      /* pseudo-time state, level n, level n-1 */
+    double *J, *Y_point;
+    double *cell_metric[9];            /* xidx..ztdz */
+    double *face_J[3];                 /* J_u, J_v, J_w */
+    double *face_metric[3][9];         /* xidx_u..ztdz_u, then _v, then _w */
+    double *Ep[3];                     /* EpX, EpY, EpZ */
+    double *inF[3][5];                 /* inFx1..5, inFy1..5, inFz1..5 */
+    double *vF[4];                     /* vF2..vF5 */
+    double *LL[4], *ML[4];             /* viscous face-flux scratch LL2..5, ML2..5 */
+    double *MR[5], *NR[5], *NL[5], *Residual[5];
+} cf_fields;
+
+typedef struct {
+    double deltaT;
+    int max_iterations;        /* pseudo-time iterations at most (iteration_end_step, main.cpp:48) */
+    double tolerance;          /* er_n / max(er_n) of fields 1-4 below this ends the step (main.cpp:406) */
+    int limiter;               /* 1: Flux_X/Y/Z_limiter, 0: Flux_X/Y/Z */
+    int filter;                /* 1: Filter (its Ep switches the limited fluxes' dissipation) */
+    double roe_criterion, e_high, e_low;
+    int statistic_step;        /* > 0: Statistic after the step */
+} cf_step_params;
+
+/* One physical time step: pseudo-time iterations of x halo, wall and
+ * periodic ghosts, [Filter], three fluxes, viscous terms and
+ * Dual_time_stepping until the normalised residuals of fields 1-4 drop
+ * below the tolerance (the maxima persist across steps, main.cpp:63, 387)
+ * or max_iterations; then Driven_force (Q), Statistic when
+ * statistic_step > 0, and Uq <- U, U <- U_.  Returns the iteration count,
+ * the last normalised er1..er5 and Q (pointers may be NULL). */
+int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields *fields, int *iterations,
+            double *er, double *Q);
+/* forget the running residual maxima */
+int cf_step_reset(cf_ctx *ctx);
 
 #ifdef __cplusplus
 }

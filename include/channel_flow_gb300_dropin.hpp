@@ -36,6 +36,12 @@ inline cf_ctx *&ctx()
     return c;
 }
 
+inline double &q0()
+{
+    static double q = 0;
+    return q;
+}
+
 inline void check(int rc, const char *what)
 {
     if (rc != CF_OK) {
@@ -52,6 +58,7 @@ inline void init(int precision = CF_PREC_FP64)
     g.d_xi = deltaXI;
     g.d_eta = deltaET;
     g.d_zeta = deltaZT;
+    q0() = g.bulk_flux;
     check(cf_create(&g, precision, &ctx()), "cf_create");
 }
 
@@ -198,6 +205,40 @@ inline void Jacobian_v(int myid, A... a)
     double *p[20];
     cf_collect(p, a...);
     cfdrop::check(cf_Jacobian_v(cfdrop::ctx(), myid, p), "Jacobian_v");
+}
+
+/* Driven_force.cpp:14: prints the bulk flux as the reference does */
+inline void Driven_force(int myid, cf_field U2_, cf_field J)
+{
+    double Q = 0, ER_Q = 0;
+    cfdrop::check(cf_Driven_force(cfdrop::ctx(), myid, CF_P(U2_), CF_P(J), &Q, &ER_Q), "Driven_force");
+    if (myid == 0) std::printf("Q0=%f\tQall=%f\tER_Q=%f\n", cfdrop::q0(), Q, ER_Q);
+}
+
+template <typename... A>
+inline void Statistic(int myid, int step, int iteration, int statistic_step, A... a)
+{
+    static_assert(sizeof...(A) == 27, "Statistic takes 27 arrays");
+    double *p[27];
+    cf_collect(p, a...);
+    cfdrop::check(cf_Statistic(cfdrop::ctx(), myid, step, iteration, statistic_step, p), "Statistic");
+}
+
+inline void Output(int step, int myid, cf_field U1, cf_field U2, cf_field U3, cf_field U4, cf_field U5,
+                   cf_field U1q, cf_field U2q, cf_field U3q, cf_field U4q, cf_field U5q, cf_field J)
+{
+    cfdrop::check(cf_Output(cfdrop::ctx(), step, myid, CF_P(U1), CF_P(U2), CF_P(U3), CF_P(U4), CF_P(U5),
+                            CF_P(U1q), CF_P(U2q), CF_P(U3q), CF_P(U4q), CF_P(U5q), CF_P(J)), "Output");
+}
+
+template <typename... A>
+inline void Initial_condition(int myid, A... a)
+{
+    static_assert(sizeof...(A) == 16, "Initial_condition takes 16 arrays");
+    double *p[16];
+    cf_collect(p, a...);
+    cfdrop::check(cf_Initial_condition(cfdrop::ctx(), myid, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8],
+                                       p[9], p[10], p[11], p[12], p[13], p[14], p[15]), "Initial_condition");
 }
 
 #undef CF_P

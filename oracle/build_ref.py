@@ -47,7 +47,7 @@ SOURCES = [
     "Viscous_terms.cpp", "Filter.cpp", "RK3NODT.cpp",
     "Dual_time_stepping.cpp", "DPLUSGS.cpp", "Hyperplane.cpp",
     "Grid.cpp", "Jacobian.cpp", "Jacobian_u.cpp", "Jacobian_v.cpp", "Jacobian_w.cpp",
-    "Driven_force.cpp",
+    "Driven_force.cpp", "Statistic.cpp", "Output.cpp", "Initial_condition.cpp",
 ]
 
 
@@ -103,14 +103,16 @@ def resolution_header(X_out, Y_out, Z_out, dxi, det, dzt) -> str:
 def build(X_out: int, Y_out: int, Z_out: int, deltas=None, jobs: int = 8,
           verbose: bool = False) -> Path:
     """Compile the reference routines for one grid; return the .so path.
-    Rebuilds only when the library is missing."""
+    Rebuilds when the library is missing or older than the harness, the
+    stand-in headers or this recipe."""
     ref = reference_dir()
     if not (ref / "Flux_X_limiter.cpp").exists():
         raise FileNotFoundError(f"reference sources not found under {ref}")
     dxi, det, dzt = deltas if deltas is not None else default_deltas(X_out, Y_out, Z_out)
     out = REF_OUT / grid_tag(X_out, Y_out, Z_out, dxi, det, dzt)
     lib = out / "libcfref.so"
-    if lib.exists():
+    deps = [HERE / "ref_harness.cpp", Path(__file__)] + sorted(OVERRIDES.rglob("*.h"))
+    if lib.exists() and all(lib.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return lib
     out.mkdir(parents=True, exist_ok=True)
     (out / "Resolution.h").write_text(resolution_header(X_out, Y_out, Z_out, dxi, det, dzt))

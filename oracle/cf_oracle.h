@@ -70,6 +70,17 @@ void cfo_Jacobian_w(const cfo_grid *g, double gamma, double **a);
 /* bulk flow integral Q (Driven_force.cpp:38-62): U2_, J */
 double cfo_Driven_force(const cfo_grid *g, double **a);
 
+/* Statistic (Statistic.cpp): 27 arrays U1_..5, J, J_v, 9 metrics _v,
+ * MR1..5, ML1..5, EpY; acc = 17*Y_m + 2 accumulators kept across calls;
+ * shear[2] = wall shear-stress increments; when step % statistic_step == 0
+ * nd[10][Y_m] and st[7][Y_m] receive the averages (returns 1) */
+int cfo_Statistic(const cfo_grid *g, double *acc, int step, int iteration, int statistic_step, double **a,
+                  double *shear, double *nd, double *st);
+
+/* restart image of Output / Initial_condition (cf_oracle_io.c) */
+void cfo_restart_pack(const cfo_grid *g, double **a, double *out);
+void cfo_restart_unpack(const cfo_grid *g, const double *img, double **a);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
-PORT_SOURCES = ["cf_oracle_flux.c", "cf_oracle_visc.c", "cf_oracle_filter.c", "cf_oracle_lusgs.c"]
+PORT_SOURCES = ["cf_oracle_flux.c", "cf_oracle_visc.c", "cf_oracle_filter.c", "cf_oracle_lusgs.c",
+                "cf_oracle_stat.c", "cf_oracle_io.c"]
 _lock = threading.Lock()
 
 
@@ -131,6 +132,37 @@ class Port:
         gs = grid_struct(g)
         return self.lib.cfo_Driven_force(C.byref(gs), _ptrs([U2, J]))
 
+    @staticmethod
+    def statistic_state(g):
+        """Accumulators of Statistic (17 rows of Y_m, then SXY_bottom, SXY_up)."""
+        return np.zeros(17 * (g.Y_out + 4) + 2)
+
+    def Statistic(self, g, acc, step, iteration, statistic_step, arrays):
+        """One Statistic call; returns (written, shear[2], nd[10][Y_m], st[7][Y_m])."""
+        Ym = g.Y_out + 4
+        shear = np.zeros(2)
+        nd = np.zeros((10, Ym))
+        st = np.zeros((7, Ym))
+        gs = grid_struct(g)
+        dp = C.POINTER(C.c_double)
+        w = self.lib.cfo_Statistic(C.byref(gs), acc.ctypes.data_as(dp), C.c_int(step), C.c_int(iteration),
+                                   C.c_int(statistic_step), _ptrs(arrays), shear.ctypes.data_as(dp),
+                                   nd.ctypes.data_as(dp), st.ctypes.data_as(dp))
+        return bool(w), shear, nd, st
+
+    def restart_pack(self, g, arrays):
+        """The LES%05d.bin image of U1..U5, U1q..U5q (times J), as float64."""
+        out = np.zeros(10 * g.X_out * g.Y_out * g.Z_out)
+        gs = grid_struct(g)
+        self.lib.cfo_restart_pack(C.byref(gs), _ptrs(arrays), out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def restart_unpack(self, g, image, arrays):
+        """Initial_condition's fill of U1..U5, U1q..U5q (divided by J)."""
+        gs = grid_struct(g)
+        img = np.ascontiguousarray(image, dtype=np.float64)
+        self.lib.cfo_restart_unpack(C.byref(gs), img.ctypes.data_as(C.POINTER(C.c_double)), _ptrs(arrays))
+
 
 def hyperplane_buffers(g):
     X_np = g.X_out + 6
@@ -167,6 +199,18 @@ class Reference:
 
     def Z_boundary_condition(self, g, arrays):
         self._call("Z_boundary_condition", arrays)
+
+    def Statistic(self, step, iteration, statistic_step, arrays):
+        """The reference's Statistic; writes its files in the current directory."""
+        self.lib.ref_Statistic(C.c_int(step), C.c_int(iteration), C.c_int(statistic_step), _ptrs(arrays))
+
+    def Output(self, step, arrays):
+        """The reference's Output (U1..U5, U1q..U5q, J): LES%05d.bin in the current directory."""
+        self.lib.ref_Output(C.c_int(step), _ptrs(arrays))
+
+    def Initial_condition(self, arrays):
+        """The reference's Initial_condition (16 arrays): reads initial.bin in the current directory."""
+        self.lib.ref_Initial_condition(_ptrs(arrays))
 
     def flux(self, name, g, arrays):
         self._call(name, arrays)

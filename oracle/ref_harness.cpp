@@ -144,4 +144,27 @@ void ref_Jacobian_v(double **a)
 /* Driven_force.cpp:14 (U2_, J); prints the bulk-flux line */
 void ref_Driven_force(double **a) { Driven_force(0, P(0), P(1)); }
 
+/* Statistic.cpp:16 (U1_..U5_, J, J_v, 9 metrics _v, MR1..5, ML1..5, EpY);
+ * appends Shear_stress.dat and writes ND%05d.dat / st%05d.dat in the
+ * current directory every statistic_step steps */
+void ref_Statistic(int step, int iteration, int statistic_step, double **a)
+{
+    Statistic(0, step, iteration, statistic_step, P(0), P(1), P(2), P(3), P(4), P(5), P(6), P(7), P(8), P(9),
+              P(10), P(11), P(12), P(13), P(14), P(15), P(16), P(17), P(18), P(19), P(20), P(21), P(22), P(23),
+              P(24), P(25), P(26));
+}
+
+/* Output.cpp:15 (U1..U5, U1q..U5q, J): writes LES%05d.bin */
+void ref_Output(int step, double **a)
+{
+    Output(step, 0, P(0), P(1), P(2), P(3), P(4), P(5), P(6), P(7), P(8), P(9), P(10));
+}
+
+/* Initial_condition.cpp:10 (U1_..U5_, U1..U5, U1q..U5q, J): reads initial.bin */
+void ref_Initial_condition(double **a)
+{
+    Initial_condition(0, P(0), P(1), P(2), P(3), P(4), P(5), P(6), P(7), P(8), P(9), P(10), P(11), P(12), P(13),
+                      P(14), P(15));
+}
+
 } /* extern "C" */

@@ -199,3 +199,85 @@ def digest(a, mask=None):
     if mask is not None:
         a[mask] = 0.0
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()[:32]
+
+
+def statistic_case(g, seed=0):
+    """27 arrays in Statistic's order: U1_..5, J, J_v + 9 face metrics,
+    MR1..5, ML1..5 (scratch the routine overwrites), EpY."""
+    rng = np.random.default_rng(seed + 13)
+    U, J = state(g, seed)
+    fm = metric_set(g, "v", seed + 17)
+    MR = [_rand_like(g, rng) for _ in range(5)]
+    ML = [_rand_like(g, rng) for _ in range(5)]
+    Ep = rng.choice(np.asarray([0.0, 1.0]), size=g.shape)
+    return U + [J] + fm + MR + ML + [Ep]
+
+
+def restart_case(g, seed=0):
+    """11 arrays in Output's order: U1..U5, U1q..U5q, J."""
+    U, J = state(g, seed)
+    Uq, _ = state(g, seed + 1)
+    return U + Uq + [J]
+
+
+def step_case(g, seed=0):
+    """The fields of one physical step (cf_fields), as numpy arrays: the
+    state at three time levels, cell and face metrics, Y_point and zeroed
+    outputs and scratch."""
+    rng = np.random.default_rng(seed + 29)
+    U_, J = state(g, seed)
+    U = [x * (1 + 1e-6 * rng.uniform(-1, 1, g.shape)) for x in U_]
+    Uq = [x * (1 + 1e-6 * rng.uniform(-1, 1, g.shape)) for x in U_]
+    z = lambda: np.zeros(g.shape)
+    faces = [metric_set(g, w, seed + s) for w, s in (("u", 31), ("v", 41), ("w", 51))]
+    return {"U_": U_, "U": U, "Uq": Uq, "J": J, "Y_point": y_points(g),
+            "cell_metric": metric_set(g, "cell", seed + 1000)[1:],
+            "face_J": [f[0] for f in faces], "face_metric": [f[1:] for f in faces],
+            "Ep": [z() for _ in range(3)], "inF": [[z() for _ in range(5)] for _ in range(3)],
+            "vF": [z() for _ in range(4)], "LL": [z() for _ in range(4)], "ML": [z() for _ in range(4)],
+            "MR": [z() for _ in range(5)], "NR": [z() for _ in range(5)], "NL": [z() for _ in range(5)],
+            "Residual": [z() for _ in range(5)]}
+
+
+def port_step(port, g, f, deltaT, max_iterations, tolerance, E, crit=(0.007, 1.0, 0.0)):
+    """The same physical step on the C oracle: the loop of main.cpp:143-480
+    with Filter and the limited fluxes; f is modified in place, E (running
+    maxima) too.  Returns (iterations, er, Q)."""
+    from oracle.cforacle import hyperplane_buffers
+    U_, J = f["U_"], f["J"]
+    s10 = [np.zeros(g.shape) for _ in range(10)]
+    Nijk, ijk = port.Hyperplane(g)
+    visc_scratch = [np.zeros(g.shape) for _ in range(30)]
+    it = 0
+    while True:
+        it += 1
+        port.x_periodic(g, U_)
+        port.Y_boundary_condition(g, U_ + [J])
+        port.Z_boundary_condition(g, U_ + [J])
+        port.Filter(g, *crit, U_ + [f["Y_point"]] + f["Ep"] + [J])
+        for d, name in enumerate(("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter")):
+            port.flux(name, g, U_ + s10 + [J, f["face_J"][d]] + f["face_metric"][d] + f["inF"][d] + [f["Ep"][d]])
+        visc = U_ + f["vF"] + [J] + f["cell_metric"]
+        for d in range(3):
+            visc += [f["face_J"][d]] + f["face_metric"][d]
+        # LR, LL, MR, ML, NR, NL scratch blocks; LL2..5, ML2..5 and NL2..5 are the
+        # driver's shared arrays
+        LR, LL1, MR_, ML1, NR_ = visc_scratch[0:5], visc_scratch[5], visc_scratch[10:15], visc_scratch[15], \
+            visc_scratch[20:25]
+        visc += LR + [LL1] + f["LL"] + MR_ + [ML1] + f["ML"] + NR_ + f["NL"]
+        port.Viscous_terms(g, visc)
+        dts = U_ + f["U"] + f["Uq"] + [J] + f["cell_metric"] + f["inF"][0] + f["inF"][1] + f["inF"][2] + \
+            f["vF"] + f["MR"] + f["NR"] + f["NL"] + f["Residual"]
+        er = port.Dual_time_stepping(g, deltaT, Nijk, ijk, dts)
+        for n in range(5):
+            E[n] = max(E[n], er[n])
+            er[n] = er[n] / E[n]
+        if (er[0] < tolerance and er[1] < tolerance and er[2] < tolerance and er[3] < tolerance) \
+                or it >= max_iterations:
+            break
+    Q = port.Driven_force(g, f["U"][1], J)
+    ix = g.interior
+    for n in range(5):
+        f["Uq"][n][ix] = f["U"][n][ix]
+        f["U"][n][ix] = f["U_"][n][ix]
+    return it, np.asarray(er), Q

@@ -37,6 +37,10 @@ int main(int argc, char **)
                 a,a,a,a,a, a,a,a,a,a, a,a,a,a,a, a, a,a,a,a,a,a,a,a,a,
                 a,a,a,a,a, a,a,a,a,a, a,a,a,a,a, a,a,a,a, a,a,a,a,a);
         Hyperplane(0, Nijk, ijk);
+        Driven_force(0, a, a);
+        Statistic(0, 1, 1, 5000, a,a,a,a,a, a, a, a,a,a,a,a,a,a,a,a, a,a,a,a,a, a,a,a,a,a, a);
+        Output(10, 0, a,a,a,a,a, a,a,a,a,a, a);
+        Initial_condition(0, a,a,a,a,a, a,a,a,a,a, a,a,a,a,a, a);
         Dual_time_stepping(0, 5e-8, &er1, &er2, &er3, &er4, &er5, Nijk, ijk,
                 a,a,a,a,a, a,a,a,a,a, a,a,a,a,a, a, a,a,a,a,a,a,a,a,a,
                 a,a,a,a,a, a,a,a,a,a, a,a,a,a,a, a,a,a,a, a,a,a,a,a,
