@@ -98,6 +98,7 @@ _SIGS = {
     "cf_Initial_condition": ([P, C.c_int] + [P] * 16, C.c_int),
     "cf_step": ([P, P, C.c_int, P, P, P, P], C.c_int),
     "cf_step_reset": ([P], C.c_int),
+    "cf_gemm_bf16": ([P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P], C.c_int),
 }
 for _n in ("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter", "Flux_X", "Flux_Y", "Flux_Z"):
     _SIGS["cf_" + _n] = ([P, C.c_int] + [P] * 32, C.c_int)

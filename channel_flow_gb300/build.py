@@ -9,7 +9,9 @@ Three translation units, compiled in parallel with nvcc:
   reduced-division face fluxes (CF_FAST_MATH) and the FP32 instantiations;
 * ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h);
 * ``cf_noalloc.cu``: the allocation-free DPLUSGS entry point (its scratch is
-  a file-scope device array).
+  a file-scope device array);
+* ``cf_mlp.cu``: the learned initial guess (tcgen05 BF16 GEMMs, TMA) and
+  its training kernels.
 
 Usage: ``python -m channel_flow_gb300.build [--verbose] [--ptxas]``
 """
@@ -62,6 +64,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "-DCF_FAST_MATH", "--fmad=true"]),
         ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
         ("cf_noalloc.cu", "cf_noalloc.o", ["-DCF_NS=cf_noalloc", "--fmad=false"]),
+        ("cf_mlp.cu", "cf_mlp.o", []),
     ]
 
     def cc(u):
@@ -72,7 +75,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
             raise RuntimeError(f"nvcc failed ({src} {' '.join(extra)}):\n{r.stderr[-6000:]}")
         return r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=4) as ex:
+    with cf.ThreadPoolExecutor(max_workers=5) as ex:
         logs = list(ex.map(cc, units))
     if verbose or ptxas:
         for log in logs:

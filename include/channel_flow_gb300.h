@@ -298,6 +298,20 @@ int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields
 /* forget the running residual maxima */
 int cf_step_reset(cf_ctx *ctx);
 
+
+/* ------------------------------------------------------------------ */
+/* learned initial guess: tensor-core building blocks (cf_mlp.cu)         */
+/* ------------------------------------------------------------------ */
+
+/* C = A B^T on the tcgen05 tensor cores: A [M x K] and B [N x K] row-major
+ * BF16 device matrices (16-byte aligned), FP32 accumulation.  M multiple
+ * of 128, K multiple of 64, N multiple of 16, ldo >= N and a multiple of 8.
+ * epilogue 0: out = C (float); 1: z = C + bias, out = SiLU(z) (bf16), zout
+ * (float, optional) = z; 2: out = C + bias (float).  err_dev (device int)
+ * gets a nonzero bit if a bounded device wait ran out. */
+int cf_gemm_bf16(void *cuda_stream, const void *A, const void *B, int M, int N, int K, int epilogue,
+                 const float *bias, void *out, float *zout, int ldo, int *err_dev);
+
 #ifdef __cplusplus
 }
 #endif
