@@ -277,6 +277,7 @@ def main():
     ap.add_argument("--grid", default="x".join(map(str, GRID)))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess physical-step comparison")
     ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs"],
                     help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
                          "(one LU-SGS pseudo-iteration per step, for profiling)")
@@ -476,6 +477,69 @@ def pseudo_iteration(ctx, g, w, calls, stream, torch, steps):
             "per_routine_ms": {k: round(v, 4) for k, v in per.items()}}
 
 
+def learned_guess_steps(torch, dims=(256, 192, 192), harvest=8, evals=3, epochs=20):
+    """Wall time per physical step at equal residual tolerance (1e-3 drop of
+    er_n / max er_n, main.cpp:406), plain FP64 vs FP32 vs FP32 with the
+    learned initial guess, on the 256 x 192 x 192 channel.  The assembled
+    dual-time loop of the reference is stable with the unlimited fluxes and
+    no filter at dt = 5e-9 on a Mach 0.05 laminar-plus-1% channel (with the
+    limiter and filter it diverges, as the reference does), so that is the
+    scheme of this comparison.  Each mode runs `harvest` plain steps (the
+    learned mode trains on them), then `evals` timed steps."""
+    import channel_flow_gb300 as cf
+    from channel_flow_gb300 import mlp, stepper, synthetic as syn
+    g = syn.channel_grid(*dims)
+    cm = syn.flat_metrics(g, GAMMA, "cell")
+    J = cm["J"]
+    host = {"U": syn.channel_state(g, J, seed=SEED, mach=0.05, noise=0.01, jitter=0.001, gamma=GAMMA),
+            "J": J, "cm": [cm[n] for n in syn.METRIC_NAMES], "Yp": syn.y_points(g, gamma=GAMMA)}
+    kw = dict(deltaT=5e-9, max_iterations=60, tolerance=1e-3, limiter=False, filter=False)
+    out = {"grid": list(dims), "scheme": "Flux_X/Y/Z (unlimited) + Viscous_terms + Dual_time_stepping, "
+                                         "dt 5e-9, tolerance 1e-3", "harvest_steps": harvest,
+           "timed_steps": evals}
+    for mode in ("fp64", "fp32", "fp32+extrapolate", "fp32+learned"):
+        prec = "fp64" if mode == "fp64" else "fp32"
+        ctx = cf.Context(g, precision=prec, gamma=GAMMA)
+        w = DeviceWorkload(ctx, g, host, torch)
+        st = stepper.Stepper(ctx, stepper.fields_from_workload(w, torch, g), **kw)
+        hist = [[u.clone() for u in w.U]]
+        for _ in range(harvest):
+            st.step()
+            hist.append([u.clone() for u in st.f["U"]])
+        guess, train_s = None, 0.0
+        if mode == "fp32+extrapolate":
+            guess = "extrapolate"
+        elif mode == "fp32+learned":
+            t0 = time.perf_counter()
+            guess = mlp.LearnedGuess(capacity=g.cells, seed=0, lr=2e-3)
+            losses = guess.train(g, hist, epochs=epochs)
+            torch.cuda.synchronize()
+            train_s = time.perf_counter() - t0
+        del hist
+        its, ms = [], []
+        for _ in range(evals):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            it, er, q = st.step(guess)
+            e1.record()
+            torch.cuda.synchronize()
+            its.append(it)
+            ms.append(e0.elapsed_time(e1))
+        out[mode] = {"subiterations": its, "ms_per_step": ms, "s_per_step_mean": float(np.mean(ms)) * 1e-3}
+        if mode == "fp32+learned":
+            out[mode]["training_s"] = train_s
+            out[mode]["training_loss_first_last"] = [losses[0], losses[-1]]
+            del guess
+        ctx.close()
+        del w, st
+        torch.cuda.empty_cache()
+    base = out["fp64"]["s_per_step_mean"]
+    for mode in ("fp32", "fp32+extrapolate", "fp32+learned"):
+        out[mode]["speedup_vs_fp64"] = base / out[mode]["s_per_step_mean"]
+    return out
+
+
 def secondary(ctx, g, w, calls, stream, torch, args):
     """Per precision: the RHS and one dual-time pseudo-iteration (RHS +
     hyperplane LU-SGS) on the benchmark grid, and on the 256 x 192 x 192
@@ -506,6 +570,11 @@ def secondary(ctx, g, w, calls, stream, torch, args):
     for k, v in out.items():
         if "fp64" in v and "fp32" in v:
             v["physical_step_fp64_over_fp32"] = v["fp64"]["physical_step_s"] / v["fp32"]["physical_step_s"]
+    if not args.no_large and not args.no_learned:
+        try:
+            out["physical_step_to_tolerance"] = learned_guess_steps(torch)
+        except Exception as exc:
+            out["physical_step_to_tolerance"] = {"error": repr(exc)}
     out["note"] = ("physical step = 10 LU-SGS sub-iterations x (RHS + Dual_time_stepping), the schedule of "
                    "configs 0 and 1; FP32 = flux/viscous/filter/LU-SGS sweeps in FP32, state update and "
                    "norms FP64; no learned initial guess")

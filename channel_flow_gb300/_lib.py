@@ -99,6 +99,16 @@ _SIGS = {
     "cf_step": ([P, P, C.c_int, P, P, P, P], C.c_int),
     "cf_step_reset": ([P], C.c_int),
     "cf_gemm_bf16": ([P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P], C.c_int),
+    "cf_mlp_features": ([P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
+    "cf_mlp_targets": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
+    "cf_mlp_apply": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P], C.c_int),
+    "cf_mlp_rms": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),
+    "cf_mlp_loss_grad": ([P, P, P, C.c_longlong, C.c_longlong, P, P, P], C.c_int),
+    "cf_mlp_silu_bwd": ([P, P, P, C.c_longlong, P, P], C.c_int),
+    "cf_transpose_bf16": ([P, P, C.c_longlong, C.c_int, P], C.c_int),
+    "cf_colsum_bf16": ([P, P, C.c_longlong, C.c_int, P], C.c_int),
+    "cf_adam": ([P, P, P, P, P, C.c_longlong, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int], C.c_int),
+    "cf_mlp_pack": ([P, P, P, P, P, P, P, P, P], C.c_int),
 }
 for _n in ("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter", "Flux_X", "Flux_Y", "Flux_Z"):
     _SIGS["cf_" + _n] = ([P, C.c_int] + [P] * 32, C.c_int)

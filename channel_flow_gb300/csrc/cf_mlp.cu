@@ -19,6 +19,8 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
+#include <cmath>
 
 #include "../../include/channel_flow_gb300.h"
 
@@ -267,6 +269,239 @@ static cudaError_t launch_gemm(const CUtensorMap &ta, const CUtensorMap &tb, int
     return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// MLP data movement and training kernels (FP32 / BF16, device pointers)
+
+constexpr int MLP_IN = 270, MLP_K1 = 320, MLP_H = 128, MLP_OUT = 5, MLP_N3 = 16, MLP_K3 = 64;
+
+struct mlp_grid {
+    int X, Y, Z;            // interior cells
+    __host__ __device__ int Ym() const { return Y + 4; }
+    __host__ __device__ int Zm() const { return Z + 4; }
+    // interior cell r (x-major, z fastest) -> field index
+    __host__ __device__ size_t cell(long long r) const
+    {
+        const int k = (int)(r % Z), j = (int)((r / Z) % Y), i = (int)(r / ((long long)Z * Y));
+        return ((size_t)(i + 3) * Ym() + (j + 2)) * Zm() + (k + 2);
+    }
+};
+
+struct mlp_levels {
+    const double *u[3][5];  // U^n, U^{n-1}, U^{n-2}
+};
+
+// features of row r: for level l (0: U^n - U^{n-1}, 1: U^{n-1} - U^{n-2}),
+// variable v and neighbour s of the 3x3x3 stencil, the scaled difference;
+// columns 270..319 are zero
+__global__ void k_mlp_features(mlp_grid g, mlp_levels L, const float *scale, const int *rows, long long M,
+                               long long Mpad, __nv_bfloat16 *X)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= Mpad) return;
+    __nv_bfloat16 *x = X + (size_t)r * MLP_K1;
+    if (r >= M) {
+        for (int c = 0; c < MLP_K1; c++) x[c] = __float2bfloat16(0.f);
+        return;
+    }
+    const long long cr = rows ? rows[r] : r;
+    const size_t q = g.cell(cr);
+    const ptrdiff_t sx = (ptrdiff_t)g.Ym() * g.Zm(), sy = g.Zm();
+    int c = 0;
+    for (int l = 0; l < 2; l++)
+        for (int v = 0; v < 5; v++) {
+            const float inv = 1.0f / scale[v];
+            const double *a = L.u[l][v], *b = L.u[l + 1][v];
+            for (int di = -1; di <= 1; di++)
+                for (int dj = -1; dj <= 1; dj++)
+                    for (int dk = -1; dk <= 1; dk++) {
+                        const size_t p = q + di * sx + dj * sy + dk;
+                        x[c++] = __float2bfloat16((float)(a[p] - b[p]) * inv);
+                    }
+        }
+    for (; c < MLP_K1; c++) x[c] = __float2bfloat16(0.f);
+}
+
+// targets of row r: the error of the quadratic extrapolation
+// U^n + 2 dU^n - dU^(n-1), i.e. U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2), over
+// scale * oscale; columns 5..15 zero.  L.u[0..2] = U^n, U^(n-1), U^(n-2),
+// next = U^(n+1)
+__global__ void k_mlp_targets(mlp_grid g, mlp_levels L, mlp_levels next, const float *scale, const float *oscale,
+                              const int *rows, long long M, long long Mpad, float *T)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= Mpad) return;
+    float *t = T + (size_t)r * MLP_N3;
+    for (int c = 0; c < MLP_N3; c++) t[c] = 0.f;
+    if (r >= M) return;
+    const size_t q = g.cell(rows ? rows[r] : r);
+    for (int v = 0; v < 5; v++) {
+        const double d3 = next.u[0][v][q] - 3.0 * L.u[0][v][q] + 3.0 * L.u[1][v][q] - L.u[2][v][q];
+        t[v] = (float)(d3 / ((double)scale[v] * (double)oscale[v]));
+    }
+}
+
+// the learned initial guess on every interior cell:
+// U_ = U^n + 2 dU^n - dU^(n-1) + scale * oscale * Y
+__global__ void k_mlp_apply(mlp_grid g, mlp_levels L, const float *scale, const float *oscale, const float *Y,
+                            long long M, double *o0, double *o1, double *o2, double *o3, double *o4)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= M) return;
+    const size_t q = g.cell(r);
+    double *o[5] = {o0, o1, o2, o3, o4};
+    const float *y = Y + (size_t)r * MLP_N3;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        const double un = L.u[0][v][q], u1 = L.u[1][v][q], u2 = L.u[2][v][q];
+        o[v][q] = un + 2.0 * (un - u1) - (u1 - u2) + (double)scale[v] * (double)oscale[v] * (double)y[v];
+    }
+}
+
+// partial sums of (U^n - U^{n-1})^2 per variable: block b of variable v
+__global__ void k_mlp_sq_partial(mlp_grid g, mlp_levels L, long long M, double *partial)
+{
+    const int v = blockIdx.y;
+    double s = 0;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x) {
+        const size_t q = g.cell(r);
+        const double d = L.u[0][v][q] - L.u[1][v][q];
+        s += d * d;
+    }
+    __shared__ double sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(size_t)v * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// dL/dY of the mean squared error over the 5 outputs of M rows: dY (bf16,
+// [Mpad x 64], columns >= 5 zero), its transpose dYT ([16 x Mpad]), and
+// per-block loss and db3 partial sums
+__global__ void k_mlp_loss_grad(const float *Y, const float *T, long long M, long long Mpad, __nv_bfloat16 *dY,
+                                __nv_bfloat16 *dYT, float *partial)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0, db[5] = {0, 0, 0, 0, 0};
+    if (r < Mpad) {
+        const float sc = 2.0f / (float)(M * MLP_OUT);
+        for (int c = 0; c < MLP_K3; c++) {
+            float gv = 0.f;
+            if (c < MLP_OUT && r < M) {
+                const float d = Y[(size_t)r * MLP_N3 + c] - T[(size_t)r * MLP_N3 + c];
+                l += d * d;
+                gv = sc * d;
+                db[c] = gv;
+            }
+            dY[(size_t)r * MLP_K3 + c] = __float2bfloat16(gv);
+            if (c < MLP_N3) dYT[(size_t)c * Mpad + r] = __float2bfloat16(gv);
+        }
+    }
+    __shared__ float sh[6][256];
+    sh[0][threadIdx.x] = l;
+    for (int c = 0; c < 5; c++) sh[1 + c][threadIdx.x] = db[c];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int n = 0; n < 6; n++) sh[n][threadIdx.x] += sh[n][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int n = 0; n < 6; n++) partial[(size_t)blockIdx.x * 6 + n] = sh[n][0];
+}
+
+// dZ = dH * SiLU'(Z), both as rows [Mpad x 128] and transposed [128 x Mpad]
+// (32 x 32 tiles through shared memory); partial column sums for the bias
+__global__ void k_mlp_silu_bwd(const float *dH, const float *Z, long long Mpad, __nv_bfloat16 *dZ,
+                               __nv_bfloat16 *dZT)
+{
+    __shared__ __nv_bfloat16 tile[32][33];
+    const long long r0 = (long long)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;      // 32 x 8
+    for (int yy = ty; yy < 32; yy += 8) {
+        const long long r = r0 + yy;
+        const int c = c0 + tx;
+        const size_t i = (size_t)r * MLP_H + c;
+        const float z = Z[i];
+        const float sgm = 1.0f / (1.0f + __expf(-z));
+        const float gz = dH[i] * (sgm * (1.0f + z * (1.0f - sgm)));
+        const __nv_bfloat16 h = __float2bfloat16(gz);
+        dZ[i] = h;
+        tile[yy][tx] = h;
+    }
+    __syncthreads();
+    for (int yy = ty; yy < 32; yy += 8) dZT[(size_t)(c0 + yy) * Mpad + r0 + tx] = tile[tx][yy];
+}
+
+// dst [cols x rows] = src [rows x cols]^T (bf16, rows multiple of 32, cols multiple of 32)
+__global__ void k_transpose_bf16(const __nv_bfloat16 *src, long long rows, int cols, __nv_bfloat16 *dst)
+{
+    __shared__ __nv_bfloat16 tile[32][33];
+    const long long r0 = (long long)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int yy = ty; yy < 32; yy += 8) tile[yy][tx] = src[(size_t)(r0 + yy) * cols + c0 + tx];
+    __syncthreads();
+    for (int yy = ty; yy < 32; yy += 8) dst[(size_t)(c0 + yy) * rows + r0 + tx] = tile[tx][yy];
+}
+
+// column sums of a bf16 [rows x cols] matrix into out[cols] (fp32); one block per column
+__global__ void k_colsum_bf16(const __nv_bfloat16 *src, long long rows, int cols, float *out)
+{
+    const int c = blockIdx.x;
+    float s = 0;
+    for (long long r = threadIdx.x; r < rows; r += blockDim.x) s += __bfloat162float(src[(size_t)r * cols + c]);
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = sh[0];
+}
+
+// Adam step on n parameters (bias-corrected)
+__global__ void k_adam(float *p, const float *gr, float *m, float *v, long long n, float lr, float b1, float b2,
+                       float eps, float c1, float c2)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float g = gr[t];
+    const float mm = b1 * m[t] + (1 - b1) * g;
+    const float vv = b2 * v[t] + (1 - b2) * g * g;
+    m[t] = mm;
+    v[t] = vv;
+    p[t] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+}
+
+// fp32 parameters -> the BF16 operand layouts of the forward and backward GEMMs:
+// W1b [128 x 320], W2b [128 x 128], W3b [16 x 128] = W3T^T, W2T [128 x 128] = W2^T,
+// W3p [128 x 64] with W3p[h][o] = W3T[h][o] (o < 16), zero beyond
+__global__ void k_mlp_pack(const float *W1, const float *W2, const float *W3T, __nv_bfloat16 *W1b,
+                           __nv_bfloat16 *W2b, __nv_bfloat16 *W3b, __nv_bfloat16 *W2T, __nv_bfloat16 *W3p)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < MLP_H * MLP_K1) W1b[t] = __float2bfloat16(W1[t]);
+    if (t < MLP_H * MLP_H) {
+        const int a = t / MLP_H, b = t % MLP_H;
+        W2b[t] = __float2bfloat16(W2[t]);
+        W2T[(size_t)b * MLP_H + a] = __float2bfloat16(W2[t]);
+    }
+    if (t < MLP_N3 * MLP_H) {
+        const int o = t / MLP_H, h = t % MLP_H;
+        W3b[t] = __float2bfloat16(W3T[(size_t)h * MLP_N3 + o]);
+    }
+    if (t < MLP_H * MLP_K3) {
+        const int h = t / MLP_K3, o = t % MLP_K3;
+        W3p[t] = __float2bfloat16(o < MLP_N3 ? W3T[(size_t)h * MLP_N3 + o] : 0.f);
+    }
+}
+
 }  // namespace cf_mlp
 
 using namespace cf_mlp;
@@ -299,6 +534,132 @@ int cf_gemm_bf16(void *stream, const void *A, const void *B, int M, int N, int K
     default: r = launch_gemm<16>(ta, tb, M, N, K, e, err_dev, s); break;
     }
     return r == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+static mlp_levels levels(const double *const *u15)
+{
+    mlp_levels L;
+    for (int l = 0; l < 3; l++)
+        for (int v = 0; v < 5; v++) L.u[l][v] = u15 ? u15[5 * l + v] : nullptr;
+    return L;
+}
+
+static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// features [Mpad x 320] bf16 of M interior rows (rows = NULL: all cells in order)
+int cf_mlp_features(void *stream, int X, int Y, int Z, const double *const *levels15, const float *scale,
+                    const int *rows, long long M, long long Mpad, void *Xout)
+{
+    if (!levels15 || !scale || !Xout || M <= 0 || Mpad < M || Mpad % 128) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    k_mlp_features<<<nblk(Mpad, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        g, levels(levels15), scale, rows, M, Mpad, static_cast<__nv_bfloat16 *>(Xout));
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+// targets [Mpad x 16] fp32: levels20 = U^(n+1), U^n, U^(n-1), U^(n-2)
+int cf_mlp_targets(void *stream, int X, int Y, int Z, const double *const *levels20, const float *scale,
+                   const float *oscale, const int *rows, long long M, long long Mpad, float *T)
+{
+    if (!levels20 || !scale || !oscale || !T || M <= 0 || Mpad < M || Mpad % 128) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    mlp_levels next{}, L{};
+    for (int v = 0; v < 5; v++) next.u[0][v] = levels20[v];
+    for (int l = 0; l < 3; l++)
+        for (int v = 0; v < 5; v++) L.u[l][v] = levels20[5 * (l + 1) + v];
+    k_mlp_targets<<<nblk(Mpad, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(g, L, next, scale, oscale, rows,
+                                                                                   M, Mpad, T);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+// U_ (out5) = U^n + 2 dU^n - dU^(n-1) + scale * oscale * Y on all interior
+// cells; levels15 = U^n, U^(n-1), U^(n-2)
+int cf_mlp_apply(void *stream, int X, int Y, int Z, const double *const *levels15, const float *scale,
+                 const float *oscale, const float *Yp, double *const *out5)
+{
+    if (!levels15 || !scale || !oscale || !Yp || !out5) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    const long long M = (long long)X * Y * Z;
+    k_mlp_apply<<<nblk(M, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        g, levels(levels15), scale, oscale, Yp, M, out5[0], out5[1], out5[2], out5[3], out5[4]);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+// RMS of U^n - U^{n-1} per variable over the interior (FP64 sums); rms5 host output
+int cf_mlp_rms(void *stream, int X, int Y, int Z, const double *const *levels10, double *partial_dev,
+               int nblocks, double *rms5)
+{
+    if (!levels10 || !partial_dev || !rms5 || nblocks <= 0) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    mlp_levels L{};
+    for (int l = 0; l < 2; l++)
+        for (int v = 0; v < 5; v++) L.u[l][v] = levels10[5 * l + v];
+    const long long M = (long long)X * Y * Z;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    k_mlp_sq_partial<<<dim3((unsigned)nblocks, 5), 256, 0, s>>>(g, L, M, partial_dev);
+    std::vector<double> h((size_t)5 * nblocks);
+    if (cudaMemcpyAsync(h.data(), partial_dev, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return CF_ERR_CUDA;
+    for (int v = 0; v < 5; v++) {
+        double t = 0;
+        for (int b = 0; b < nblocks; b++) t += h[(size_t)v * nblocks + b];
+        rms5[v] = std::sqrt(t / (double)M);
+    }
+    return CF_OK;
+}
+
+int cf_mlp_loss_grad(void *stream, const float *Yv, const float *T, long long M, long long Mpad, void *dY, void *dYT,
+                     float *partial)
+{
+    if (!Yv || !T || !dY || !dYT || !partial || Mpad % 256) return CF_ERR_ARG;
+    k_mlp_loss_grad<<<nblk(Mpad, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        Yv, T, M, Mpad, static_cast<__nv_bfloat16 *>(dY), static_cast<__nv_bfloat16 *>(dYT), partial);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_mlp_silu_bwd(void *stream, const float *dH, const float *Zv, long long Mpad, void *dZ, void *dZT)
+{
+    if (!dH || !Zv || !dZ || !dZT || Mpad % 32) return CF_ERR_ARG;
+    k_mlp_silu_bwd<<<dim3((unsigned)(Mpad / 32), MLP_H / 32), dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
+        dH, Zv, Mpad, static_cast<__nv_bfloat16 *>(dZ), static_cast<__nv_bfloat16 *>(dZT));
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_transpose_bf16(void *stream, const void *src, long long rows, int cols, void *dst)
+{
+    if (!src || !dst || rows % 32 || cols % 32) return CF_ERR_ARG;
+    k_transpose_bf16<<<dim3((unsigned)(rows / 32), (unsigned)(cols / 32)), dim3(32, 8), 0,
+                       static_cast<cudaStream_t>(stream)>>>(static_cast<const __nv_bfloat16 *>(src), rows, cols,
+                                                            static_cast<__nv_bfloat16 *>(dst));
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_colsum_bf16(void *stream, const void *src, long long rows, int cols, float *out)
+{
+    if (!src || !out) return CF_ERR_ARG;
+    k_colsum_bf16<<<(unsigned)cols, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(src), rows, cols, out);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_adam(void *stream, float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2,
+            float eps, int t)
+{
+    if (!p || !g || !m || !v || n <= 0 || t < 1) return CF_ERR_ARG;
+    const float c1 = 1.f - std::pow(b1, (float)t), c2 = 1.f - std::pow(b2, (float)t);
+    k_adam<<<nblk(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(p, g, m, v, n, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_mlp_pack(void *stream, const float *W1, const float *W2, const float *W3, void *W1b, void *W2b, void *W3b,
+                void *W2T, void *W3p)
+{
+    if (!W1 || !W2 || !W3 || !W1b || !W2b || !W3b || !W2T || !W3p) return CF_ERR_ARG;
+    k_mlp_pack<<<nblk(MLP_H * MLP_K1, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        W1, W2, W3, static_cast<__nv_bfloat16 *>(W1b), static_cast<__nv_bfloat16 *>(W2b),
+        static_cast<__nv_bfloat16 *>(W3b), static_cast<__nv_bfloat16 *>(W2T), static_cast<__nv_bfloat16 *>(W3p));
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
 }  // extern "C"

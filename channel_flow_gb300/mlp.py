@@ -1,0 +1,266 @@
+"""Learned initial guess of the pseudo-time iterations.
+
+A per-cell MLP maps the 3x3x3 neighbourhood of the last two time
+increments, dU^n = U^n - U^(n-1) and dU^(n-1) = U^(n-1) - U^(n-2), of the
+five conserved variables (2 x 27 x 5 = 270 features, scaled per variable by
+the RMS of dU^n) through two hidden layers of 128 SiLU units to the five
+components of the error of the quadratic extrapolation U^n + 2 dU^n -
+dU^(n-1) of U^(n+1) (scaled by RMS(dU^n) times a per-variable factor fixed
+from the training data).  The network corrects the extrapolation rather than
+predicting the increment itself, so its BF16 precision limits only the
+small correction.  Before the sub-iterations of a physical step the state
+starts from that guess instead of U^n; the sub-iterations still run to the
+same residual tolerance, so the plain LU-SGS loop remains the judge and the
+fallback.
+
+Every matrix product runs on the tcgen05 tensor cores (``cf_gemm_bf16``,
+BF16 operands, FP32 accumulation) and every other step in the package's own
+kernels (``cf_mlp_*``); PyTorch only holds the device buffers.  Training is
+Adam on the mean squared error over snapshots harvested from the solver's
+own steps.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+IN, K1, H, OUT, N3, K3 = 270, 320, 128, 5, 16, 64
+EPI_F32, EPI_SILU, EPI_BIAS = 0, 1, 2
+
+# flat parameter vector: W1 [128 x 320], b1 [128], W2 [128 x 128], b2 [128],
+# W3T [128 x 16] (the transposed output layer), b3 [16]
+_SHAPES = [("W1", (H, K1)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3T", (H, N3)), ("b3", (N3,))]
+
+
+def _offsets():
+    off, out = 0, {}
+    for n, s in _SHAPES:
+        size = int(np.prod(s))
+        out[n] = (off, s)
+        off += size
+    return out, off
+
+
+OFFS, NPARAM = _offsets()
+
+
+def init_params(seed: int = 0) -> np.ndarray:
+    """Seeded initial parameters (scaled normal weights, zero biases; the
+    padded feature columns and output rows are zero)."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(NPARAM, np.float32)
+
+    def put(name, val):
+        o, s = OFFS[name]
+        p[o:o + int(np.prod(s))] = val.astype(np.float32).ravel()
+    W1 = np.zeros((H, K1))
+    W1[:, :IN] = rng.normal(0, np.sqrt(1.0 / IN), (H, IN))
+    put("W1", W1)
+    put("W2", rng.normal(0, np.sqrt(1.0 / H), (H, H)))
+    W3T = np.zeros((H, N3))
+    W3T[:, :OUT] = rng.normal(0, 0.1 * np.sqrt(1.0 / H), (H, OUT))
+    put("W3T", W3T)
+    return p
+
+
+def _pad(m: int) -> int:
+    return (m + 255) // 256 * 256
+
+
+class LearnedGuess:
+    """The MLP on one device; ``capacity`` rows per forward/training call."""
+
+    def __init__(self, capacity: int = 32768, seed: int = 0, lr: float = 1e-3):
+        import torch
+        self.torch = torch
+        self.lib = _lib.load()
+        self.cap = _pad(capacity)
+        dev = "cuda"
+        f32, bf = torch.float32, torch.bfloat16
+        self.p = torch.from_numpy(init_params(seed)).to(dev)
+        self.g = torch.zeros(NPARAM, dtype=f32, device=dev)
+        self.m = torch.zeros(NPARAM, dtype=f32, device=dev)
+        self.v = torch.zeros(NPARAM, dtype=f32, device=dev)
+        self.t = 0
+        self.lr = lr
+        self.W1b = torch.zeros(H, K1, dtype=bf, device=dev)
+        self.W2b = torch.zeros(H, H, dtype=bf, device=dev)
+        self.W3b = torch.zeros(N3, H, dtype=bf, device=dev)
+        self.W2T = torch.zeros(H, H, dtype=bf, device=dev)
+        self.W3p = torch.zeros(H, K3, dtype=bf, device=dev)
+        M = self.cap
+        self.X = torch.zeros(M, K1, dtype=bf, device=dev)
+        self.H1 = torch.zeros(M, H, dtype=bf, device=dev)
+        self.H2 = torch.zeros(M, H, dtype=bf, device=dev)
+        self.Z1 = torch.zeros(M, H, dtype=f32, device=dev)
+        self.Z2 = torch.zeros(M, H, dtype=f32, device=dev)
+        self.Y = torch.zeros(M, N3, dtype=f32, device=dev)
+        self.T = torch.zeros(M, N3, dtype=f32, device=dev)
+        self.dY = torch.zeros(M, K3, dtype=bf, device=dev)
+        self.dYT = torch.zeros(N3, M, dtype=bf, device=dev)
+        self.dH = torch.zeros(M, H, dtype=f32, device=dev)
+        self.dZ2 = torch.zeros(M, H, dtype=bf, device=dev)
+        self.dZ2T = torch.zeros(H, M, dtype=bf, device=dev)
+        self.dZ1 = torch.zeros(M, H, dtype=bf, device=dev)
+        self.dZ1T = torch.zeros(H, M, dtype=bf, device=dev)
+        self.H1T = torch.zeros(H, M, dtype=bf, device=dev)
+        self.H2T = torch.zeros(H, M, dtype=bf, device=dev)
+        self.XT = torch.zeros(K1, M, dtype=bf, device=dev)
+        self.partial = torch.zeros(M // 256 * 6, dtype=f32, device=dev)
+        self.rms_partial = torch.zeros(5 * 512, dtype=torch.float64, device=dev)
+        self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.scale = torch.ones(5, dtype=f32, device=dev)
+        self.oscale = torch.ones(5, dtype=f32, device=dev)
+        self.pack()
+
+    # -- helpers ----------------------------------------------------------
+    def _s(self):
+        return self.torch.cuda.current_stream().cuda_stream
+
+    def _ok(self, rc, what):
+        if rc != _lib.CF_OK:
+            raise RuntimeError(f"{what} failed with status {rc}")
+
+    def view(self, name, t=None):
+        o, s = OFFS[name]
+        t = self.p if t is None else t
+        return t[o:o + int(np.prod(s))].view(*s)
+
+    def pack(self):
+        """fp32 parameters -> BF16 GEMM operands."""
+        self._ok(self.lib.cf_mlp_pack(self._s(), self.view("W1").data_ptr(), self.view("W2").data_ptr(),
+                                      self.view("W3T").data_ptr(), self.W1b.data_ptr(), self.W2b.data_ptr(),
+                                      self.W3b.data_ptr(), self.W2T.data_ptr(), self.W3p.data_ptr()),
+                 "cf_mlp_pack")
+
+    def gemm(self, A, B, M, N, K, epi, bias, out, zout, ldo):
+        rc = self.lib.cf_gemm_bf16(self._s(), A.data_ptr(), B.data_ptr(), M, N, K, epi,
+                                   None if bias is None else bias.data_ptr(), out.data_ptr(),
+                                   None if zout is None else zout.data_ptr(), ldo, self.err.data_ptr())
+        self._ok(rc, "cf_gemm_bf16")
+
+    def check_device(self):
+        if int(self.err.item()):
+            raise RuntimeError("a tensor-core GEMM wait ran out on the device")
+
+    # -- network ----------------------------------------------------------
+    def forward(self, Mpad: int):
+        """Y = MLP(X[:Mpad]) with the hidden pre-activations kept."""
+        b1, b2, b3 = self.view("b1"), self.view("b2"), self.view("b3")
+        self.gemm(self.X, self.W1b, Mpad, H, K1, EPI_SILU, b1, self.H1, self.Z1, H)
+        self.gemm(self.H1, self.W2b, Mpad, H, H, EPI_SILU, b2, self.H2, self.Z2, H)
+        self.gemm(self.H2, self.W3b, Mpad, N3, H, EPI_BIAS, b3, self.Y, None, N3)
+
+    def backward(self, M: int, Mpad: int):
+        """Gradients of the mean squared error over the first M rows into self.g."""
+        s = self._s()
+        self._ok(self.lib.cf_mlp_loss_grad(s, self.Y.data_ptr(), self.T.data_ptr(), M, Mpad, self.dY.data_ptr(),
+                                           self.dYT.data_ptr(), self.partial.data_ptr()), "cf_mlp_loss_grad")
+        # activation gradients
+        self.gemm(self.dY, self.W3p, Mpad, H, K3, EPI_F32, None, self.dH, None, H)
+        self._ok(self.lib.cf_mlp_silu_bwd(s, self.dH.data_ptr(), self.Z2.data_ptr(), Mpad, self.dZ2.data_ptr(),
+                                          self.dZ2T.data_ptr()), "cf_mlp_silu_bwd")
+        self.gemm(self.dZ2, self.W2T, Mpad, H, H, EPI_F32, None, self.dH, None, H)
+        self._ok(self.lib.cf_mlp_silu_bwd(s, self.dH.data_ptr(), self.Z1.data_ptr(), Mpad, self.dZ1.data_ptr(),
+                                          self.dZ1T.data_ptr()), "cf_mlp_silu_bwd")
+        # weight gradients: reductions over the rows as K of the GEMM
+        for src, dst, cols in ((self.H2, self.H2T, H), (self.H1, self.H1T, H), (self.X, self.XT, K1)):
+            self._ok(self.lib.cf_transpose_bf16(s, src.data_ptr(), Mpad, cols, dst.data_ptr()), "cf_transpose_bf16")
+        self.gemm(self.H2T, self.dYT, H, N3, Mpad, EPI_F32, None, self.view("W3T", self.g), None, N3)
+        self.gemm(self.dZ2T, self.H1T, H, H, Mpad, EPI_F32, None, self.view("W2", self.g), None, H)
+        self.gemm(self.dZ1T, self.XT, H, K1, Mpad, EPI_F32, None, self.view("W1", self.g), None, K1)
+        for src, name, cols in ((self.dZ1, "b1", H), (self.dZ2, "b2", H)):
+            self._ok(self.lib.cf_colsum_bf16(s, src.data_ptr(), Mpad, cols, self.view(name, self.g).data_ptr()),
+                     "cf_colsum_bf16")
+        db3 = self.torch.zeros(K3, dtype=self.torch.float32, device="cuda")
+        self._ok(self.lib.cf_colsum_bf16(s, self.dY.data_ptr(), Mpad, K3, db3.data_ptr()), "cf_colsum_bf16")
+        self.view("b3", self.g).copy_(db3[:N3])
+
+    def loss(self, Mpad: int) -> float:
+        part = self.partial[: (Mpad // 256) * 6].view(-1, 6)
+        return float(part[:, 0].sum().item())
+
+    def step(self, M: int, Mpad: int) -> float:
+        """One Adam step on the rows loaded in X / T; returns the loss."""
+        self.forward(Mpad)
+        self.backward(M, Mpad)
+        self.t += 1
+        self._ok(self.lib.cf_adam(self._s(), self.p.data_ptr(), self.g.data_ptr(), self.m.data_ptr(),
+                                  self.v.data_ptr(), NPARAM, self.lr, 0.9, 0.999, 1e-8, self.t), "cf_adam")
+        self.pack()
+        return self.loss(Mpad) / (M * OUT)
+
+    # -- data ---------------------------------------------------------------
+    def set_scale(self, grid, Un, Unm1):
+        """Per-variable scaling: RMS of U^n - U^(n-1) over the interior."""
+        rms = np.zeros(5)
+        arr = (C.c_void_p * 10)(*[t.data_ptr() for t in list(Un) + list(Unm1)])
+        self._ok(self.lib.cf_mlp_rms(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
+                                     self.rms_partial.data_ptr(), 512, rms.ctypes.data), "cf_mlp_rms")
+        rms = np.where(rms > 0, rms, 1.0)
+        self.scale.copy_(self.torch.from_numpy(rms.astype(np.float32)))
+        return rms
+
+    def load_features(self, grid, Un, Unm1, Unm2, rows=None, M=None):
+        M = grid.cells if rows is None else len(rows)
+        Mpad = _pad(M)
+        if Mpad > self.cap:
+            raise ValueError(f"{M} rows exceed the capacity {self.cap}")
+        arr = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
+        self._ok(self.lib.cf_mlp_features(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
+                                          self.scale.data_ptr(), None if rows is None else rows.data_ptr(),
+                                          M, Mpad, self.X.data_ptr()), "cf_mlp_features")
+        return M, Mpad
+
+    def load_targets(self, grid, Unp1, Un, Unm1, Unm2, rows=None):
+        M = grid.cells if rows is None else len(rows)
+        Mpad = _pad(M)
+        arr = (C.c_void_p * 20)(*[t.data_ptr() for t in list(Unp1) + list(Un) + list(Unm1) + list(Unm2)])
+        self._ok(self.lib.cf_mlp_targets(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr, self.scale.data_ptr(),
+                                         self.oscale.data_ptr(), None if rows is None else rows.data_ptr(), M, Mpad,
+                                         self.T.data_ptr()), "cf_mlp_targets")
+        return M, Mpad
+
+    def fit_output_scale(self, grid, history):
+        """Per-variable output factor: RMS of the extrapolation error over
+        RMS(dU^n), averaged over a history [U^0, U^1, ...] of FP64 states."""
+        r = []
+        for n in range(2, len(history) - 1):
+            s = self.set_scale(grid, history[n], history[n - 1])
+            err = [history[n + 1][v] - 3 * history[n][v] + 3 * history[n - 1][v] - history[n - 2][v]
+                   for v in range(5)]
+            e = np.asarray([float(x[3:grid.gend + 1, 2:grid.ny + 1, 2:grid.nz + 1].pow(2).mean().sqrt())
+                            for x in err])
+            r.append(e / s)
+        f = np.mean(r, axis=0) if r else np.ones(5)
+        f = np.where(f > 0, f, 1.0)
+        self.oscale.copy_(self.torch.from_numpy(f.astype(np.float32)))
+        return f
+
+    def train(self, grid, history, epochs: int = 20):
+        """Adam on every (U^(n-2), U^(n-1), U^n) -> U^(n+1) window of a
+        history of FP64 states (each window one batch of all cells)."""
+        self.fit_output_scale(grid, history)
+        losses = []
+        for _ in range(epochs):
+            for n in range(2, len(history) - 1):
+                self.set_scale(grid, history[n], history[n - 1])
+                M, Mpad = self.load_features(grid, history[n], history[n - 1], history[n - 2])
+                self.load_targets(grid, history[n + 1], history[n], history[n - 1], history[n - 2])
+                losses.append(self.step(M, Mpad))
+        self.check_device()
+        return losses
+
+    def guess(self, grid, Un, Unm1, Unm2, out):
+        """out (U_) = U^n + 2 dU^n - dU^(n-1) + the network's correction on
+        every interior cell; the grid's cells must fit the capacity."""
+        self.set_scale(grid, Un, Unm1)
+        M, Mpad = self.load_features(grid, Un, Unm1, Unm2)
+        self.forward(Mpad)
+        a = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
+        o = (C.c_void_p * 5)(*[t.data_ptr() for t in out])
+        self._ok(self.lib.cf_mlp_apply(self._s(), grid.X_out, grid.Y_out, grid.Z_out, a, self.scale.data_ptr(),
+                                       self.oscale.data_ptr(), self.Y.data_ptr(), o), "cf_mlp_apply")

@@ -1,0 +1,57 @@
+"""Physical time steps with an initial guess for the pseudo-time iterations.
+
+``Stepper`` drives ``Context.step`` (the C-ABI ``cf_step``: sub-iterations
+of the dual-time LU-SGS to a residual tolerance) and keeps the last three
+time levels U^n, U^(n-1), U^(n-2) on the device, so that each step can start
+its sub-iterations from
+
+* ``None``: U^n (the reference's start, main.cpp:443-462),
+* ``"extrapolate"``: the quadratic extrapolation U^n + 2 dU^n - dU^(n-1),
+* a trained ``mlp.LearnedGuess``: that extrapolation corrected by the
+  network.
+
+The tolerance and the iteration loop are the same in every case; only the
+starting point differs.
+"""
+from __future__ import annotations
+
+from collections import deque
+
+
+class Stepper:
+    def __init__(self, ctx, fields: dict, **step_kw):
+        self.ctx = ctx
+        self.f = fields
+        self.kw = step_kw
+        self.n = 0
+        self.hist = deque(maxlen=3)
+        self.hist.append([u.clone() for u in fields["U"]])
+
+    def step(self, guess=None):
+        """One physical step; returns (sub-iterations, er[5], Q)."""
+        if guess is not None and len(self.hist) == 3:
+            un, u1, u2 = self.hist[2], self.hist[1], self.hist[0]
+            if isinstance(guess, str):
+                if guess != "extrapolate":
+                    raise ValueError(f"unknown guess {guess!r}")
+                for v in range(5):
+                    self.f["U_"][v].copy_(3 * un[v] - 3 * u1[v] + u2[v])
+            else:
+                guess.guess(self.ctx.grid, un, u1, u2, self.f["U_"])
+        self.n += 1
+        it, er, q = self.ctx.step(self.f, step=self.n, **self.kw)
+        self.hist.append([u.clone() for u in self.f["U"]])
+        return it, er, q
+
+    def history(self):
+        return list(self.hist)
+
+
+def fields_from_workload(w, torch, grid):
+    """cf_fields of a bench.DeviceWorkload-like object (state U = U_ = Uq)."""
+    z = lambda: torch.zeros(grid.shape, dtype=torch.float64, device="cuda")
+    return {"U_": w.U, "U": [u.clone() for u in w.U], "Uq": [u.clone() for u in w.U], "J": w.J, "Y_point": w.Yp,
+            "cell_metric": w.cm, "face_J": [w.fu[0], w.fv[0], w.fw[0]],
+            "face_metric": [w.fu[1:], w.fv[1:], w.fw[1:]], "Ep": w.Ep, "inF": [w.Fx, w.Fy, w.Fz], "vF": w.vF,
+            "LL": w.LL, "ML": w.ML, "MR": [z() for _ in range(5)], "NR": [z() for _ in range(5)],
+            "NL": [z() for _ in range(5)], "Residual": [z() for _ in range(5)]}

@@ -312,6 +312,37 @@ int cf_step_reset(cf_ctx *ctx);
 int cf_gemm_bf16(void *cuda_stream, const void *A, const void *B, int M, int N, int K, int epilogue,
                  const float *bias, void *out, float *zout, int ldo, int *err_dev);
 
+
+/* The per-cell MLP of the learned initial guess (270 -> 128 -> 128 -> 5,
+ * SiLU; training by Adam).  Grids are given by their interior extents; a
+ * row r is interior cell (i, j, k) = (3 + r / (Y*Z), 2 + (r / Z) % Y,
+ * 2 + r % Z), or rows[r] of that numbering when rows is not NULL; Mpad
+ * (multiple of 128) rows are written, rows >= M zero.  Fields are FP64
+ * device arrays in the reference layout; levels arrays list U^n,
+ * U^(n-1)[, U^(n-2)] (five fields each). */
+int cf_mlp_features(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale5,
+                    const int *rows, long long M, long long Mpad, void *X_bf16_Mpad_x_320);
+/* targets: the error of the quadratic extrapolation, U^(n+1) - 3 U^n +
+ * 3 U^(n-1) - U^(n-2), over scale5 * oscale5 (levels20 = U^(n+1), U^n,
+ * U^(n-1), U^(n-2)) */
+int cf_mlp_targets(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, const float *scale5,
+                   const float *oscale5, const int *rows, long long M, long long Mpad, float *T_Mpad_x_16);
+/* the guess: out = U^n + 2 dU^n - dU^(n-1) + scale5 * oscale5 * Y (levels15 = U^n, U^(n-1), U^(n-2)) */
+int cf_mlp_apply(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale5,
+                 const float *oscale5, const float *Y_M_x_16, double *const *out5);
+int cf_mlp_rms(void *cuda_stream, int X, int Y, int Z, const double *const *levels10, double *partial_dev,
+               int nblocks, double *rms5_host);
+int cf_mlp_loss_grad(void *cuda_stream, const float *Y, const float *T, long long M, long long Mpad,
+                     void *dY_bf16_Mpad_x_64, void *dYT_bf16_16_x_Mpad, float *partial);
+int cf_mlp_silu_bwd(void *cuda_stream, const float *dH, const float *Z, long long Mpad, void *dZ_bf16,
+                    void *dZT_bf16);
+int cf_transpose_bf16(void *cuda_stream, const void *src, long long rows, int cols, void *dst);
+int cf_colsum_bf16(void *cuda_stream, const void *src, long long rows, int cols, float *out);
+int cf_adam(void *cuda_stream, float *param, const float *grad, float *m, float *v, long long n, float lr,
+            float beta1, float beta2, float eps, int step);
+int cf_mlp_pack(void *cuda_stream, const float *W1, const float *W2, const float *W3T, void *W1b, void *W2b,
+                void *W3b, void *W2T, void *W3p);
+
 #ifdef __cplusplus
 }
 #endif
