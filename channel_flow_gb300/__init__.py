@@ -159,6 +159,21 @@ class Context:
     def step_reset(self):
         self._ok(self.lib.cf_step_reset(self.h))
 
+    def step_scale(self, E=None) -> np.ndarray:
+        """The running residual maxima E1..E5; with ``E`` given, set them."""
+        e = np.zeros(5) if E is None else np.ascontiguousarray(E, dtype=np.float64).copy()
+        self._ok(self.lib.cf_step_scale(self.h, e.ctypes.data, 0 if E is None else 1))
+        return e
+
+    def step_residuals(self) -> np.ndarray:
+        """[iterations x 5] normalised er1..er5 of the last step's iterations."""
+        n = C.c_int(0)
+        self._ok(self.lib.cf_step_residuals(self.h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 5))
+        if n.value:
+            self._ok(self.lib.cf_step_residuals(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
     def set_precision(self, precision: str):
         self._ok(self.lib.cf_set_precision(self.h, _lib.PREC[precision]))
         self.precision = precision

@@ -98,11 +98,15 @@ _SIGS = {
     "cf_Initial_condition": ([P, C.c_int] + [P] * 16, C.c_int),
     "cf_step": ([P, P, C.c_int, P, P, P, P], C.c_int),
     "cf_step_reset": ([P], C.c_int),
+    "cf_step_scale": ([P, P, C.c_int], C.c_int),
+    "cf_step_residuals": ([P, P, C.c_int, P], C.c_int),
     "cf_gemm_bf16": ([P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P], C.c_int),
     "cf_mlp_features": ([P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
     "cf_mlp_targets": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
     "cf_mlp_apply": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P], C.c_int),
+    "cf_mlp_dot": ([P, P, P, C.c_longlong, P, C.c_int, P], C.c_int),
     "cf_mlp_rms": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),
+    "cf_mlp_rms3": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),
     "cf_mlp_loss_grad": ([P, P, P, C.c_longlong, C.c_longlong, P, P, P], C.c_int),
     "cf_mlp_silu_bwd": ([P, P, P, C.c_longlong, P, P], C.c_int),
     "cf_transpose_bf16": ([P, P, C.c_longlong, C.c_int, P], C.c_int),

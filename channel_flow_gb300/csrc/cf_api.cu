@@ -27,6 +27,7 @@ struct cf_ctx {
     double *stat_acc = nullptr;       // Statistic accumulators, 17 rows of Y_m (device)
     double sxy_bottom = 0, sxy_up = 0;
     double E[5] = {0, 0, 0, 0, 0};    // running maxima of the residual norms (main.cpp:63, 387-391)
+    std::vector<double> er_hist;      // normalised er1..er5 of every iteration of the last cf_step
     std::unordered_map<const double *, double *> mirrors;
     std::unordered_map<std::string, std::pair<double *, size_t>> scratch;
     std::vector<int> nijk;            // plane tables, Hyperplane layout (host)
@@ -1038,6 +1039,30 @@ int cf_step_reset(cf_ctx *c)
     return CF_OK;
 }
 
+int cf_step_scale(cf_ctx *c, double *E, int set)
+{
+    if (!c || !E) return CF_ERR_ARG;
+    for (int n = 0; n < 5; n++) {
+        if (set) {
+            if (!(E[n] >= 0)) return fail(c, CF_ERR_ARG, "cf_step_scale: E[%d] must be >= 0", n);
+            c->E[n] = E[n];
+        } else {
+            E[n] = c->E[n];
+        }
+    }
+    return CF_OK;
+}
+
+int cf_step_residuals(cf_ctx *c, double *out, int cap, int *count)
+{
+    if (!c || !count || (cap > 0 && !out)) return CF_ERR_ARG;
+    const int n = (int)(c->er_hist.size() / 5);
+    *count = n;
+    const int m = std::min(n, std::max(cap, 0));
+    for (int t = 0; t < 5 * m; t++) out[t] = c->er_hist[t];
+    return CF_OK;
+}
+
 int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, int *iterations, double *er_out,
             double *Q)
 {
@@ -1075,6 +1100,7 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
     for (int n = 0; n < 9; n++) dts[16 + n] = f->cell_metric[n];
     for (int n = 0; n < 4; n++) dts[40 + n] = f->vF[n];
     double er[5] = {0, 0, 0, 0, 0};
+    c->er_hist.clear();
     int it = 1;
     for (;; it++) {
         if (int rc = cf_X_periodic(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4])) return rc;
@@ -1103,6 +1129,7 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         for (int n = 0; n < 5; n++) {
             c->E[n] = std::max(c->E[n], er[n]);
             er[n] = er[n] / c->E[n];
+            c->er_hist.push_back(er[n]);
         }
         const double tol = pp->tolerance;
         if ((er[0] < tol && er[1] < tol && er[2] < tol && er[3] < tol) || it >= pp->max_iterations) break;

@@ -163,7 +163,11 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     T Rk[5];
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        T Rp = -(T(3) * T(a.U_[n][q]) - T(4) * T(a.U[n][q]) + T(a.Uq[n][q])) / (T(2) * deltaT);
+        // the BDF2 time term combines three nearly equal FP64 states: it is
+        // formed in FP64 in every build (the same operations as the
+        // reference's expression when T is double) and only then rounded,
+        // so an FP32 build keeps the digits that the difference resolves
+        T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) / (2.0 * dt));
         T Rf = -((T(a.Fx[n][fx]) - T(a.Fx[n][f0])) / dXI + (T(a.Fy[n][fy]) - T(a.Fy[n][f0])) / dET +
                  (T(a.Fz[n][fz]) - T(a.Fz[n][f0])) / dZT);
         Rk[n] = Rp + Rf;

@@ -291,40 +291,48 @@ struct mlp_levels {
     const double *u[3][5];  // U^n, U^{n-1}, U^{n-2}
 };
 
-// features of row r: for level l (0: U^n - U^{n-1}, 1: U^{n-1} - U^{n-2}),
-// variable v and neighbour s of the 3x3x3 stencil, the scaled difference;
-// columns 270..319 are zero
+// features of row r: for kind l (0: the first time difference
+// U^n - U^(n-1), over scale[v]; 1: the second difference U^n - 2 U^(n-1) +
+// U^(n-2), over scale[5 + v]), variable v and neighbour s of the 3x3x3
+// stencil (s = 9 (di+1) + 3 (dj+1) + (dk+1)), column 135 l + 27 v + s;
+// columns 270..319 are zero.  The second difference is formed in FP64
+// before the BF16 rounding, so the features resolve it at BF16 precision
+// relative to its own size.  One thread writes 8 columns (16 bytes).
 __global__ void k_mlp_features(mlp_grid g, mlp_levels L, const float *scale, const int *rows, long long M,
                                long long Mpad, __nv_bfloat16 *X)
 {
-    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr int CH = MLP_K1 / 8;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r = t / CH;
+    const int ch = (int)(t % CH);
     if (r >= Mpad) return;
-    __nv_bfloat16 *x = X + (size_t)r * MLP_K1;
-    if (r >= M) {
-        for (int c = 0; c < MLP_K1; c++) x[c] = __float2bfloat16(0.f);
-        return;
-    }
-    const long long cr = rows ? rows[r] : r;
-    const size_t q = g.cell(cr);
-    const ptrdiff_t sx = (ptrdiff_t)g.Ym() * g.Zm(), sy = g.Zm();
-    int c = 0;
-    for (int l = 0; l < 2; l++)
-        for (int v = 0; v < 5; v++) {
-            const float inv = 1.0f / scale[v];
-            const double *a = L.u[l][v], *b = L.u[l + 1][v];
-            for (int di = -1; di <= 1; di++)
-                for (int dj = -1; dj <= 1; dj++)
-                    for (int dk = -1; dk <= 1; dk++) {
-                        const size_t p = q + di * sx + dj * sy + dk;
-                        x[c++] = __float2bfloat16((float)(a[p] - b[p]) * inv);
-                    }
+    __align__(16) __nv_bfloat16 h[8];
+    if (r >= M || ch * 8 >= MLP_IN) {
+#pragma unroll
+        for (int e = 0; e < 8; e++) h[e] = __float2bfloat16(0.f);
+    } else {
+        const size_t q = g.cell(rows ? rows[r] : r);
+        const ptrdiff_t sx = (ptrdiff_t)g.Ym() * g.Zm(), sy = g.Zm();
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int c = ch * 8 + e;
+            float f = 0.f;
+            if (c < MLP_IN) {
+                const int l = c / 135, rem = c % 135, v = rem / 27, st = rem % 27;
+                const ptrdiff_t p = (ptrdiff_t)q + (st / 9 - 1) * sx + ((st / 3) % 3 - 1) * sy + (st % 3 - 1);
+                const double a0 = L.u[0][v][p], a1 = L.u[1][v][p];
+                const double d = l == 0 ? a0 - a1 : (a0 - 2.0 * a1) + L.u[2][v][p];
+                f = (float)d * (1.0f / scale[5 * l + v]);
+            }
+            h[e] = __float2bfloat16(f);
         }
-    for (; c < MLP_K1; c++) x[c] = __float2bfloat16(0.f);
+    }
+    *reinterpret_cast<uint4 *>(X + (size_t)r * MLP_K1 + ch * 8) = *reinterpret_cast<const uint4 *>(h);
 }
 
 // targets of row r: the error of the quadratic extrapolation
 // U^n + 2 dU^n - dU^(n-1), i.e. U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2), over
-// scale * oscale; columns 5..15 zero.  L.u[0..2] = U^n, U^(n-1), U^(n-2),
+// scale[5 + v] * oscale[v]; columns 5..15 zero.  L.u[0..2] = U^n, U^(n-1), U^(n-2),
 // next = U^(n+1)
 __global__ void k_mlp_targets(mlp_grid g, mlp_levels L, mlp_levels next, const float *scale, const float *oscale,
                               const int *rows, long long M, long long Mpad, float *T)
@@ -337,12 +345,13 @@ __global__ void k_mlp_targets(mlp_grid g, mlp_levels L, mlp_levels next, const f
     const size_t q = g.cell(rows ? rows[r] : r);
     for (int v = 0; v < 5; v++) {
         const double d3 = next.u[0][v][q] - 3.0 * L.u[0][v][q] + 3.0 * L.u[1][v][q] - L.u[2][v][q];
-        t[v] = (float)(d3 / ((double)scale[v] * (double)oscale[v]));
+        t[v] = (float)(d3 / ((double)scale[5 + v] * (double)oscale[v]));
     }
 }
 
 // the learned initial guess on every interior cell:
-// U_ = U^n + 2 dU^n - dU^(n-1) + scale * oscale * Y
+// U_ = U^n + 2 dU^n - dU^(n-1) + scale[5 + v] * oscale[v] * Y (Y null: the
+// plain quadratic extrapolation)
 __global__ void k_mlp_apply(mlp_grid g, mlp_levels L, const float *scale, const float *oscale, const float *Y,
                             long long M, double *o0, double *o1, double *o2, double *o3, double *o4)
 {
@@ -350,22 +359,35 @@ __global__ void k_mlp_apply(mlp_grid g, mlp_levels L, const float *scale, const 
     if (r >= M) return;
     const size_t q = g.cell(r);
     double *o[5] = {o0, o1, o2, o3, o4};
-    const float *y = Y + (size_t)r * MLP_N3;
 #pragma unroll
     for (int v = 0; v < 5; v++) {
         const double un = L.u[0][v][q], u1 = L.u[1][v][q], u2 = L.u[2][v][q];
-        o[v][q] = un + 2.0 * (un - u1) - (u1 - u2) + (double)scale[v] * (double)oscale[v] * (double)y[v];
+        const double c = Y ? (double)scale[5 + v] * (double)oscale[v] * (double)Y[(size_t)r * MLP_N3 + v] : 0.0;
+        o[v][q] = un + 2.0 * (un - u1) - (u1 - u2) + c;
     }
 }
 
-// partial sums of (U^n - U^{n-1})^2 per variable: block b of variable v
-__global__ void k_mlp_sq_partial(mlp_grid g, mlp_levels L, long long M, double *partial)
+// partial sums (block b of row y of the grid) of squared time differences
+// over the interior: D = 1: y < 5 the first difference U^n - U^(n-1) of
+// variable y, y >= 5 the second difference U^n - 2 U^(n-1) + U^(n-2) of
+// variable y - 5 (levels L.u[0..2]); D = 3: the third difference
+// U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2) of variable y (levels L.u[0..3])
+struct mlp_levels4 {
+    const double *u[4][5];
+};
+
+template <int D>
+__global__ void k_mlp_sq_partial(mlp_grid g, mlp_levels4 L, long long M, double *partial)
 {
-    const int v = blockIdx.y;
+    const int y = blockIdx.y, v = D == 1 ? y % 5 : y;
+    const bool second = D == 1 && y >= 5;
     double s = 0;
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x) {
         const size_t q = g.cell(r);
-        const double d = L.u[0][v][q] - L.u[1][v][q];
+        double d;
+        if (D == 3) d = L.u[0][v][q] - 3.0 * L.u[1][v][q] + 3.0 * L.u[2][v][q] - L.u[3][v][q];
+        else if (second) d = (L.u[0][v][q] - 2.0 * L.u[1][v][q]) + L.u[2][v][q];
+        else d = L.u[0][v][q] - L.u[1][v][q];
         s += d * d;
     }
     __shared__ double sh[256];
@@ -375,7 +397,35 @@ __global__ void k_mlp_sq_partial(mlp_grid g, mlp_levels L, long long M, double *
         if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[(size_t)v * gridDim.x + blockIdx.x] = sh[0];
+    if (threadIdx.x == 0) partial[(size_t)y * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// per-block sums over rows of T.Y, Y.Y and T.T for each of the 5 outputs
+// (FP64): partial[(b * 3 + s) * 5 + v]
+__global__ void k_mlp_dot_partial(const float *Y, const float *T, long long M, double *partial)
+{
+    double ty[5] = {0, 0, 0, 0, 0}, yy[5] = {0, 0, 0, 0, 0}, tt[5] = {0, 0, 0, 0, 0};
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+            const double y = Y[(size_t)r * MLP_N3 + v], t = T[(size_t)r * MLP_N3 + v];
+            ty[v] += t * y;
+            yy[v] += y * y;
+            tt[v] += t * t;
+        }
+    __shared__ double sh[15][256];
+    for (int v = 0; v < 5; v++) {
+        sh[v][threadIdx.x] = ty[v];
+        sh[5 + v][threadIdx.x] = yy[v];
+        sh[10 + v][threadIdx.x] = tt[v];
+    }
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int n = 0; n < 15; n++) sh[n][threadIdx.x] += sh[n][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 15) partial[(size_t)blockIdx.x * 15 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
 // dL/dY of the mean squared error over the 5 outputs of M rows: dY (bf16,
@@ -552,7 +602,7 @@ int cf_mlp_features(void *stream, int X, int Y, int Z, const double *const *leve
 {
     if (!levels15 || !scale || !Xout || M <= 0 || Mpad < M || Mpad % 128) return CF_ERR_ARG;
     mlp_grid g{X, Y, Z};
-    k_mlp_features<<<nblk(Mpad, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+    k_mlp_features<<<nblk(Mpad * (MLP_K1 / 8), 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         g, levels(levels15), scale, rows, M, Mpad, static_cast<__nv_bfloat16 *>(Xout));
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
@@ -577,7 +627,7 @@ int cf_mlp_targets(void *stream, int X, int Y, int Z, const double *const *level
 int cf_mlp_apply(void *stream, int X, int Y, int Z, const double *const *levels15, const float *scale,
                  const float *oscale, const float *Yp, double *const *out5)
 {
-    if (!levels15 || !scale || !oscale || !Yp || !out5) return CF_ERR_ARG;
+    if (!levels15 || !out5 || (Yp && (!scale || !oscale))) return CF_ERR_ARG;
     mlp_grid g{X, Y, Z};
     const long long M = (long long)X * Y * Z;
     k_mlp_apply<<<nblk(M, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
@@ -585,26 +635,65 @@ int cf_mlp_apply(void *stream, int X, int Y, int Z, const double *const *levels1
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
-// RMS of U^n - U^{n-1} per variable over the interior (FP64 sums); rms5 host output
-int cf_mlp_rms(void *stream, int X, int Y, int Z, const double *const *levels10, double *partial_dev,
-               int nblocks, double *rms5)
+static int mlp_rms(int D, void *stream, int X, int Y, int Z, const double *const *lv, double *partial_dev,
+                   int nblocks, double *rms)
 {
-    if (!levels10 || !partial_dev || !rms5 || nblocks <= 0) return CF_ERR_ARG;
+    if (!lv || !partial_dev || !rms || nblocks <= 0 || X <= 0 || Y <= 0 || Z <= 0) return CF_ERR_ARG;
     mlp_grid g{X, Y, Z};
-    mlp_levels L{};
-    for (int l = 0; l < 2; l++)
-        for (int v = 0; v < 5; v++) L.u[l][v] = levels10[5 * l + v];
+    mlp_levels4 L{};
+    const int nlev = D == 1 ? 3 : 4, nrow = D == 1 ? 10 : 5;
+    for (int l = 0; l < nlev; l++)
+        for (int v = 0; v < 5; v++) {
+            if (!lv[5 * l + v]) return CF_ERR_ARG;
+            L.u[l][v] = lv[5 * l + v];
+        }
     const long long M = (long long)X * Y * Z;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    k_mlp_sq_partial<<<dim3((unsigned)nblocks, 5), 256, 0, s>>>(g, L, M, partial_dev);
-    std::vector<double> h((size_t)5 * nblocks);
+    if (D == 1) k_mlp_sq_partial<1><<<dim3((unsigned)nblocks, nrow), 256, 0, s>>>(g, L, M, partial_dev);
+    else k_mlp_sq_partial<3><<<dim3((unsigned)nblocks, nrow), 256, 0, s>>>(g, L, M, partial_dev);
+    std::vector<double> h((size_t)nrow * nblocks);
     if (cudaMemcpyAsync(h.data(), partial_dev, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return CF_ERR_CUDA;
-    for (int v = 0; v < 5; v++) {
+    for (int y = 0; y < nrow; y++) {
         double t = 0;
-        for (int b = 0; b < nblocks; b++) t += h[(size_t)v * nblocks + b];
-        rms5[v] = std::sqrt(t / (double)M);
+        for (int b = 0; b < nblocks; b++) t += h[(size_t)y * nblocks + b];
+        rms[y] = std::sqrt(t / (double)M);
+    }
+    return CF_OK;
+}
+
+// RMS over the interior per variable of the first (rms10[0..4]) and second
+// (rms10[5..9]) time differences; levels15 = U^n, U^(n-1), U^(n-2)
+int cf_mlp_rms(void *stream, int X, int Y, int Z, const double *const *levels15, double *partial_dev,
+               int nblocks, double *rms10)
+{
+    return mlp_rms(1, stream, X, Y, Z, levels15, partial_dev, nblocks, rms10);
+}
+
+// RMS of U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2) per variable (levels20 in that order)
+int cf_mlp_rms3(void *stream, int X, int Y, int Z, const double *const *levels20, double *partial_dev,
+                int nblocks, double *rms5)
+{
+    return mlp_rms(3, stream, X, Y, Z, levels20, partial_dev, nblocks, rms5);
+}
+
+// sums over M rows of T.Y, Y.Y and T.T per output into sums15 (host):
+// [0..4] = T.Y, [5..9] = Y.Y, [10..14] = T.T
+int cf_mlp_dot(void *stream, const float *Yv, const float *T, long long M, double *partial_dev, int nblocks,
+               double *sums15)
+{
+    if (!Yv || !T || !partial_dev || !sums15 || M <= 0 || nblocks <= 0) return CF_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    k_mlp_dot_partial<<<(unsigned)nblocks, 256, 0, s>>>(Yv, T, M, partial_dev);
+    std::vector<double> h((size_t)15 * nblocks);
+    if (cudaMemcpyAsync(h.data(), partial_dev, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return CF_ERR_CUDA;
+    for (int n = 0; n < 15; n++) {
+        double t = 0;
+        for (int b = 0; b < nblocks; b++) t += h[(size_t)b * 15 + n];
+        sums15[n] = t;
     }
     return CF_OK;
 }

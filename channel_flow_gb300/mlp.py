@@ -1,23 +1,27 @@
 """Learned initial guess of the pseudo-time iterations.
 
 A per-cell MLP maps the 3x3x3 neighbourhood of the last two time
-increments, dU^n = U^n - U^(n-1) and dU^(n-1) = U^(n-1) - U^(n-2), of the
-five conserved variables (2 x 27 x 5 = 270 features, scaled per variable by
-the RMS of dU^n) through two hidden layers of 128 SiLU units to the five
-components of the error of the quadratic extrapolation U^n + 2 dU^n -
-dU^(n-1) of U^(n+1) (scaled by RMS(dU^n) times a per-variable factor fixed
-from the training data).  The network corrects the extrapolation rather than
-predicting the increment itself, so its BF16 precision limits only the
-small correction.  Before the sub-iterations of a physical step the state
-starts from that guess instead of U^n; the sub-iterations still run to the
-same residual tolerance, so the plain LU-SGS loop remains the judge and the
-fallback.
+increments dU^n = U^n - U^(n-1) and dU^(n-1) = U^(n-1) - U^(n-2) of the
+five conserved variables, presented as dU^n and dU^n - dU^(n-1) (2 x 27 x 5
+= 270 features, each kind scaled per variable by its interior RMS; the
+second difference is formed in FP64, because in BF16 the two increments
+agree to about the digits that their difference needs), through two hidden
+layers of 128 SiLU units to the five components of the error of the
+quadratic extrapolation U^n + 2 dU^n - dU^(n-1) of U^(n+1) (in units of the
+RMS second difference times a per-variable factor fitted on the training
+windows).  The network corrects the extrapolation rather than predicting the
+increment itself, so its BF16 precision limits only the small correction,
+and a least-squares gain per variable, fitted on a held-out window, scales a
+correction that does not help there towards zero.  Before the
+sub-iterations of a physical step the state starts from that guess instead
+of U^n; the sub-iterations still run to the same residual tolerance, so the
+plain LU-SGS loop remains the judge and the fallback.
 
 Every matrix product runs on the tcgen05 tensor cores (``cf_gemm_bf16``,
 BF16 operands, FP32 accumulation) and every other step in the package's own
 kernels (``cf_mlp_*``); PyTorch only holds the device buffers.  Training is
-Adam on the mean squared error over snapshots harvested from the solver's
-own steps.
+Adam on the mean squared error over windows harvested from the solver's own
+steps.
 """
 from __future__ import annotations
 
@@ -73,11 +77,14 @@ def _pad(m: int) -> int:
 class LearnedGuess:
     """The MLP on one device; ``capacity`` rows per forward/training call."""
 
-    def __init__(self, capacity: int = 32768, seed: int = 0, lr: float = 1e-3):
+    def __init__(self, capacity: int = 32768, seed: int = 0, lr: float = 1e-3, batch: int | None = None):
+        """``capacity``: rows of one inference pass (the grid's cells for
+        ``guess``); ``batch``: rows of one training step (default capacity)."""
         import torch
         self.torch = torch
         self.lib = _lib.load()
         self.cap = _pad(capacity)
+        self.tcap = self.cap if batch is None else min(_pad(batch), self.cap)
         dev = "cuda"
         f32, bf = torch.float32, torch.bfloat16
         self.p = torch.from_numpy(init_params(seed)).to(dev)
@@ -91,13 +98,16 @@ class LearnedGuess:
         self.W3b = torch.zeros(N3, H, dtype=bf, device=dev)
         self.W2T = torch.zeros(H, H, dtype=bf, device=dev)
         self.W3p = torch.zeros(H, K3, dtype=bf, device=dev)
+        # inference-sized buffers
         M = self.cap
         self.X = torch.zeros(M, K1, dtype=bf, device=dev)
         self.H1 = torch.zeros(M, H, dtype=bf, device=dev)
         self.H2 = torch.zeros(M, H, dtype=bf, device=dev)
+        self.Y = torch.zeros(M, N3, dtype=f32, device=dev)
+        # training-sized buffers
+        M = self.tcap
         self.Z1 = torch.zeros(M, H, dtype=f32, device=dev)
         self.Z2 = torch.zeros(M, H, dtype=f32, device=dev)
-        self.Y = torch.zeros(M, N3, dtype=f32, device=dev)
         self.T = torch.zeros(M, N3, dtype=f32, device=dev)
         self.dY = torch.zeros(M, K3, dtype=bf, device=dev)
         self.dYT = torch.zeros(N3, M, dtype=bf, device=dev)
@@ -110,10 +120,15 @@ class LearnedGuess:
         self.H2T = torch.zeros(H, M, dtype=bf, device=dev)
         self.XT = torch.zeros(K1, M, dtype=bf, device=dev)
         self.partial = torch.zeros(M // 256 * 6, dtype=f32, device=dev)
-        self.rms_partial = torch.zeros(5 * 512, dtype=torch.float64, device=dev)
+        self.rms_partial = torch.zeros(10 * 512, dtype=torch.float64, device=dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.scale = torch.ones(5, dtype=f32, device=dev)
-        self.oscale = torch.ones(5, dtype=f32, device=dev)
+        self.scale = torch.ones(10, dtype=f32, device=dev)
+        self.oscale = torch.ones(5, dtype=f32, device=dev)   # output unit of the network (targets)
+        self.ogain = torch.ones(5, dtype=f32, device=dev)    # oscale times the fitted gain (the guess)
+        self.gen = torch.Generator(device=dev)
+        self.gen.manual_seed(seed + 7919)
+        self.validation = None
+        self.updates = []
         self.pack()
 
     # -- helpers ----------------------------------------------------------
@@ -147,11 +162,14 @@ class LearnedGuess:
             raise RuntimeError("a tensor-core GEMM wait ran out on the device")
 
     # -- network ----------------------------------------------------------
-    def forward(self, Mpad: int):
-        """Y = MLP(X[:Mpad]) with the hidden pre-activations kept."""
+    def forward(self, Mpad: int, keep: bool = True):
+        """Y = MLP(X[:Mpad]); ``keep`` stores the hidden pre-activations
+        for backward (at most the training batch)."""
+        if keep and Mpad > self.tcap:
+            raise ValueError(f"{Mpad} rows exceed the training batch {self.tcap}")
         b1, b2, b3 = self.view("b1"), self.view("b2"), self.view("b3")
-        self.gemm(self.X, self.W1b, Mpad, H, K1, EPI_SILU, b1, self.H1, self.Z1, H)
-        self.gemm(self.H1, self.W2b, Mpad, H, H, EPI_SILU, b2, self.H2, self.Z2, H)
+        self.gemm(self.X, self.W1b, Mpad, H, K1, EPI_SILU, b1, self.H1, self.Z1 if keep else None, H)
+        self.gemm(self.H1, self.W2b, Mpad, H, H, EPI_SILU, b2, self.H2, self.Z2 if keep else None, H)
         self.gemm(self.H2, self.W3b, Mpad, N3, H, EPI_BIAS, b3, self.Y, None, N3)
 
     def backward(self, M: int, Mpad: int):
@@ -194,10 +212,11 @@ class LearnedGuess:
         return self.loss(Mpad) / (M * OUT)
 
     # -- data ---------------------------------------------------------------
-    def set_scale(self, grid, Un, Unm1):
-        """Per-variable scaling: RMS of U^n - U^(n-1) over the interior."""
-        rms = np.zeros(5)
-        arr = (C.c_void_p * 10)(*[t.data_ptr() for t in list(Un) + list(Unm1)])
+    def set_scale(self, grid, Un, Unm1, Unm2):
+        """Per-variable scaling: interior RMS of the first and second time
+        differences U^n - U^(n-1) and U^n - 2 U^(n-1) + U^(n-2) (10 values)."""
+        rms = np.zeros(10)
+        arr = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
         self._ok(self.lib.cf_mlp_rms(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
                                      self.rms_partial.data_ptr(), 512, rms.ctypes.data), "cf_mlp_rms")
         rms = np.where(rms > 0, rms, 1.0)
@@ -218,49 +237,134 @@ class LearnedGuess:
     def load_targets(self, grid, Unp1, Un, Unm1, Unm2, rows=None):
         M = grid.cells if rows is None else len(rows)
         Mpad = _pad(M)
+        if Mpad > self.tcap:
+            raise ValueError(f"{M} rows exceed the training batch {self.tcap}")
         arr = (C.c_void_p * 20)(*[t.data_ptr() for t in list(Unp1) + list(Un) + list(Unm1) + list(Unm2)])
         self._ok(self.lib.cf_mlp_targets(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr, self.scale.data_ptr(),
                                          self.oscale.data_ptr(), None if rows is None else rows.data_ptr(), M, Mpad,
                                          self.T.data_ptr()), "cf_mlp_targets")
         return M, Mpad
 
-    def fit_output_scale(self, grid, history):
+    def fit_output_scale(self, grid, history, windows=None):
         """Per-variable output factor: RMS of the extrapolation error over
-        RMS(dU^n), averaged over a history [U^0, U^1, ...] of FP64 states."""
+        the RMS of the second time difference, averaged over the windows n
+        (default all) of a history [U^0, U^1, ...] of FP64 states."""
         r = []
-        for n in range(2, len(history) - 1):
-            s = self.set_scale(grid, history[n], history[n - 1])
-            err = [history[n + 1][v] - 3 * history[n][v] + 3 * history[n - 1][v] - history[n - 2][v]
-                   for v in range(5)]
-            e = np.asarray([float(x[3:grid.gend + 1, 2:grid.ny + 1, 2:grid.nz + 1].pow(2).mean().sqrt())
-                            for x in err])
+        for n in (range(2, len(history) - 1) if windows is None else windows):
+            s = self.set_scale(grid, history[n], history[n - 1], history[n - 2])[5:]
+            e = np.zeros(5)
+            lv = [history[n + 1], history[n], history[n - 1], history[n - 2]]
+            arr = (C.c_void_p * 20)(*[t.data_ptr() for level in lv for t in level])
+            self._ok(self.lib.cf_mlp_rms3(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
+                                          self.rms_partial.data_ptr(), 512, e.ctypes.data), "cf_mlp_rms3")
             r.append(e / s)
         f = np.mean(r, axis=0) if r else np.ones(5)
         f = np.where(f > 0, f, 1.0)
         self.oscale.copy_(self.torch.from_numpy(f.astype(np.float32)))
+        self.ogain.copy_(self.oscale)
         return f
 
-    def train(self, grid, history, epochs: int = 20):
-        """Adam on every (U^(n-2), U^(n-1), U^n) -> U^(n+1) window of a
-        history of FP64 states (each window one batch of all cells)."""
-        self.fit_output_scale(grid, history)
+    def _rows(self, grid, batch, gen):
+        if batch is None or batch >= grid.cells:
+            return None
+        torch = self.torch
+        return torch.randint(0, grid.cells, (batch,), generator=gen, device="cuda", dtype=torch.int32)
+
+    def train(self, grid, history, epochs: int = 20, batch: int | None = None, seed: int = 0,
+              holdout: bool = True):
+        """Adam on the (U^(n-2), U^(n-1), U^n) -> U^(n+1) windows of a
+        history of FP64 states, one step per window and epoch: on all cells
+        (``batch`` None) or on ``batch`` cells drawn at random each step.
+        With ``holdout`` (and at least two windows) the last window is kept
+        out of training and used by ``calibrate``."""
+        torch = self.torch
+        windows = list(range(2, len(history) - 1))
+        if not windows:
+            raise ValueError("training needs a history of at least four states")
+        val = windows.pop() if holdout and len(windows) >= 2 else None
+        self.fit_output_scale(grid, history, windows)
+        scales = {n: self.set_scale(grid, history[n], history[n - 1], history[n - 2]).astype(np.float32)
+                  for n in windows}
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(seed)
         losses = []
         for _ in range(epochs):
-            for n in range(2, len(history) - 1):
-                self.set_scale(grid, history[n], history[n - 1])
-                M, Mpad = self.load_features(grid, history[n], history[n - 1], history[n - 2])
-                self.load_targets(grid, history[n + 1], history[n], history[n - 1], history[n - 2])
+            for n in windows:
+                self.scale.copy_(torch.from_numpy(scales[n]))
+                rows = self._rows(grid, batch, gen)
+                M, Mpad = self.load_features(grid, history[n], history[n - 1], history[n - 2], rows=rows)
+                self.load_targets(grid, history[n + 1], history[n], history[n - 1], history[n - 2], rows=rows)
                 losses.append(self.step(M, Mpad))
         self.check_device()
+        self.validation = None
+        if val is not None:
+            self.validation = self.calibrate(grid, history[val + 1], history[val], history[val - 1],
+                                             history[val - 2], batch=batch, seed=seed + 1)
         return losses
+
+    def calibrate(self, grid, Unp1, Un, Unm1, Unm2, batch: int | None = None, seed: int | None = None):
+        """Least-squares gain per output of the correction on a window the
+        network has not been trained on, alpha_v = <t, y> / <y, y> clipped
+        to [0, 2]; the guess then uses oscale * alpha, so that a correction
+        that does not reduce the extrapolation error there is scaled down.
+        Returns alpha and the window's RMS error of extrapolation +
+        correction relative to the extrapolation alone, per variable,
+        before and after the gain."""
+        torch = self.torch
+        gen = self.gen
+        if seed is not None:
+            gen = torch.Generator(device="cuda")
+            gen.manual_seed(seed)
+        self.set_scale(grid, Un, Unm1, Unm2)
+        rows = self._rows(grid, batch if batch is not None else self.tcap, gen)
+        M, Mpad = self.load_features(grid, Un, Unm1, Unm2, rows=rows)
+        self.load_targets(grid, Unp1, Un, Unm1, Unm2, rows=rows)
+        self.forward(Mpad, keep=False)
+        sums = np.zeros(15)
+        self._ok(self.lib.cf_mlp_dot(self._s(), self.Y.data_ptr(), self.T.data_ptr(), M, self.rms_partial.data_ptr(),
+                                     128, sums.ctypes.data), "cf_mlp_dot")
+        ty, yy, tt = sums[:5], sums[5:10], sums[10:]
+        tt = np.where(tt > 0, tt, 1.0)
+        alpha = np.clip(np.where(yy > 0, ty / np.where(yy > 0, yy, 1.0), 0.0), 0.0, 2.0)
+        before = np.sqrt(np.maximum(tt - 2 * ty + yy, 0) / tt)
+        after = np.sqrt(np.maximum(tt - 2 * alpha * ty + alpha * alpha * yy, 0) / tt)
+        self.ogain.copy_(self.oscale * torch.from_numpy(alpha.astype(np.float32)).to(self.oscale.device))
+        return {"alpha": alpha.tolist(), "err_over_extrapolation_raw": before.tolist(),
+                "err_over_extrapolation": after.tolist()}
+
+    def update(self, grid, Unp1, Un, Unm1, Unm2, adam_steps: int = 2, batch: int = 65536):
+        """Online step once U^(n+1) is known: first the gain on this window
+        (which the network has not seen, so the fit is out of sample), then
+        ``adam_steps`` Adam steps on random cells of it.  Returns the
+        calibration of ``calibrate``."""
+        cal = self.calibrate(grid, Unp1, Un, Unm1, Unm2, batch=batch)
+        for _ in range(adam_steps):
+            rows = self._rows(grid, batch, self.gen)
+            M, Mpad = self.load_features(grid, Un, Unm1, Unm2, rows=rows)
+            self.load_targets(grid, Unp1, Un, Unm1, Unm2, rows=rows)
+            self.step(M, Mpad)
+        self.updates.append(cal)
+        return cal
+
+    @staticmethod
+    def extrapolate(grid, Un, Unm1, Unm2, out, stream=None):
+        """out (U_) = U^n + 2 dU^n - dU^(n-1) on every interior cell."""
+        import torch
+        lib = _lib.load()
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        a = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
+        o = (C.c_void_p * 5)(*[t.data_ptr() for t in out])
+        rc = lib.cf_mlp_apply(s, grid.X_out, grid.Y_out, grid.Z_out, a, None, None, None, o)
+        if rc != _lib.CF_OK:
+            raise RuntimeError(f"cf_mlp_apply failed with status {rc}")
 
     def guess(self, grid, Un, Unm1, Unm2, out):
         """out (U_) = U^n + 2 dU^n - dU^(n-1) + the network's correction on
         every interior cell; the grid's cells must fit the capacity."""
-        self.set_scale(grid, Un, Unm1)
+        self.set_scale(grid, Un, Unm1, Unm2)
         M, Mpad = self.load_features(grid, Un, Unm1, Unm2)
-        self.forward(Mpad)
+        self.forward(Mpad, keep=False)
         a = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
         o = (C.c_void_p * 5)(*[t.data_ptr() for t in out])
         self._ok(self.lib.cf_mlp_apply(self._s(), grid.X_out, grid.Y_out, grid.Z_out, a, self.scale.data_ptr(),
-                                       self.oscale.data_ptr(), self.Y.data_ptr(), o), "cf_mlp_apply")
+                                       self.ogain.data_ptr(), self.Y.data_ptr(), o), "cf_mlp_apply")

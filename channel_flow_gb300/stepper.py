@@ -11,21 +11,43 @@ its sub-iterations from
   network.
 
 The tolerance and the iteration loop are the same in every case; only the
-starting point differs.
+starting point differs.  With ``online`` set, a learned guess also learns
+during the run: once a step has converged, the network's gain is refitted
+on that step (which it predicted without seeing it) and it takes a few Adam
+steps on it (``LearnedGuess.update``).  Both guesses replace the interior
+cells of U_; its ghost cells are rebuilt by the boundary conditions at the
+start of every sub-iteration, as in the plain loop.
 """
 from __future__ import annotations
 
 from collections import deque
 
+from . import mlp
+
 
 class Stepper:
-    def __init__(self, ctx, fields: dict, **step_kw):
+    def __init__(self, ctx, fields: dict, online: dict | None = None, **step_kw):
         self.ctx = ctx
         self.f = fields
+        self.online = online
         self.kw = step_kw
         self.n = 0
         self.hist = deque(maxlen=3)
         self.hist.append([u.clone() for u in fields["U"]])
+
+    def restore(self, levels, step: int = 0):
+        """Restart from saved time levels [..., U^(n-1), U^n] (the last
+        three are kept): U_ = U = U^n, Uq = U^(n-1)."""
+        self.hist.clear()
+        for lv in levels[-3:]:
+            self.hist.append([u.clone() for u in lv])
+        un = self.hist[-1]
+        uq = self.hist[-2] if len(self.hist) > 1 else un
+        for v in range(5):
+            self.f["U_"][v].copy_(un[v])
+            self.f["U"][v].copy_(un[v])
+            self.f["Uq"][v].copy_(uq[v])
+        self.n = step
 
     def step(self, guess=None):
         """One physical step; returns (sub-iterations, er[5], Q)."""
@@ -34,12 +56,13 @@ class Stepper:
             if isinstance(guess, str):
                 if guess != "extrapolate":
                     raise ValueError(f"unknown guess {guess!r}")
-                for v in range(5):
-                    self.f["U_"][v].copy_(3 * un[v] - 3 * u1[v] + u2[v])
+                mlp.LearnedGuess.extrapolate(self.ctx.grid, un, u1, u2, self.f["U_"])
             else:
                 guess.guess(self.ctx.grid, un, u1, u2, self.f["U_"])
         self.n += 1
         it, er, q = self.ctx.step(self.f, step=self.n, **self.kw)
+        if self.online is not None and guess is not None and not isinstance(guess, str) and len(self.hist) == 3:
+            guess.update(self.ctx.grid, self.f["U"], self.hist[2], self.hist[1], self.hist[0], **self.online)
         self.hist.append([u.clone() for u in self.f["U"]])
         return it, er, q
 

@@ -297,6 +297,12 @@ int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields
             double *er, double *Q);
 /* forget the running residual maxima */
 int cf_step_reset(cf_ctx *ctx);
+/* read (set = 0) or replace (set = 1) the running residual maxima E1..E5 */
+int cf_step_scale(cf_ctx *ctx, double *E, int set);
+/* the normalised er1..er5 of each pseudo-time iteration of the last cf_step,
+ * row-major [iteration][5]; *count = that step's iterations, at most cap
+ * rows are copied */
+int cf_step_residuals(cf_ctx *ctx, double *out, int cap, int *count);
 
 
 /* ------------------------------------------------------------------ */
@@ -319,19 +325,36 @@ int cf_gemm_bf16(void *cuda_stream, const void *A, const void *B, int M, int N, 
  * 2 + r % Z), or rows[r] of that numbering when rows is not NULL; Mpad
  * (multiple of 128) rows are written, rows >= M zero.  Fields are FP64
  * device arrays in the reference layout; levels arrays list U^n,
- * U^(n-1)[, U^(n-2)] (five fields each). */
-int cf_mlp_features(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale5,
+ * U^(n-1)[, U^(n-2)] (five fields each).  scale10 (device floats) holds the
+ * interior RMS of the first time difference U^n - U^(n-1) per variable
+ * ([0..4]) and of the second, U^n - 2 U^(n-1) + U^(n-2) ([5..9]).
+ * features: column 135 l + 27 v + s of a row is the first (l = 0) or
+ * second (l = 1) difference of variable v at neighbour s = 9 (di+1) +
+ * 3 (dj+1) + (dk+1) of the 3x3x3 stencil, over its scale. */
+int cf_mlp_features(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale10,
                     const int *rows, long long M, long long Mpad, void *X_bf16_Mpad_x_320);
 /* targets: the error of the quadratic extrapolation, U^(n+1) - 3 U^n +
- * 3 U^(n-1) - U^(n-2), over scale5 * oscale5 (levels20 = U^(n+1), U^n,
- * U^(n-1), U^(n-2)) */
-int cf_mlp_targets(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, const float *scale5,
+ * 3 U^(n-1) - U^(n-2), over scale10[5 + v] * oscale5[v] (levels20 = U^(n+1),
+ * U^n, U^(n-1), U^(n-2)) */
+int cf_mlp_targets(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, const float *scale10,
                    const float *oscale5, const int *rows, long long M, long long Mpad, float *T_Mpad_x_16);
-/* the guess: out = U^n + 2 dU^n - dU^(n-1) + scale5 * oscale5 * Y (levels15 = U^n, U^(n-1), U^(n-2)) */
-int cf_mlp_apply(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale5,
+/* the guess on every interior cell: out = U^n + 2 dU^n - dU^(n-1) +
+ * scale10[5 + v] * oscale5[v] * Y (levels15 = U^n, U^(n-1), U^(n-2));
+ * Y = NULL gives the plain quadratic extrapolation (scale10, oscale5 may then be NULL) */
+int cf_mlp_apply(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale10,
                  const float *oscale5, const float *Y_M_x_16, double *const *out5);
-int cf_mlp_rms(void *cuda_stream, int X, int Y, int Z, const double *const *levels10, double *partial_dev,
-               int nblocks, double *rms5_host);
+/* interior RMS per variable of the first and second time differences
+ * (rms10_host[0..4], [5..9]); levels15 = U^n, U^(n-1), U^(n-2); partial_dev
+ * holds 10 * nblocks doubles */
+int cf_mlp_rms(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, double *partial_dev,
+               int nblocks, double *rms10_host);
+/* interior RMS per variable of U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2) (levels20 in that order) */
+int cf_mlp_rms3(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, double *partial_dev,
+                int nblocks, double *rms5_host);
+/* sums over M rows of T.Y, Y.Y, T.T per output (FP64) into sums15_host[0..4], [5..9], [10..14];
+ * partial_dev holds 15 * nblocks doubles */
+int cf_mlp_dot(void *cuda_stream, const float *Y, const float *T, long long M, double *partial_dev, int nblocks,
+               double *sums15_host);
 int cf_mlp_loss_grad(void *cuda_stream, const float *Y, const float *T, long long M, long long Mpad,
                      void *dY_bf16_Mpad_x_64, void *dYT_bf16_16_x_Mpad, float *partial);
 int cf_mlp_silu_bwd(void *cuda_stream, const float *dH, const float *Z, long long Mpad, void *dZ_bf16,

@@ -61,3 +61,73 @@ def forward_backward(p, offs, X, T, M):
     for name, (o, s) in offs.items():
         flat[o:o + int(np.prod(s))] = g[name].ravel()
     return loss, Y, flat
+
+
+# ---------------------------------------------------------------------------
+# data kernels: features, targets, the guess and the scalings, on fields in
+# the reference layout [X_out+6][Y_out+4][Z_out+4] (interior i = 3..,
+# j = 2.., k = 2..; rows x-major, z fastest)
+
+def _interior(a, X, Y, Z, di=0, dj=0, dk=0):
+    return a[3 + di:3 + di + X, 2 + dj:2 + dj + Y, 2 + dk:2 + dk + Z].reshape(-1)
+
+
+def rms(levels, X, Y, Z):
+    """RMS per variable of the first and second time differences
+    (cf_mlp_rms); levels = [U^n, U^(n-1), U^(n-2)], five arrays each."""
+    out = np.zeros(10)
+    for v in range(5):
+        a0, a1, a2 = (_interior(levels[l][v], X, Y, Z) for l in range(3))
+        out[v] = np.sqrt(np.mean((a0 - a1) ** 2))
+        out[5 + v] = np.sqrt(np.mean(((a0 - 2.0 * a1) + a2) ** 2))
+    return out
+
+
+def features(levels, scale10, X, Y, Z, rows=None):
+    """Feature rows (BF16 values as float64) of cf_mlp_features: column
+    135 l + 27 v + s = kind l (first / second difference) of variable v at
+    stencil neighbour s, times the float32 reciprocal of its scale."""
+    n = X * Y * Z
+    rows = np.arange(n) if rows is None else np.asarray(rows)
+    F = np.zeros((len(rows), K1))
+    sc = np.asarray(scale10, np.float32)
+    for l in range(2):
+        for v in range(5):
+            inv = np.float32(1.0) / sc[5 * l + v]
+            for st in range(27):
+                di, dj, dk = st // 9 - 1, (st // 3) % 3 - 1, st % 3 - 1
+                a0 = _interior(levels[0][v], X, Y, Z, di, dj, dk)[rows]
+                a1 = _interior(levels[1][v], X, Y, Z, di, dj, dk)[rows]
+                if l == 0:
+                    d = a0 - a1
+                else:
+                    d = (a0 - 2.0 * a1) + _interior(levels[2][v], X, Y, Z, di, dj, dk)[rows]
+                F[:, 135 * l + 27 * v + st] = bf16(d.astype(np.float32) * inv)
+    return F
+
+
+def targets(next_level, levels, scale10, oscale5, X, Y, Z, rows=None):
+    """cf_mlp_targets: the third time difference over scale10[5+v] * oscale5[v]."""
+    n = X * Y * Z
+    rows = np.arange(n) if rows is None else np.asarray(rows)
+    T = np.zeros((len(rows), N3))
+    for v in range(5):
+        u = [_interior(a[v], X, Y, Z)[rows] for a in (next_level, levels[0], levels[1], levels[2])]
+        d3 = u[0] - 3.0 * u[1] + 3.0 * u[2] - u[3]
+        T[:, v] = d3 / (np.float64(np.float32(scale10[5 + v])) * np.float64(np.float32(oscale5[v])))
+    return T
+
+
+def apply(levels, scale10, oscale5, Y_out16, X, Y, Z):
+    """cf_mlp_apply on the interior: U^n + 2 dU^n - dU^(n-1) + the scaled
+    correction (Y_out16 None: the extrapolation alone); returns five
+    interior arrays [X*Y*Z]."""
+    out = []
+    for v in range(5):
+        un, u1, u2 = (_interior(levels[l][v], X, Y, Z) for l in range(3))
+        c = 0.0
+        if Y_out16 is not None:
+            c = np.float64(np.float32(scale10[5 + v])) * np.float64(np.float32(oscale5[v])) * \
+                np.asarray(Y_out16[:, v], np.float64)
+        out.append(un + 2.0 * (un - u1) - (u1 - u2) + c)
+    return out
