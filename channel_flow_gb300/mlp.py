@@ -15,7 +15,7 @@ and a least-squares gain per variable, fitted on a held-out window, scales a
 correction that does not help there towards zero.  Before the
 sub-iterations of a physical step the state starts from that guess instead
 of U^n; the sub-iterations still run to the same residual tolerance, so the
-plain LU-SGS loop remains the judge and the fallback.
+plain LU-SGS loop still decides convergence and remains the fallback.
 
 Every matrix product runs on the tcgen05 tensor cores (``cf_gemm_bf16``,
 BF16 operands, FP32 accumulation) and every other step in the package's own
