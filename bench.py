@@ -278,6 +278,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess physical-step comparison")
+    ap.add_argument("--no-wavy", action="store_true", help="skip the 512x256x384 wavy-wall measurement")
     ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs"],
                     help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
                          "(one LU-SGS pseudo-iteration per step, for profiling)")
@@ -601,6 +602,26 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=12, evals=3,
     return out
 
 
+def wavy_workload(ctx, g, torch, amplitude_over_h=0.05, wavelength_over_h=math.pi):
+    """The benchmark channel with a wavy lower wall (amplitude 0.05 h,
+    wavelength pi h: two waves over 2 pi h) and the conservative metrics of
+    cf_wavy_metrics; seeded laminar-plus-noise state at Mach 0.5."""
+    from channel_flow_gb300 import synthetic as syn, wavy
+    wall = wavy.wall_for(g, amplitude_over_h, wavelength_over_h, stretching=GAMMA, conservative=True)
+    m = wavy.channel_metrics(g, wall)
+    J = m["J"].cpu().numpy()
+    host = {"U": syn.channel_state(g, J, seed=SEED, mach=0.5, noise=0.05, jitter=0.01, gamma=GAMMA), "J": J,
+            "cm": [t.cpu().numpy() for t in m["cm"]], "Yp": m["Yp"].cpu().numpy()}
+    w = DeviceWorkload(ctx, g, host, torch)
+    del host
+    for dst, src in ((w.fu, m["fu"]), (w.fv, m["fv"]), (w.fw, m["fw"])):
+        for a, b in zip(dst, src):
+            a.copy_(b)
+    del m
+    torch.cuda.synchronize()
+    return w, wall
+
+
 def secondary(ctx, g, w, calls, stream, torch, args):
     """Per precision: the RHS and one dual-time pseudo-iteration (RHS +
     hyperplane LU-SGS) on the benchmark grid, and on the 256 x 192 x 192
@@ -627,6 +648,23 @@ def secondary(ctx, g, w, calls, stream, torch, args):
             out["256x192x192"][prec] = pseudo_iteration(ctx2, g2, w2, calls2, stream, torch, 3)
         ctx2.close()
         del w2, calls2
+        torch.cuda.empty_cache()
+    if not args.no_large and not args.no_wavy:
+        # the 50 M-cell channel with a wavy lower wall (metrics from cf_wavy_metrics)
+        try:
+            g3 = syn.channel_grid(512, 256, 384)
+            ctx3 = cf.Context(g3, precision="fp64", gamma=GAMMA)
+            w3, wall = wavy_workload(ctx3, g3, torch)
+            calls3 = rhs_calls(ctx3, w3, lambda x: x.data_ptr())
+            r = {"wall": {"amplitude_over_h": 0.05, "wavelength_over_h": math.pi, "metrics": "conservative"}}
+            for prec in ("fp64", "fp32"):
+                ctx3.set_precision(prec)
+                r[prec] = pseudo_iteration(ctx3, g3, w3, calls3, stream, torch, 2)
+            out["512x256x384_wavy"] = r
+            ctx3.close()
+            del w3, calls3
+        except Exception as exc:
+            out["512x256x384_wavy"] = {"error": repr(exc)}
         torch.cuda.empty_cache()
     for k, v in out.items():
         if "fp64" in v and "fp32" in v:

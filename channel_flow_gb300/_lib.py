@@ -40,6 +40,11 @@ class cf_step_params(C.Structure):
                 ("e_high", C.c_double), ("e_low", C.c_double), ("statistic_step", C.c_int)]
 
 
+class cf_wavy_wall(C.Structure):
+    _fields_ = [("amplitude", C.c_double), ("wavelength", C.c_double), ("stretching", C.c_double),
+                ("conservative", C.c_int)]
+
+
 def grid_struct(grid) -> "cf_grid":
     return cf_grid(grid.X_out, grid.Y_out, grid.Z_out, grid.deltaXI, grid.deltaET, grid.deltaZT,
                    grid.K, grid.R, grid.e, grid.Cv, grid.mu_L, grid.Pr_L, grid.f, grid.high, grid.Q0)
@@ -89,6 +94,8 @@ _SIGS = {
     "cf_Jacobian_u": ([P, C.c_int, C.POINTER(P)], C.c_int),
     "cf_Jacobian_v": ([P, C.c_int, C.POINTER(P)], C.c_int),
     "cf_Jacobian_w": ([P, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_wavy_metrics": ([P, P, P, C.c_int, C.POINTER(P)], C.c_int),
+    "cf_wavy_y_point": ([P, P, P, P], C.c_int),
     "cf_set_output_dir": ([P, C.c_char_p], C.c_int),
     "cf_Driven_force": ([P, C.c_int, P, P, P, P], C.c_int),
     "cf_Statistic": ([P, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(P)], C.c_int),

@@ -1,6 +1,6 @@
 """Build the CUDA library ``channel_flow_gb300/libcfgb300.so`` (sm_103a).
 
-Three translation units, compiled in parallel with nvcc:
+Translation units, compiled in parallel with nvcc:
 
 * ``cf_variant.cu`` as namespace ``cf_exact`` with ``--fmad=false``: the FP64
   kernels without fused multiply-add, whose results equal the reference's
@@ -11,7 +11,8 @@ Three translation units, compiled in parallel with nvcc:
 * ``cf_noalloc.cu``: the allocation-free DPLUSGS entry point (its scratch is
   a file-scope device array);
 * ``cf_mlp.cu``: the learned initial guess (tcgen05 BF16 GEMMs, TMA) and
-  its training kernels.
+  its training kernels;
+* ``cf_metrics.cu``: the wavy-wall metric generator (no FMA contraction).
 
 Usage: ``python -m channel_flow_gb300.build [--verbose] [--ptxas]``
 """
@@ -65,6 +66,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
         ("cf_noalloc.cu", "cf_noalloc.o", ["-DCF_NS=cf_noalloc", "--fmad=false"]),
         ("cf_mlp.cu", "cf_mlp.o", []),
+        ("cf_metrics.cu", "cf_metrics.o", ["--fmad=false"]),
     ]
 
     def cc(u):
@@ -75,7 +77,7 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
             raise RuntimeError(f"nvcc failed ({src} {' '.join(extra)}):\n{r.stderr[-6000:]}")
         return r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=5) as ex:
+    with cf.ThreadPoolExecutor(max_workers=6) as ex:
         logs = list(ex.map(cc, units))
     if verbose or ptxas:
         for log in logs:

@@ -217,6 +217,33 @@ int cf_Jacobian_w(cf_ctx *ctx, int myid, double **arrays10);
  * 9 cell metrics (read for the wall rows) */
 int cf_Jacobian_v(cf_ctx *ctx, int myid, double **arrays20);
 
+/* Metrics of a channel whose lower wall undulates in x, y_w(x) =
+ * amplitude * sin(2 pi x / wavelength), with the upper wall flat at y =
+ * height and the tanh wall-normal stretching of Jacobian.cpp:73-84 (the
+ * reference builds flat-wall metrics only: Grid.cpp:49-141, Jacobian*.cpp).
+ * conservative = 1 forms dy/dxi and dy/deta from differences of the mapping
+ * half a spacing to each side, so face values are differences between cell
+ * corners and the finite-volume divergence of a constant flux vanishes to
+ * rounding; 0 uses the analytic derivatives (amplitude 0 then gives the
+ * reference's flat-wall values).  Needs |amplitude| < height / 2. */
+typedef struct {
+    double amplitude, wavelength;
+    double stretching;          /* gamma of the tanh stretching */
+    int conservative;
+} cf_wavy_wall;
+
+enum { CF_AT_CELL = 0, CF_AT_XFACE = 1, CF_AT_YFACE = 2, CF_AT_ZFACE = 3 };
+
+/* J and xidx, xidy, xidz, etdx, etdy, etdz, ztdx, ztdy, ztdz (device arrays
+ * in the reference layout, every index written) at the cells or one face
+ * set, in the reference's face indexing (x face between cells i and i+1 at
+ * [i][j-1][k-1], and so on).  Stream-ordered; no allocation. */
+int cf_wavy_metrics(const cf_grid *g, void *cuda_stream, const cf_wavy_wall *wall, int where,
+                    double *const *J_and_metrics10);
+/* cell-centre y (Y_point, read by Filter) with the ghost rows of
+ * Grid.cpp:49-108 taken about the local wall */
+int cf_wavy_y_point(const cf_grid *g, void *cuda_stream, const cf_wavy_wall *wall, double *Y_point);
+
 
 /* ------------------------------------------------------------------ */
 /* reductions and IO around the step (FP64 in every precision mode)      */
