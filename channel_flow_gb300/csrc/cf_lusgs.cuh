@@ -161,13 +161,20 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     const size_t fy = d.ix(i - 1, j, k - 1), fz = d.ix(i - 1, j - 1, k);
     const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
     T Rk[5];
+#ifdef CF_FAST_MATH
+    const double rdt2 = 0.5 / dt;     // one FP64 division per cell instead of five
+#endif
 #pragma unroll
     for (int n = 0; n < 5; n++) {
         // the BDF2 time term combines three nearly equal FP64 states: it is
         // formed in FP64 in every build (the same operations as the
         // reference's expression when T is double) and only then rounded,
         // so an FP32 build keeps the digits that the difference resolves
+#ifdef CF_FAST_MATH
+        T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) * rdt2);
+#else
         T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) / (2.0 * dt));
+#endif
         T Rf = -((T(a.Fx[n][fx]) - T(a.Fx[n][f0])) / dXI + (T(a.Fy[n][fy]) - T(a.Fy[n][f0])) / dET +
                  (T(a.Fz[n][fz]) - T(a.Fz[n][f0])) / dZT);
         Rk[n] = Rp + Rf;

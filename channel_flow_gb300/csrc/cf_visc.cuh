@@ -12,6 +12,22 @@
 
 namespace CF_NS {
 
+// the primitive scratch holds the compute type: FP64, or FP32 in the FP32
+// build (the FP64 allocation reinterpreted), so the face kernel's many
+// neighbour reads need no FP64 -> FP32 conversion (a conversion issues to
+// GB300's FP64 pipe, 1/64 of the FP32 rate)
+__device__ __forceinline__ void prim_st(double *p, size_t q, double v) { p[q] = v; }
+__device__ __forceinline__ void prim_st(double *p, size_t q, float v) { reinterpret_cast<float *>(p)[q] = v; }
+template <typename T>
+__device__ __forceinline__ T prim_ld(const double *p, size_t q);
+template <>
+__device__ __forceinline__ double prim_ld<double>(const double *p, size_t q) { return p[q]; }
+template <>
+__device__ __forceinline__ float prim_ld<float>(const double *p, size_t q)
+{
+    return reinterpret_cast<const float *>(p)[q];
+}
+
 template <typename T>
 __global__ void k_visc_prim(cf_dims d, cf_visc_args a, size_t n)
 {
@@ -26,10 +42,10 @@ __global__ void k_visc_prim(cf_dims d, cf_visc_args a, size_t n)
     T Jq = T(a.J[q]);
     T P = (T(a.U[4][q]) - T(0.5) * rho * VV) * (K - T(1)) * Jq;
     T Tt = P / (rho * R) / Jq;
-    a.prim[0][q] = double(U);
-    a.prim[1][q] = double(V);
-    a.prim[2][q] = double(W);
-    a.prim[3][q] = double(Tt);
+    prim_st(a.prim[0], q, U);
+    prim_st(a.prim[1], q, V);
+    prim_st(a.prim[2], q, W);
+    prim_st(a.prim[3], q, Tt);
 }
 
 template <typename T>
@@ -44,7 +60,8 @@ struct vcell {
 template <typename T>
 __device__ __forceinline__ vcell<T> ld(const cf_visc_args &a, size_t q)
 {
-    return vcell<T>{T(a.prim[0][q]), T(a.prim[1][q]), T(a.prim[2][q]), T(a.prim[3][q])};
+    return vcell<T>{prim_ld<T>(a.prim[0], q), prim_ld<T>(a.prim[1], q), prim_ld<T>(a.prim[2], q),
+                    prim_ld<T>(a.prim[3], q)};
 }
 
 // one-sided difference c - n (Viscous_terms.cpp:400-415)
