@@ -385,7 +385,10 @@ int cf_X_periodic(cf_ctx *c, int, double *U1_, double *U2_, double *U3_, double 
 // ---------------------------------------------------------------------------
 // fluxes
 
-static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double *const *p32)
+// reuse_shadow: the FP32 copies of U and J made by the previous FP32 flux
+// call are still current (the step driver's y and z fluxes after x)
+static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double *const *p32,
+                       bool reuse_shadow = false)
 {
     if (!c) return CF_ERR_ARG;
     // arrays 5..14 (ML/MR) are the reference's scratch and are not needed
@@ -409,8 +412,16 @@ static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double
         a.wz[0] = wz;
         a.wz[1] = wz + c->d.total();
     }
+    if (kprec(c) == 1) {
+        // FP32: the stencils read FP32 copies of U, J, 1/J (7 fields)
+        double *sh = scratch(c, "flux_f32", 4);
+        if (!sh) return fail(c, CF_ERR_NOMEM, "%s: scratch allocation failed", who);
+        if (!a.J && dir != 0) return fail(c, CF_ERR_ARG, "%s: J is NULL", who);
+        return cuda_check(c, cf_fast::flux_f32(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow, dir, limited,
+                                               c->stream), who);
+    }
     cudaError_t e = exact(c) ? cf_exact::flux(c->d, a, dir, limited, 0, c->stream)
-                             : cf_fast::flux(c->d, a, dir, limited, kprec(c), c->stream);
+                             : cf_fast::flux(c->d, a, dir, limited, 0, c->stream);
     return cuda_check(c, e, who);
 }
 
@@ -1121,7 +1132,8 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
             p32[31] = f->Ep[dir];
             static const char *names[2][3] = {{"Flux_X", "Flux_Y", "Flux_Z"},
                                               {"Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter"}};
-            if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32)) return rc;
+            if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32, dir > 0))
+                return rc;
         }
         if (int rc = cf_Viscous_terms(c, 0, visc)) return rc;
         if (int rc = cf_Dual_time_stepping(c, 0, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr,

@@ -65,40 +65,40 @@ __device__ __forceinline__ T right5(T iiu, T iu, T u, T ui, T uii)
 }
 
 // linear states of the unlimited scheme (Flux_X.cpp:108-122, 138-162)
-template <typename T>
-__device__ __forceinline__ T lin5L(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T lin5L(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T temp = T(1.) / (T(2) / T(J[q - 2 * s]) - T(13) / T(J[q - s]) + T(47) / T(J[q]) + T(27) / T(J[q + s]) - T(3) / T(J[q + 2 * s]));
     return temp * (T(2) * T(U[q - 2 * s]) - T(13) * T(U[q - s]) + T(47) * T(U[q]) + T(27) * T(U[q + s]) - T(3) * T(U[q + 2 * s]));
 }
-template <typename T>
-__device__ __forceinline__ T lin5R(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T lin5R(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T temp = T(1.) / (T(-3) / T(J[q - 2 * s]) + T(27) / T(J[q - s]) + T(47) / T(J[q]) - T(13) / T(J[q + s]) + T(2) / T(J[q + 2 * s]));
     return temp * (T(-3) * T(U[q - 2 * s]) + T(27) * T(U[q - s]) + T(47) * T(U[q]) - T(13) * T(U[q + s]) + T(2) * T(U[q + 2 * s]));
 }
-template <typename T>
-__device__ __forceinline__ T lin3L(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T lin3L(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T temp = T(1.) / (T(-1) / T(J[q - s]) + T(5) / T(J[q]) + T(2) / T(J[q + s]));
     return temp * (-T(U[q - s]) + T(5) * T(U[q]) + T(2) * T(U[q + s]));
 }
-template <typename T>
-__device__ __forceinline__ T lin3R(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T lin3R(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T temp = T(1.) / (T(2) / T(J[q - s]) + T(5) / T(J[q]) - T(1) / T(J[q + s]));
     return temp * (T(2) * T(U[q - s]) + T(5) * T(U[q]) - T(U[q + s]));
 }
 // two-cell average of cells q and q+s (Flux_X.cpp:138-144)
-template <typename T>
-__device__ __forceinline__ T avg2(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T avg2(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T temp = T(1.) / (T(1) / T(J[q]) + T(1) / T(J[q + s]));
     return temp * (T(U[q]) + T(U[q + s]));
 }
 // same pair taken high cell first (Flux_Y.cpp:206-219)
-template <typename T>
-__device__ __forceinline__ T avg2hi(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T avg2hi(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T temp = T(1.) / (T(1) / T(J[q]) + T(1) / T(J[q - s]));
     return temp * (T(U[q]) + T(U[q - s]));
@@ -113,8 +113,8 @@ __device__ __forceinline__ T avg2hi(const double *U, const double *J, size_t q, 
 // cR = (i+1, j+1, k+1);  z: cL = (i+1, j+1, k), cR = (i+1, j+1, k+1).
 
 // Flux_X_limiter.cpp:113-341: 3rd order where the cell index is <= 3 or >= gend
-template <typename T>
-__device__ __forceinline__ void states_x_limited(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void states_x_limited(const cf_dims &d, const A &a, int i, int j,
                                                  int k, T *mL, T *mR)
 {
     const ptrdiff_t s = (ptrdiff_t)d.plane();
@@ -124,7 +124,7 @@ __device__ __forceinline__ void states_x_limited(const cf_dims &d, const cf_flux
     const bool hi3 = (i + 1 <= 3) || (i + 1 >= d.gend);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        const double *U = a.U[n];
+        const auto *U = a.U[n];
         if (lo3) mL[n] = left3<T, 1>(T(U[qL - s]), T(U[qL]), T(U[qL + s])) * jf;
         else mL[n] = left5<T, 1>(T(U[qL - 2 * s]), T(U[qL - s]), T(U[qL]), T(U[qL + s]), T(U[qL + 2 * s])) * jf;
         if (hi3) mR[n] = right3<T>(T(U[qR - s]), T(U[qR]), T(U[qR + s])) * jf;
@@ -137,16 +137,16 @@ __device__ __forceinline__ void states_x_limited(const cf_dims &d, const cf_flux
 // reference's jL/jR there are uninitialised, here they are the face J_v, as
 // in the interior branch.  Face 1 takes its left state and face ny its right
 // state from the wall averages (Flux_Y_limiter.cpp:365-477).
-template <typename T>
-__device__ __forceinline__ T ywall_var1_left(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T ywall_var1_left(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T iu = T(U[q - s]), u = T(U[q]), ui = T(U[q + s]);
     T rL = (ui - u) / ((u - iu) + T(0.0000001));
     T m = lim3(rL);
     return (u * T(J[q]) + T(0.5) * rmax(T(0), m) * (u - iu));
 }
-template <typename T>
-__device__ __forceinline__ T ywall_var1_right(const double *U, const double *J, size_t q, ptrdiff_t s)
+template <typename T, typename SP>
+__device__ __forceinline__ T ywall_var1_right(const SP *U, const SP *J, size_t q, ptrdiff_t s)
 {
     T iu = T(U[q - s]), u = T(U[q]), ui = T(U[q + s]);
     T rR = (u - iu) / ((ui - u) + T(0.0000001));
@@ -154,8 +154,8 @@ __device__ __forceinline__ T ywall_var1_right(const double *U, const double *J, 
     return (u * T(J[q]) - T(0.5) * rmax(T(0), m) * (ui - u));
 }
 
-template <typename T>
-__device__ __forceinline__ void states_y_limited(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void states_y_limited(const cf_dims &d, const A &a, int i, int j,
                                                  int k, T *mL, T *mR)
 {
     const ptrdiff_t s = d.Zm;
@@ -175,7 +175,7 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const cf_flux
     } else {
 #pragma unroll
         for (int n = 0; n < 5; n++) {
-            const double *U = a.U[n];
+            const auto *U = a.U[n];
             mL[n] = left5<T, 1>(T(U[qL - 2 * s]), T(U[qL - s]), T(U[qL]), T(U[qL + s]), T(U[qL + 2 * s])) * jf;
         }
     }
@@ -194,7 +194,7 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const cf_flux
     } else {
 #pragma unroll
         for (int n = 0; n < 5; n++) {
-            const double *U = a.U[n];
+            const auto *U = a.U[n];
             mR[n] = right5<T>(T(U[qR - 2 * s]), T(U[qR - s]), T(U[qR]), T(U[qR + s]), T(U[qR + 2 * s])) * jf;
         }
     }
@@ -204,29 +204,29 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const cf_flux
 // (average, linear 3rd order); interior cells k = 3..nz-1 the limited states
 // scaled by 1/sum(w/J) with the reference's unnormalised weights, and the
 // 3rd-order branch where k >= ny (the reference compares with the y extent).
-template <typename T>
-__device__ __forceinline__ T zjL5(const double *J, size_t q)
+template <typename T, typename SP>
+__device__ __forceinline__ T zjL5(const SP *J, size_t q)
 {
     return T(1.) / (T(2) / T(J[q - 2]) - T(13) / T(J[q - 1]) + T(47) / T(J[q]) + T(27) / T(J[q + 1]) - T(3) / T(J[q + 2]));
 }
-template <typename T>
-__device__ __forceinline__ T zjR5(const double *J, size_t q)
+template <typename T, typename SP>
+__device__ __forceinline__ T zjR5(const SP *J, size_t q)
 {
     return T(1.) / (T(-3) / T(J[q - 2]) + T(27) / T(J[q - 1]) + T(47) / T(J[q]) - T(13) / T(J[q + 1]) + T(2) / T(J[q + 2]));
 }
-template <typename T>
-__device__ __forceinline__ T zjL3(const double *J, size_t q)
+template <typename T, typename SP>
+__device__ __forceinline__ T zjL3(const SP *J, size_t q)
 {
     return T(1.) / (T(-1) / T(J[q - 1]) + T(5) / T(J[q]) + T(2) / T(J[q + 1]));
 }
-template <typename T>
-__device__ __forceinline__ T zjR3(const double *J, size_t q)
+template <typename T, typename SP>
+__device__ __forceinline__ T zjR3(const SP *J, size_t q)
 {
     return T(1.) / (T(2) / T(J[q - 1]) + T(5) / T(J[q]) - T(1) / T(J[q + 1]));
 }
 
-template <typename T>
-__device__ __forceinline__ void states_z_limited(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void states_z_limited(const cf_dims &d, const A &a, int i, int j,
                                                  int k, T *mL, T *mR)
 {
     const int nz = d.nz, ny = d.ny;
@@ -247,7 +247,7 @@ __device__ __forceinline__ void states_z_limited(const cf_dims &d, const cf_flux
         T jl = T(a.wz[0][qL]);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
-            const double *U = a.U[n];
+            const auto *U = a.U[n];
             mL[n] = left5<T, -1>(T(U[qL - 2]), T(U[qL - 1]), T(U[qL]), T(U[qL + 1]), T(U[qL + 2])) * jl;
         }
     }
@@ -268,15 +268,15 @@ __device__ __forceinline__ void states_z_limited(const cf_dims &d, const cf_flux
         T jr = T(a.wz[1][qR]);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
-            const double *U = a.U[n];
+            const auto *U = a.U[n];
             mR[n] = right5<T>(T(U[qR - 2]), T(U[qR - 1]), T(U[qR]), T(U[qR + 1]), T(U[qR + 2])) * jr;
         }
     }
 }
 
 // Flux_X.cpp:102-215 (5-point for cells 4..gend-1; seam rows 2, 3, gend)
-template <typename T>
-__device__ __forceinline__ void states_x_linear(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void states_x_linear(const cf_dims &d, const A &a, int i, int j,
                                                 int k, T *mL, T *mR)
 {
     const ptrdiff_t s = (ptrdiff_t)d.plane();
@@ -284,7 +284,7 @@ __device__ __forceinline__ void states_x_linear(const cf_dims &d, const cf_flux_
     const size_t qL = d.ix(i, j + 1, k + 1), qR = d.ix(i + 1, j + 1, k + 1);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        const double *U = a.U[n];
+        const auto *U = a.U[n];
         if (i == 2) mL[n] = avg2<T>(U, a.J, qL, s);
         else if (i == 3 || i == gend) mL[n] = lin3L<T>(U, a.J, qL, s);
         else mL[n] = lin5L<T>(U, a.J, qL, s);
@@ -295,8 +295,8 @@ __device__ __forceinline__ void states_x_linear(const cf_dims &d, const cf_flux_
 }
 
 // Flux_Y.cpp:100-240 (5-point for cells 4..ny-2; rows 1, 2, 3, ny-1, ny)
-template <typename T>
-__device__ __forceinline__ void states_y_linear(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void states_y_linear(const cf_dims &d, const A &a, int i, int j,
                                                 int k, T *mL, T *mR)
 {
     const ptrdiff_t s = d.Zm;
@@ -304,7 +304,7 @@ __device__ __forceinline__ void states_y_linear(const cf_dims &d, const cf_flux_
     const size_t qL = d.ix(i + 1, j, k + 1), qR = d.ix(i + 1, j + 1, k + 1);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        const double *U = a.U[n];
+        const auto *U = a.U[n];
         if (j == 1 || j == 2) mL[n] = avg2<T>(U, a.J, qL, s);
         else if (j == 3 || j == ny - 1) mL[n] = lin3L<T>(U, a.J, qL, s);
         else if (j == ny) mL[n] = avg2hi<T>(U, a.J, qL, s);
@@ -318,15 +318,15 @@ __device__ __forceinline__ void states_y_linear(const cf_dims &d, const cf_flux_
 }
 
 // Flux_Z.cpp:104-300 (5-point for cells 3..nz-1; rows 1, 2, nz)
-template <typename T>
-__device__ __forceinline__ void states_z_linear(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void states_z_linear(const cf_dims &d, const A &a, int i, int j,
                                                 int k, T *mL, T *mR)
 {
     const int nz = d.nz;
     const size_t qL = d.ix(i + 1, j + 1, k), qR = d.ix(i + 1, j + 1, k + 1);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        const double *U = a.U[n];
+        const auto *U = a.U[n];
         if (k == 1) mL[n] = avg2<T>(U, a.J, qL, 1);
         else if (k == 2 || k == nz) mL[n] = lin3L<T>(U, a.J, qL, 1);
         else mL[n] = lin5L<T>(U, a.J, qL, 1);
@@ -530,8 +530,11 @@ __device__ __forceinline__ void flux_roe(const T *mL, const T *mR, const T *m, i
 namespace CF_NS {
 
 // One thread per face of the box; DIR 0/1/2, LIMITED selects the scheme.
-template <int DIR, bool LIMITED, typename T>
-__global__ void __launch_bounds__(256) k_flux(cf_dims d, cf_flux_args a, cf_box b)
+// A is cf_flux_args (FP64 cell arrays) or, in the FP32 build,
+// cf_flux_args_f (FP32 copies of U, J and 1/J made once per call, so the
+// stencil reads convert nothing; the face arrays stay FP64).
+template <int DIR, bool LIMITED, typename T, typename A = cf_flux_args>
+__global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     T mL[5], mR[5], m[9], F[6];
@@ -639,5 +642,65 @@ cudaError_t launch_flux(const cf_dims &d, const cf_flux_args &a, int dir, bool l
     }
     return cudaGetLastError();
 }
+
+
+#ifdef CF_WITH_FLOAT
+// FP32 copies of the cell arrays the stencils read: U1..U5, J and 1/J over
+// every index of the array (one FP64 -> FP32 conversion per value instead
+// of one per stencil read)
+__global__ void __launch_bounds__(256) k_flux_shadow(size_t n, cf_ptr5 U, const double *__restrict__ J, float *u0,
+                                                     float *u1, float *u2, float *u3, float *u4, float *jf,
+                                                     float *ij)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    u0[q] = float(U.p[0][q]);
+    u1[q] = float(U.p[1][q]);
+    u2[q] = float(U.p[2][q]);
+    u3[q] = float(U.p[3][q]);
+    u4[q] = float(U.p[4][q]);
+    if (J) {
+        const float j = float(J[q]);
+        jf[q] = j;
+        ij[q] = 1.0f / j;
+    }
+}
+
+// FP32 fluxes from the FP32 copies in sh (7 fields: U1..U5, J, 1/J);
+// convert = false reuses copies made by an earlier call for the same U, J
+inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, float *sh, bool convert, int dir,
+                                   bool limited, cudaStream_t s)
+{
+    const size_t n = d.total();
+    if (convert) {
+        cf_ptr5 U;
+        for (int v = 0; v < 5; v++) U.p[v] = const_cast<double *>(a.U[v]);
+        k_flux_shadow<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, U, a.J, sh, sh + n, sh + 2 * n, sh + 3 * n,
+                                                                  sh + 4 * n, sh + 5 * n, sh + 6 * n);
+    }
+    cf_flux_args_f fa;
+    for (int v = 0; v < 5; v++) fa.U[v] = sh + v * n;
+    fa.J = sh + 5 * n;
+    fa.wz[0] = sh + 6 * n;
+    fa.wz[1] = nullptr;
+    fa.Jf = a.Jf;
+    for (int v = 0; v < 9; v++) fa.m[v] = a.m[v];
+    fa.Ep = a.Ep;
+    for (int v = 0; v < 5; v++) fa.F[v] = a.F[v];
+    cf_box b = flux_box(d, dir);
+    if (b.ni == 0 || b.nj == 0 || b.nk == 0) return cudaGetLastError();
+    dim3 g = box_grid(b), t = box_block();
+    if (limited) {
+        if (dir == 0) k_flux<0, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+        else if (dir == 1) k_flux<1, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+        else k_flux<2, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+    } else {
+        if (dir == 0) k_flux<0, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+        else if (dir == 1) k_flux<1, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+        else k_flux<2, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+    }
+    return cudaGetLastError();
+}
+#endif
 
 }  // namespace CF_NS

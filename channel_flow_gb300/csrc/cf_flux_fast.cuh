@@ -94,16 +94,16 @@ __device__ __forceinline__ T fast_right(const T *w, bool o3)
     return w[2] - T(0.5) * phi * Dp;
 }
 
-template <typename T>
-__device__ __forceinline__ void load5(const double *U, size_t qc, ptrdiff_t s, T *u)
+template <typename T, typename SP>
+__device__ __forceinline__ void load5(const SP *U, size_t qc, ptrdiff_t s, T *u)
 {
 #pragma unroll
     for (int t = 0; t < 5; t++) u[t] = T(U[qc + (t - 2) * s]);
 }
 
 // loads the cells the selected orders need (others stay 0)
-template <typename T>
-__device__ __forceinline__ void load6(const double *U, size_t qc, ptrdiff_t s, bool lo3, bool hi3, T *u)
+template <typename T, typename SP>
+__device__ __forceinline__ void load6(const SP *U, size_t qc, ptrdiff_t s, bool lo3, bool hi3, T *u)
 {
     u[0] = lo3 ? T(0) : T(U[qc - 2 * s]);
     u[1] = T(U[qc - s]);
@@ -113,8 +113,8 @@ __device__ __forceinline__ void load6(const double *U, size_t qc, ptrdiff_t s, b
     u[5] = hi3 ? T(0) : T(U[qc + 3 * s]);
 }
 
-template <typename T>
-__device__ __forceinline__ void fast_states_x_limited(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void fast_states_x_limited(const cf_dims &d, const A &a, int i, int j,
                                                       int k, T *mL, T *mR)
 {
     const ptrdiff_t s = (ptrdiff_t)d.plane();
@@ -130,8 +130,8 @@ __device__ __forceinline__ void fast_states_x_limited(const cf_dims &d, const cf
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A &a, int i, int j,
                                                       int k, T *mL, T *mR)
 {
     const ptrdiff_t s = d.Zm;
@@ -196,8 +196,8 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const cf
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A &a, int i, int j,
                                                       int k, T *mL, T *mR)
 {
     const int nz = d.nz, ny = d.ny;
@@ -205,7 +205,7 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf
     const bool limL = k >= 3 && k <= nz - 1;          // cell k takes a limited state
     const bool limR = k + 1 >= 3 && k + 1 <= nz - 1;  // cell k+1 takes a limited state
     const bool lo3 = k >= ny, hi3 = k + 1 >= ny;      // the reference compares with the y extent
-    const double *iJp = a.wz[0];      // 1/J per cell
+    const auto *iJp = a.wz[0];      // 1/J per cell
     if (limL && limR) {
         T iJ[6];
         iJ[0] = lo3 ? T(0) : T(iJp[qL - 2]);
@@ -265,8 +265,8 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const cf
 }
 
 // linear 5-point states of the unlimited scheme with shared 1/J (Flux_X.cpp:108-122)
-template <typename T>
-__device__ __forceinline__ void fast_lin_pair(const cf_flux_args &a, size_t qc, ptrdiff_t s, T *mL, T *mR)
+template <typename T, typename A>
+__device__ __forceinline__ void fast_lin_pair(const A &a, size_t qc, ptrdiff_t s, T *mL, T *mR)
 {
     T iJ[6];
 #pragma unroll
@@ -275,7 +275,7 @@ __device__ __forceinline__ void fast_lin_pair(const cf_flux_args &a, size_t qc, 
     const T tr = T(1.) / (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        const double *U = a.U[n];
+        const auto *U = a.U[n];
         T u0 = T(U[qc - 2 * s]), u1 = T(U[qc - s]), u2 = T(U[qc]), u3 = T(U[qc + s]), u4 = T(U[qc + 2 * s]),
           u5 = T(U[qc + 3 * s]);
         mL[n] = tl * (T(2) * u0 - T(13) * u1 + T(47) * u2 + T(27) * u3 - T(3) * u4);
@@ -283,8 +283,8 @@ __device__ __forceinline__ void fast_lin_pair(const cf_flux_args &a, size_t qc, 
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void fast_states_x_linear(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void fast_states_x_linear(const cf_dims &d, const A &a, int i, int j,
                                                      int k, T *mL, T *mR)
 {
     if (i <= 3 || i >= d.gend - 1) {
@@ -294,8 +294,8 @@ __device__ __forceinline__ void fast_states_x_linear(const cf_dims &d, const cf_
     fast_lin_pair<T>(a, d.ix(i, j + 1, k + 1), (ptrdiff_t)d.plane(), mL, mR);
 }
 
-template <typename T>
-__device__ __forceinline__ void fast_states_y_linear(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void fast_states_y_linear(const cf_dims &d, const A &a, int i, int j,
                                                      int k, T *mL, T *mR)
 {
     if (j <= 3 || j >= d.ny - 2) {
@@ -305,8 +305,8 @@ __device__ __forceinline__ void fast_states_y_linear(const cf_dims &d, const cf_
     fast_lin_pair<T>(a, d.ix(i + 1, j, k + 1), d.Zm, mL, mR);
 }
 
-template <typename T>
-__device__ __forceinline__ void fast_states_z_linear(const cf_dims &d, const cf_flux_args &a, int i, int j,
+template <typename T, typename A>
+__device__ __forceinline__ void fast_states_z_linear(const cf_dims &d, const A &a, int i, int j,
                                                      int k, T *mL, T *mR)
 {
     if (k <= 2 || k >= d.nz - 1) {

@@ -63,6 +63,17 @@ struct cf_flux_args {
     double *wz[2];        // scratch of the z limiter: per-cell 1/sum(w/J) of the left and right states
 };
 
+// the FP32 flux kernels' view: FP32 copies of the cell arrays, FP64 face arrays
+struct cf_flux_args_f {
+    const float *U[5];
+    const float *J;
+    const double *Jf;
+    const double *m[9];
+    const double *Ep;
+    double *F[5];
+    const float *wz[2];   // wz[0]: 1/J per cell
+};
+
 struct cf_visc_args {
     const double *U[5];
     double *vF[4];

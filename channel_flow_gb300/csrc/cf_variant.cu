@@ -44,9 +44,22 @@ cudaError_t z_periodic(const cf_dims &d, const cf_ptr5 &U, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// FP64 fluxes; the FP32 ones go through flux_f32 (they need the FP32 copies)
 cudaError_t flux(const cf_dims &d, const cf_flux_args &a, int dir, bool limited, int prec, cudaStream_t s)
 {
-    return CF_DISPATCH(prec, launch_flux<double>(d, a, dir, limited, s), launch_flux<float>(d, a, dir, limited, s));
+    return prec == 1 ? cudaErrorNotSupported : launch_flux<double>(d, a, dir, limited, s);
+}
+
+// shadow: 7 FP32 fields (U1..U5, J, 1/J) of d.total() values each
+cudaError_t flux_f32(const cf_dims &d, const cf_flux_args &a, float *shadow, bool convert, int dir, bool limited,
+                     cudaStream_t s)
+{
+#ifdef CF_WITH_FLOAT
+    return launch_flux_f32(d, a, shadow, convert, dir, limited, s);
+#else
+    (void)d; (void)a; (void)shadow; (void)convert; (void)dir; (void)limited; (void)s;
+    return cudaErrorNotSupported;
+#endif
 }
 
 cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStream_t s)
