@@ -279,9 +279,11 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess physical-step comparison")
     ap.add_argument("--no-wavy", action="store_true", help="skip the 512x256x384 wavy-wall measurement")
-    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs"],
+    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs", "mlp"],
                     help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
-                         "(one LU-SGS pseudo-iteration per step, for profiling)")
+                         "(one LU-SGS pseudo-iteration per step, for profiling); mlp: the learned guess's "
+                         "tensor-core GEMMs on --mlp-rows feature rows")
+    ap.add_argument("--mlp-rows", type=int, default=2097152, help="rows (cells) of the --step mlp GEMMs")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
 
@@ -318,6 +320,13 @@ def main():
 
     import torch
     import channel_flow_gb300 as cf
+
+    if args.step == "mlp":
+        torch.cuda.set_device(local)
+        r = mlp_gemms(torch, args.mlp_rows, max(2, args.steps), max(1, args.warmup))
+        if rank == 0:
+            print(json.dumps(r))
+        return 0
 
     dist = None
     if world > 1:
@@ -602,6 +611,58 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=12, evals=3,
     return out
 
 
+def mlp_gemms(torch, rows, steps=5, warmup=2):
+    """The learned guess's six tcgen05 GEMMs (forward: features x W1,
+    H1 x W2, H2 x W3; backward: the activation gradients and the weight
+    gradients, whose reduction dimension is the rows) on `rows` random
+    feature rows: CUDA-event time per GEMM and its TFLOP/s (2 M N K per
+    product) against the measured BF16 peak."""
+    from channel_flow_gb300 import mlp
+    net = mlp.LearnedGuess(capacity=rows, seed=0, batch=rows)
+    M = net.cap
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(SEED)
+    net.X.copy_(torch.randn(M, mlp.K1, generator=gen, device="cuda").to(torch.bfloat16))
+    net.T.copy_(torch.randn(M, mlp.N3, generator=gen, device="cuda"))
+    H, K1, N3, K3 = mlp.H, mlp.K1, mlp.N3, mlp.K3
+    b1, b2, b3 = net.view("b1"), net.view("b2"), net.view("b3")
+    g = net.g
+    prods = [
+        ("fwd_L1", lambda: net.gemm(net.X, net.W1b, M, H, K1, mlp.EPI_SILU, b1, net.H1, net.Z1, H), M, H, K1),
+        ("fwd_L2", lambda: net.gemm(net.H1, net.W2b, M, H, H, mlp.EPI_SILU, b2, net.H2, net.Z2, H), M, H, H),
+        ("fwd_L3", lambda: net.gemm(net.H2, net.W3b, M, N3, H, mlp.EPI_BIAS, b3, net.Y, None, N3), M, N3, H),
+        ("bwd_dH2", lambda: net.gemm(net.dY, net.W3p, M, H, K3, mlp.EPI_F32, None, net.dH, None, H), M, H, K3),
+        ("bwd_dH1", lambda: net.gemm(net.dZ2, net.W2T, M, H, H, mlp.EPI_F32, None, net.dH, None, H), M, H, H),
+        ("bwd_dW1", lambda: net.gemm(net.dZ1T, net.XT, H, K1, M, mlp.EPI_F32, None, net.view("W1", g), None, K1),
+         H, K1, M),
+    ]
+    # one full training step first, so that every operand holds data
+    net.step(M, M)
+    out = {"rows": M, "peak_bf16_tflops": None, "gemms": {}}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    peak = float(json.loads(pk.read_text())["bf16_tflops"]) if pk.exists() else 1900.0
+    out["peak_bf16_tflops"] = peak
+    for name, fn, m, n, k in prods:
+        for _ in range(warmup):
+            fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        tf = 2.0 * m * n * k / (ms * 1e-3) / 1e12
+        out["gemms"][name] = {"M": m, "N": n, "K": k, "ms": ms, "tflops": tf, "frac_of_peak": tf / peak}
+    net.check_device()
+    # the guess on all rows: features are not timed here; forward = the three products
+    out["forward_ms"] = sum(out["gemms"][k]["ms"] for k in ("fwd_L1", "fwd_L2", "fwd_L3"))
+    del net
+    torch.cuda.empty_cache()
+    return out
+
+
 def wavy_workload(ctx, g, torch, amplitude_over_h=0.05, wavelength_over_h=math.pi):
     """The benchmark channel with a wavy lower wall (amplitude 0.05 h,
     wavelength pi h: two waves over 2 pi h) and the conservative metrics of
@@ -669,6 +730,11 @@ def secondary(ctx, g, w, calls, stream, torch, args):
     for k, v in out.items():
         if "fp64" in v and "fp32" in v:
             v["physical_step_fp64_over_fp32"] = v["fp64"]["physical_step_s"] / v["fp32"]["physical_step_s"]
+    if not args.no_learned:
+        try:
+            out["mlp_gemm"] = mlp_gemms(torch, 2097152)
+        except Exception as exc:
+            out["mlp_gemm"] = {"error": repr(exc)}
     if not args.no_large and not args.no_learned:
         try:
             out["physical_step_to_tolerance"] = physical_step_to_tolerance(torch)

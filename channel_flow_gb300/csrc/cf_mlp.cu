@@ -26,7 +26,7 @@
 
 namespace cf_mlp {
 
-constexpr int BM = 128, BK = 64, STAGES = 4;
+constexpr int BM = 128, BK = 64;
 constexpr unsigned long long WAIT_NS = 2000000000ull;   // a wait gives up after two seconds
 
 enum { EPI_F32 = 0, EPI_BIAS_SILU_BF16 = 1, EPI_BIAS_F32 = 2 };
@@ -87,7 +87,11 @@ struct tmem_cols {
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 
-template <int BN>
+// STAGES: depth of the TMA ring.  Short reductions (the network's layers,
+// K <= 512) use two stages, so that three CTAs fit an SM and one CTA's
+// epilogue overlaps the others' loads; the long weight-gradient
+// reductions (K = rows) use four.
+template <int BN, int STAGES>
 __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUtensorMap tA,
                                                     const __grid_constant__ CUtensorMap tB, int M, int N, int K,
                                                     gemm_epi e, int *err)
@@ -257,18 +261,24 @@ static bool make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int bo
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+template <int BN, int STAGES>
+static cudaError_t launch_gemm_st(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K,
+                                  const gemm_epi &e, int *err, cudaStream_t s)
+{
+    constexpr size_t smem = (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 1024;
+    cudaError_t r = cudaFuncSetAttribute(k_gemm_tn<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (r != cudaSuccess) return r;
+    dim3 g((unsigned)(M / BM), (unsigned)(N / BN));
+    k_gemm_tn<BN, STAGES><<<g, 128, smem, s>>>(ta, tb, M, N, K, e, err);
+    return cudaGetLastError();
+}
+
 template <int BN>
 static cudaError_t launch_gemm(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K, const gemm_epi &e,
                                int *err, cudaStream_t s)
 {
-    constexpr size_t smem = (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 1024;
-    cudaError_t r = cudaFuncSetAttribute(k_gemm_tn<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (r != cudaSuccess) return r;
-    dim3 g((unsigned)(M / BM), (unsigned)(N / BN));
-    k_gemm_tn<BN><<<g, 128, smem, s>>>(ta, tb, M, N, K, e, err);
-    return cudaGetLastError();
+    return K <= 512 ? launch_gemm_st<BN, 2>(ta, tb, M, N, K, e, err, s) : launch_gemm_st<BN, 4>(ta, tb, M, N, K, e, err, s);
 }
-
 
 // ---------------------------------------------------------------------------
 // MLP data movement and training kernels (FP32 / BF16, device pointers)
