@@ -638,8 +638,9 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     const size_t fz = (size_t)w.ntiles * 5 * CF_WAVE_TI * CF_WAVE_TJ * T8;
     const size_t nl = (size_t)w.ntiles * 5 * cells * T8;
     const size_t flags = (((size_t)w.ntiles + 2) * sizeof(int) + 255) / 256 * 256;
+    const size_t part = (size_t)w.ntiles * 5 * sizeof(double);
     unsigned char *base = static_cast<unsigned char *>(
-        scratch_bytes(c, "lu_wave", 2 * pack + fx + fy + fz + nl + flags));
+        scratch_bytes(c, "lu_wave", 2 * pack + fx + fy + fz + nl + flags + part));
     if (!base) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: wavefront scratch allocation failed");
     w.packF = base;
     w.packB = base + pack;
@@ -651,6 +652,7 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     w.flags = reinterpret_cast<int *>(f);
     w.counter = w.flags + w.ntiles;
     w.err = w.flags + w.ntiles + 1;
+    w.partial = reinterpret_cast<double *>(f + flags);
     w.trace = nullptr;
     if (c->trace_tiles) {
         if (c->trace_tiles != (size_t)w.ntiles) {
@@ -701,8 +703,18 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, 0, s)
                                      : cf_fast::lu_wave_pack(d, a, w, dt, true, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
+        // FP32: the backward sweep also updates the state (FP64), copies
+        // NL <- NR and leaves per-tile norm partial sums; its blocks have
+        // FP64 issue slots to spare while they wait on their neighbours.
+        // The FP64 sweeps keep their FP64 pipe for the sweep itself.
+        const bool fuse = pr == 1;
+        if (!fuse) wb.partial = nullptr;
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, wb, false, 0, s)
                                      : cf_fast::lu_wave_sweep(a, wb, false, pr, s);
+        if (fuse) {
+            if (e == cudaSuccess) e = cf_fast::lu_wave_norm(d, w, c->er_dev, s);
+            return e;
+        }
     } else {
         if (e == cudaSuccess) e = ex ? cf_exact::lu_pack(d, a, pack, dt, 0, s) : cf_fast::lu_pack(d, a, pack, dt, pr, s);
         const int mlast = d.gend + d.ny + d.nz;

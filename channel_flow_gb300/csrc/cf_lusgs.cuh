@@ -488,9 +488,60 @@ __global__ void k_lu_copy(cf_dims d, cf_lu_args a, cf_box b)
     for (int v = 0; v < 5; v++) a.NL[v][q] = a.NR[v][q];
 }
 
-// primitive update and the squared-change arrays (Dual_time_stepping.cpp:
-// 1290-1326), FP64 in every precision mode; each block also writes its
-// partial sums of Residual^2 (the reference's Sum(Delta^2)^2 norm)
+// primitive update of one cell from its NR and the squared changes
+// (Dual_time_stepping.cpp:1290-1326), FP64 in every precision mode; r2
+// gets the squares of the five squared changes (the terms of the
+// reference's Sum(Delta^2)^2 norm)
+__device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_args &a, size_t q, const double *nr,
+                                               double *r2)
+{
+    const double K = d.K, Jq = a.J[q];
+    double rhoold = a.U_[0][q] * Jq;
+#ifdef CF_FAST_MATH
+    // FP64 with four divisions instead of ten (reciprocals of U1, J)
+    const double iu1 = 1.0 / a.U_[0][q], iJ = 1.0 / Jq;
+    double Uold = a.U_[1][q] * iu1;
+    double Vold = a.U_[2][q] * iu1;
+    double Wold = a.U_[3][q] * iu1;
+#else
+    double Uold = a.U_[1][q] / a.U_[0][q];
+    double Vold = a.U_[2][q] / a.U_[0][q];
+    double Wold = a.U_[3][q] / a.U_[0][q];
+#endif
+    double VVold = Uold * Uold + Vold * Vold + Wold * Wold;
+    double Pold = (a.U_[4][q] * Jq - 0.5 * rhoold * VVold) * (K - 1);
+    double Told = Pold / rhoold;
+    double P = Pold + nr[0] * Jq;
+    double U = Uold + nr[1] * Jq;
+    double V = Vold + nr[2] * Jq;
+    double W = Wold + nr[3] * Jq;
+    double Tt = Told + nr[4] * Jq;
+    double rho = P / Tt;
+#ifdef CF_FAST_MATH
+    const double rJ = rho * iJ;
+    a.U_[0][q] = rJ;
+    a.U_[1][q] = rJ * U;
+    a.U_[2][q] = rJ * V;
+    a.U_[3][q] = rJ * W;
+    a.U_[4][q] = (P * (1.0 / (K - 1)) + 0.5 * rho * (U * U + V * V + W * W)) * iJ;
+#else
+    a.U_[0][q] = rho / Jq;
+    a.U_[1][q] = rho * U / Jq;
+    a.U_[2][q] = rho * V / Jq;
+    a.U_[3][q] = rho * W / Jq;
+    a.U_[4][q] = (P / (K - 1) + 0.5 * rho * (U * U + V * V + W * W)) / Jq;
+#endif
+    double r[5] = {(P - Pold) * (P - Pold), (U - Uold) * (U - Uold), (V - Vold) * (V - Vold),
+                   (W - Wold) * (W - Wold), (Tt - Told) * (Tt - Told)};
+#pragma unroll
+    for (int n = 0; n < 5; n++) {
+        a.Res[n][q] = r[n];
+        r2[n] = r[n] * r[n];
+    }
+}
+
+// the update over the interior box; each block also writes its partial
+// sums of Residual^2
 __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_box b)
 {
     const int k = b.k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -499,49 +550,10 @@ __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_b
     double r2[5] = {0, 0, 0, 0, 0};
     if (k < b.k0 + b.nk && j < b.j0 + b.nj) {
         const size_t q = d.ix(i, j, k);
-        const double K = d.K, Jq = a.J[q];
-        double rhoold = a.U_[0][q] * Jq;
-#ifdef CF_FAST_MATH
-        // FP64 with four divisions instead of ten (reciprocals of U1, J)
-        const double iu1 = 1.0 / a.U_[0][q], iJ = 1.0 / Jq;
-        double Uold = a.U_[1][q] * iu1;
-        double Vold = a.U_[2][q] * iu1;
-        double Wold = a.U_[3][q] * iu1;
-#else
-        double Uold = a.U_[1][q] / a.U_[0][q];
-        double Vold = a.U_[2][q] / a.U_[0][q];
-        double Wold = a.U_[3][q] / a.U_[0][q];
-#endif
-        double VVold = Uold * Uold + Vold * Vold + Wold * Wold;
-        double Pold = (a.U_[4][q] * Jq - 0.5 * rhoold * VVold) * (K - 1);
-        double Told = Pold / rhoold;
-        double P = Pold + a.NR[0][q] * Jq;
-        double U = Uold + a.NR[1][q] * Jq;
-        double V = Vold + a.NR[2][q] * Jq;
-        double W = Wold + a.NR[3][q] * Jq;
-        double Tt = Told + a.NR[4][q] * Jq;
-        double rho = P / Tt;
-#ifdef CF_FAST_MATH
-        const double rJ = rho * iJ;
-        a.U_[0][q] = rJ;
-        a.U_[1][q] = rJ * U;
-        a.U_[2][q] = rJ * V;
-        a.U_[3][q] = rJ * W;
-        a.U_[4][q] = (P * (1.0 / (K - 1)) + 0.5 * rho * (U * U + V * V + W * W)) * iJ;
-#else
-        a.U_[0][q] = rho / Jq;
-        a.U_[1][q] = rho * U / Jq;
-        a.U_[2][q] = rho * V / Jq;
-        a.U_[3][q] = rho * W / Jq;
-        a.U_[4][q] = (P / (K - 1) + 0.5 * rho * (U * U + V * V + W * W)) / Jq;
-#endif
-        double r[5] = {(P - Pold) * (P - Pold), (U - Uold) * (U - Uold), (V - Vold) * (V - Vold),
-                       (W - Wold) * (W - Wold), (Tt - Told) * (Tt - Told)};
+        double nr[5];
 #pragma unroll
-        for (int n = 0; n < 5; n++) {
-            a.Res[n][q] = r[n];
-            r2[n] = r[n] * r[n];
-        }
+        for (int n = 0; n < 5; n++) nr[n] = a.NR[n][q];
+        lu_update_cell(d, a, q, nr, r2);
     }
     // block reduction in a fixed order (deterministic)
     __shared__ double sh[5][256];

@@ -121,6 +121,7 @@ struct cf_wave_args {
     int *err;                // bit 0: dependency wait ran out, bit 1: pack copy wait ran out
     long long *trace;        // optional: per tile 4 global-timer stamps (claimed, inputs ready,
                              // pack landed, done); NULL when tracing is off
+    double *partial;         // per tile: the 5 residual-norm partial sums of the fused update
 };
 
 struct cf_stat_args {
