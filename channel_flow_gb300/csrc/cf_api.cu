@@ -387,8 +387,10 @@ int cf_X_periodic(cf_ctx *c, int, double *U1_, double *U2_, double *U3_, double 
 
 // reuse_shadow: the FP32 copies of U and J made by the previous FP32 flux
 // call are still current (the step driver's y and z fluxes after x)
+// f32_out: in FP32 mode, write inF as FP32 values into their FP64 arrays
+// (only the step driver, whose own Dual_time_stepping reads them)
 static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double *const *p32,
-                       bool reuse_shadow = false)
+                       bool reuse_shadow = false, bool f32_out = false)
 {
     if (!c) return CF_ERR_ARG;
     // arrays 5..14 (ML/MR) are the reference's scratch and are not needed
@@ -406,6 +408,8 @@ static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double
     for (int n = 0; n < 5; n++) a.F[n] = R(c, p32[26 + n]);
     a.Ep = p32[31] ? R(c, p32[31]) : nullptr;
     a.wz[0] = a.wz[1] = nullptr;
+    a.f32_out = (f32_out && kprec(c) == 1) ? 1 : 0;
+    a.reserved = 0;
     if (dir == 2 && limited) {
         double *wz = scratch(c, "flux_zweights", 2);
         if (!wz) return fail(c, CF_ERR_NOMEM, "%s: scratch allocation failed", who);
@@ -446,7 +450,8 @@ CF_FLUX_ENTRY(Flux_Z, 2, false)
 // ---------------------------------------------------------------------------
 // viscous terms
 
-int cf_Viscous_terms(cf_ctx *c, int, double **p)
+// f32_io: in FP32 mode, LL/ML/NL and vF hold FP32 values (the step driver)
+static int viscous_common(cf_ctx *c, double **p, bool f32_io)
 {
     if (!c || !p) return CF_ERR_ARG;
     // read: U (0-4), J (9), face metric sets (19-48); written: vF (5-8),
@@ -472,10 +477,14 @@ int cf_Viscous_terms(cf_ctx *c, int, double **p)
     double *prim = scratch(c, "visc_prim", 4);
     if (!prim) return fail(c, CF_ERR_NOMEM, "Viscous_terms: scratch allocation failed");
     for (int n = 0; n < 4; n++) a.prim[n] = prim + (size_t)n * c->d.total();
+    a.f32_io = (f32_io && kprec(c) == 1) ? 1 : 0;
+    a.reserved = 0;
     cudaError_t e = exact(c) ? cf_exact::viscous(c->d, a, 0, c->stream)
                              : cf_fast::viscous(c->d, a, kprec(c), c->stream);
     return cuda_check(c, e, "Viscous_terms");
 }
+
+int cf_Viscous_terms(cf_ctx *c, int, double **p) { return viscous_common(c, p, false); }
 
 // ---------------------------------------------------------------------------
 // sensor
@@ -569,6 +578,8 @@ static int lu_args(cf_ctx *c, double **p, const char *who, cf_lu_args &a)
     a.J = R(c, p[15]);
     for (int n = 0; n < 9; n++) a.m[n] = R(c, p[16 + n]);
     for (int n = 0; n < 4; n++) a.vF[n] = R(c, p[40 + n]);
+    a.f32_rhs = 0;
+    a.reserved = 0;
     cf_dims &d = c->d;
     const size_t np = cf_fast::lu_partial_count(d);
     auto &e = c->scratch["lu_partial"];
@@ -764,8 +775,9 @@ static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, const cf_wa
     return CF_OK;
 }
 
-int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4,
-                          double *er5, int *Nijk, int *ijk, double **p)
+// f32_rhs: in FP32 mode, Fx/Fy/Fz and vF hold FP32 values (the step driver)
+static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,
+                      int *Nijk, int *ijk, double **p, bool f32_rhs)
 {
     if (!c || !p) return CF_ERR_ARG;
     // the plane tables are a fixed function of the grid; the context holds
@@ -777,6 +789,7 @@ int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er
     }
     cf_lu_args a;
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
+    a.f32_rhs = (f32_rhs && kprec(c) == 1) ? 1 : 0;
     double *pack = nullptr;
     cf_wave_args w{};
     if (c->lu_schedule == CF_LU_WAVEFRONT) {
@@ -817,6 +830,12 @@ int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er
     if (*err_host)
         return fail(c, CF_ERR_TIMEOUT, "Dual_time_stepping: a wavefront wait ran out (code %d)", *err_host);
     return CF_OK;
+}
+
+int cf_Dual_time_stepping(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4,
+                          double *er5, int *Nijk, int *ijk, double **p)
+{
+    return dts_common(c, deltaT, er1, er2, er3, er4, er5, Nijk, ijk, p, false);
 }
 
 int cf_DPLUSGS(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,
@@ -1123,6 +1142,10 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
     for (int n = 0; n < 9; n++) dts[16 + n] = f->cell_metric[n];
     for (int n = 0; n < 4; n++) dts[40 + n] = f->vF[n];
     double er[5] = {0, 0, 0, 0, 0};
+    // FP32: the fluxes, viscous terms and Dual_time_stepping of the loop
+    // pass the right-hand-side arrays as FP32 values (the caller's inF, vF,
+    // LL/ML/NL are the loop's own scratch here)
+    const bool f32_rhs = kprec(c) == 1;
     c->er_hist.clear();
     int it = 1;
     for (;; it++) {
@@ -1144,12 +1167,13 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
             p32[31] = f->Ep[dir];
             static const char *names[2][3] = {{"Flux_X", "Flux_Y", "Flux_Z"},
                                               {"Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter"}};
-            if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32, dir > 0))
+            if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32, dir > 0,
+                                     f32_rhs))
                 return rc;
         }
-        if (int rc = cf_Viscous_terms(c, 0, visc)) return rc;
-        if (int rc = cf_Dual_time_stepping(c, 0, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr,
-                                           nullptr, dts)) return rc;
+        if (int rc = viscous_common(c, visc, f32_rhs)) return rc;
+        if (int rc = dts_common(c, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr, nullptr, dts,
+                                f32_rhs)) return rc;
         for (int n = 0; n < 5; n++) {
             c->E[n] = std::max(c->E[n], er[n]);
             er[n] = er[n] / c->E[n];

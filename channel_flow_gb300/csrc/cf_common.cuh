@@ -23,6 +23,25 @@ template <typename T>
 __device__ __forceinline__ T rmax(T a, T b) { return (a > b) ? a : b; }
 
 
+// Arrays of the right-hand side that the step driver passes between its own
+// FP32 kernels (face fluxes, viscous face fluxes and divergence) can hold
+// FP32 values in their FP64 allocation (flag f32, warp-uniform): no FP64 ->
+// FP32 conversion, which issues to GB300's slow FP64 pipe, on either side.
+// In the FP64 kernels (T = double) the flag is ignored.
+template <typename T>
+__device__ __forceinline__ void rhs_put(double *p, size_t q, T v, int f32)
+{
+    if (sizeof(T) == 4 && f32) reinterpret_cast<float *>(p)[q] = float(v);
+    else p[q] = double(v);
+}
+template <typename T>
+__device__ __forceinline__ T rhs_get(const double *p, size_t q, int f32)
+{
+    if (sizeof(T) == 4 && f32) return T(reinterpret_cast<const float *>(p)[q]);
+    return T(p[q]);
+}
+
+
 #define CF_BOX_INDEX(b, i, j, k)                                    \
     const int k = (b).k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); \
     const int j = (b).j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y); \

@@ -575,16 +575,17 @@ __global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
     else
         flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), T(d.K), F);
 #endif
+    const int f32 = a.f32_out;
     if (DIR == 1 && (j == 1 || j == d.ny)) {
         // wall faces keep the pressure term of the normal momentum only
-        a.F[0][q] = 0;
-        a.F[1][q] = 0;
-        a.F[2][q] = double(F[5]);
-        a.F[3][q] = 0;
-        a.F[4][q] = 0;
+        rhs_put<T>(a.F[0], q, T(0), f32);
+        rhs_put<T>(a.F[1], q, T(0), f32);
+        rhs_put<T>(a.F[2], q, F[5], f32);
+        rhs_put<T>(a.F[3], q, T(0), f32);
+        rhs_put<T>(a.F[4], q, T(0), f32);
     } else {
 #pragma unroll
-        for (int n = 0; n < 5; n++) a.F[n][q] = double(F[n]);
+        for (int n = 0; n < 5; n++) rhs_put<T>(a.F[n], q, F[n], f32);
     }
 }
 
@@ -687,6 +688,7 @@ inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, floa
     for (int v = 0; v < 9; v++) fa.m[v] = a.m[v];
     fa.Ep = a.Ep;
     for (int v = 0; v < 5; v++) fa.F[v] = a.F[v];
+    fa.f32_out = a.f32_out;
     cf_box b = flux_box(d, dir);
     if (b.ni == 0 || b.nj == 0 || b.nk == 0) return cudaGetLastError();
     dim3 g = box_grid(b), t = box_block();

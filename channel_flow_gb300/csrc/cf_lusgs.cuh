@@ -175,15 +175,17 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
 #else
         T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) / (2.0 * dt));
 #endif
-        T Rf = -((T(a.Fx[n][fx]) - T(a.Fx[n][f0])) / dXI + (T(a.Fy[n][fy]) - T(a.Fy[n][f0])) / dET +
-                 (T(a.Fz[n][fz]) - T(a.Fz[n][f0])) / dZT);
+        const int f32 = a.f32_rhs;
+        T Rf = -((rhs_get<T>(a.Fx[n], fx, f32) - rhs_get<T>(a.Fx[n], f0, f32)) / dXI +
+                 (rhs_get<T>(a.Fy[n], fy, f32) - rhs_get<T>(a.Fy[n], f0, f32)) / dET +
+                 (rhs_get<T>(a.Fz[n], fz, f32) - rhs_get<T>(a.Fz[n], f0, f32)) / dZT);
         Rk[n] = Rp + Rf;
     }
     const T f = T(d.f), Jq = T(a.J[q]);
-    Rk[1] = Rk[1] + T(a.vF[0][q]) + f / Jq;
-    Rk[2] = Rk[2] + T(a.vF[1][q]);
-    Rk[3] = Rk[3] + T(a.vF[2][q]);
-    Rk[4] = Rk[4] + T(a.vF[3][q]) + f * u / Jq;
+    Rk[1] = Rk[1] + rhs_get<T>(a.vF[0], q, a.f32_rhs) + f / Jq;
+    Rk[2] = Rk[2] + rhs_get<T>(a.vF[1], q, a.f32_rhs);
+    Rk[3] = Rk[3] + rhs_get<T>(a.vF[2], q, a.f32_rhs);
+    Rk[4] = Rk[4] + rhs_get<T>(a.vF[3], q, a.f32_rhs) + f * u / Jq;
     T MR1 = (d11 * Rk[0] + d12 * Rk[1] + d13 * Rk[2] + d14 * Rk[3] + d15 * Rk[4]);
     T MR2 = (d21 * Rk[0] + d22 * Rk[1]);
     T MR3 = (d31 * Rk[0] + d22 * Rk[2]);

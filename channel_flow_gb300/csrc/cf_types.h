@@ -61,6 +61,8 @@ struct cf_flux_args {
     const double *Ep;     // sensor EpX / EpY / EpZ (limited fluxes only)
     double *F[5];         // inF1..inF5
     double *wz[2];        // scratch of the z limiter: per-cell 1/sum(w/J) of the left and right states
+    int f32_out;          // FP32 build: inF hold FP32 values (the step driver's internal use)
+    int reserved;
 };
 
 // the FP32 flux kernels' view: FP32 copies of the cell arrays, FP64 face arrays
@@ -72,6 +74,8 @@ struct cf_flux_args_f {
     const double *Ep;
     double *F[5];
     const float *wz[2];   // wz[0]: 1/J per cell
+    int f32_out;          // inF hold FP32 values
+    int reserved;
 };
 
 struct cf_visc_args {
@@ -82,6 +86,8 @@ struct cf_visc_args {
     const double *mf[3][9];    // x-, y-, z-face metrics
     double *LL[4], *ML[4], *NL[4];   // x/y/z face fluxes of variables 2..5
     double *prim[4];           // scratch: u, v, w, T of every cell
+    int f32_io;                // FP32 build: LL/ML/NL and vF hold FP32 values (the step driver's internal use)
+    int reserved;
 };
 
 struct cf_filter_args {
@@ -105,6 +111,8 @@ struct cf_lu_args {
     const double *vF[4];
     double *MR[5], *NR[5], *NL[5], *Res[5];
     double *partial;         // scratch: per-block partial norm sums (5 per block)
+    int f32_rhs;             // FP32 build: Fx/Fy/Fz and vF hold FP32 values (the step driver's internal use)
+    int reserved;
 };
 
 // tiled wavefront of the hyperplane sweeps (cf_wave.cuh)

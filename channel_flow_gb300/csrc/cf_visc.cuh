@@ -184,12 +184,12 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
 #ifdef CF_FAST_MATH
         const T iJf = T(1) / Jf;
 #endif
-        a.LL[0][q] = double(CF_VJF(mu_E * (A.s1 * X.du + A.s5 * X.dv + A.s7 * X.dw + D.x1 * Y.du + D.x7 * Y.dv + D.x9 * Y.dw + E.x1 * Z.du + E.x7 * Z.dv + E.x9 * Z.dw)));
-        a.LL[1][q] = double(CF_VJF(mu_E * (A.s5 * X.du + A.s2 * X.dv + A.s6 * X.dw + D.x5 * Y.du + D.x2 * Y.dv + D.x10 * Y.dw + E.x5 * Z.du + E.x2 * Z.dv + E.x10 * Z.dw)));
-        a.LL[2][q] = double(CF_VJF(mu_E * (A.s7 * X.du + A.s6 * X.dv + A.s3 * X.dw + D.x6 * Y.du + D.x8 * Y.dv + D.x3 * Y.dw + E.x6 * Z.du + E.x8 * Z.dv + E.x3 * Z.dw)));
-        a.LL[3][q] = double(CF_VJF(mu_E * (T(0.5) * A.s1 * X.du2 + T(0.5) * A.s2 * X.dv2 + T(0.5) * A.s3 * X.dw2 + A.s5 * X.duv + A.s6 * X.dvw + A.s7 * X.duw + CF_VPR(Cv * K * A.s4 * X.dT) +
+        rhs_put<T>(a.LL[0], q, T(CF_VJF(mu_E * (A.s1 * X.du + A.s5 * X.dv + A.s7 * X.dw + D.x1 * Y.du + D.x7 * Y.dv + D.x9 * Y.dw + E.x1 * Z.du + E.x7 * Z.dv + E.x9 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.LL[1], q, T(CF_VJF(mu_E * (A.s5 * X.du + A.s2 * X.dv + A.s6 * X.dw + D.x5 * Y.du + D.x2 * Y.dv + D.x10 * Y.dw + E.x5 * Z.du + E.x2 * Z.dv + E.x10 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.LL[2], q, T(CF_VJF(mu_E * (A.s7 * X.du + A.s6 * X.dv + A.s3 * X.dw + D.x6 * Y.du + D.x8 * Y.dv + D.x3 * Y.dw + E.x6 * Z.du + E.x8 * Z.dv + E.x3 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.LL[3], q, T(CF_VJF(mu_E * (T(0.5) * A.s1 * X.du2 + T(0.5) * A.s2 * X.dv2 + T(0.5) * A.s3 * X.dw2 + A.s5 * X.duv + A.s6 * X.dvw + A.s7 * X.duw + CF_VPR(Cv * K * A.s4 * X.dT) +
             T(0.5) * D.x1 * Y.du2 + T(0.5) * D.x2 * Y.dv2 + T(0.5) * D.x3 * Y.dw2 + D.x5 * Vx * Y.du + D.x6 * Wx * Y.du + D.x7 * Ux * Y.dv + D.x8 * Wx * Y.dv + D.x9 * Ux * Y.dw + D.x10 * Vx * Y.dw + CF_VPR(Cv * K * D.x4 * Y.dT) +
-            T(0.5) * E.x1 * Z.du2 + T(0.5) * E.x2 * Z.dv2 + T(0.5) * E.x3 * Z.dw2 + E.x5 * Vx * Z.du + E.x6 * Wx * Z.du + E.x7 * Ux * Z.dv + E.x8 * Wx * Z.dv + E.x9 * Ux * Z.dw + E.x10 * Vx * Z.dw + CF_VPR(Cv * K * E.x4 * Z.dT))));
+            T(0.5) * E.x1 * Z.du2 + T(0.5) * E.x2 * Z.dv2 + T(0.5) * E.x3 * Z.dw2 + E.x5 * Vx * Z.du + E.x6 * Wx * Z.du + E.x7 * Ux * Z.dv + E.x8 * Wx * Z.dv + E.x9 * Ux * Z.dw + E.x10 * Vx * Z.dw + CF_VPR(Cv * K * E.x4 * Z.dT)))), a.f32_io);
     }
     // ---- y face (Viscous_terms.cpp:550-695) ----
     if (FACE == 1 || FACE == 3) {
@@ -209,12 +209,12 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
 #ifdef CF_FAST_MATH
         const T iJf = T(1) / Jf;
 #endif
-        a.ML[0][q] = double(CF_VJF(mu_E * (D.x1 * X.du + D.x5 * X.dv + D.x6 * X.dw + B.s1 * Y.du + B.s5 * Y.dv + B.s7 * Y.dw + F.x1 * Z.du + F.x7 * Z.dv + F.x9 * Z.dw)));
-        a.ML[1][q] = double(CF_VJF(mu_E * (D.x7 * X.du + D.x2 * X.dv + D.x8 * X.dw + B.s5 * Y.du + B.s2 * Y.dv + B.s6 * Y.dw + F.x5 * Z.du + F.x2 * Z.dv + F.x10 * Z.dw)));
-        a.ML[2][q] = double(CF_VJF(mu_E * (D.x9 * X.du + D.x10 * X.dv + D.x3 * X.dw + B.s7 * Y.du + B.s6 * Y.dv + B.s3 * Y.dw + F.x6 * Z.du + F.x8 * Z.dv + F.x3 * Z.dw)));
-        a.ML[3][q] = double(CF_VJF(mu_E * (T(0.5) * B.s1 * Y.du2 + T(0.5) * B.s2 * Y.dv2 + T(0.5) * B.s3 * Y.dw2 + B.s5 * Y.duv + B.s6 * Y.dvw + B.s7 * Y.duw + CF_VPR(Cv * K * B.s4 * Y.dT) +
+        rhs_put<T>(a.ML[0], q, T(CF_VJF(mu_E * (D.x1 * X.du + D.x5 * X.dv + D.x6 * X.dw + B.s1 * Y.du + B.s5 * Y.dv + B.s7 * Y.dw + F.x1 * Z.du + F.x7 * Z.dv + F.x9 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.ML[1], q, T(CF_VJF(mu_E * (D.x7 * X.du + D.x2 * X.dv + D.x8 * X.dw + B.s5 * Y.du + B.s2 * Y.dv + B.s6 * Y.dw + F.x5 * Z.du + F.x2 * Z.dv + F.x10 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.ML[2], q, T(CF_VJF(mu_E * (D.x9 * X.du + D.x10 * X.dv + D.x3 * X.dw + B.s7 * Y.du + B.s6 * Y.dv + B.s3 * Y.dw + F.x6 * Z.du + F.x8 * Z.dv + F.x3 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.ML[3], q, T(CF_VJF(mu_E * (T(0.5) * B.s1 * Y.du2 + T(0.5) * B.s2 * Y.dv2 + T(0.5) * B.s3 * Y.dw2 + B.s5 * Y.duv + B.s6 * Y.dvw + B.s7 * Y.duw + CF_VPR(Cv * K * B.s4 * Y.dT) +
             T(0.5) * D.x1 * X.du2 + T(0.5) * D.x2 * X.dv2 + T(0.5) * D.x3 * X.dw2 + D.x5 * Uy * X.dv + D.x6 * Uy * X.dw + D.x7 * Vy * X.du + D.x8 * Vy * X.dw + D.x9 * Wy * X.du + D.x10 * Wy * X.dv + CF_VPR(Cv * K * D.x4 * X.dT) +
-            T(0.5) * F.x1 * Z.du2 + T(0.5) * F.x2 * Z.dv2 + T(0.5) * F.x3 * Z.dw2 + F.x5 * Vy * Z.du + F.x6 * Wy * Z.du + F.x7 * Uy * Z.dv + F.x8 * Wy * Z.dv + F.x9 * Uy * Z.dw + F.x10 * Vy * Z.dw + CF_VPR(Cv * K * F.x4 * Z.dT))));
+            T(0.5) * F.x1 * Z.du2 + T(0.5) * F.x2 * Z.dv2 + T(0.5) * F.x3 * Z.dw2 + F.x5 * Vy * Z.du + F.x6 * Wy * Z.du + F.x7 * Uy * Z.dv + F.x8 * Wy * Z.dv + F.x9 * Uy * Z.dw + F.x10 * Vy * Z.dw + CF_VPR(Cv * K * F.x4 * Z.dT)))), a.f32_io);
     }
     // ---- z face (Viscous_terms.cpp:698-841) ----
     if (FACE == 2 || FACE == 3) {
@@ -234,12 +234,12 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
 #ifdef CF_FAST_MATH
         const T iJf = T(1) / Jf;
 #endif
-        a.NL[0][q] = double(CF_VJF(mu_E * (E.x1 * X.du + E.x5 * X.dv + E.x6 * X.dw + F.x1 * Y.du + F.x5 * Y.dv + F.x6 * Y.dw + Cc.s1 * Z.du + Cc.s5 * Z.dv + Cc.s7 * Z.dw)));
-        a.NL[1][q] = double(CF_VJF(mu_E * (E.x7 * X.du + E.x2 * X.dv + E.x8 * X.dw + F.x7 * Y.du + F.x2 * Y.dv + F.x8 * Y.dw + Cc.s5 * Z.du + Cc.s2 * Z.dv + Cc.s6 * Z.dw)));
-        a.NL[2][q] = double(CF_VJF(mu_E * (E.x9 * X.du + E.x10 * X.dv + E.x3 * X.dw + F.x9 * Y.du + F.x10 * Y.dv + F.x3 * Y.dw + Cc.s7 * Z.du + Cc.s6 * Z.dv + Cc.s3 * Z.dw)));
-        a.NL[3][q] = double(CF_VJF(mu_E * (T(0.5) * Cc.s1 * Z.du2 + T(0.5) * Cc.s2 * Z.dv2 + T(0.5) * Cc.s3 * Z.dw2 + Cc.s5 * Z.duv + Cc.s6 * Z.dvw + Cc.s7 * Z.duw + CF_VPR(Cv * K * Cc.s4 * Z.dT) +
+        rhs_put<T>(a.NL[0], q, T(CF_VJF(mu_E * (E.x1 * X.du + E.x5 * X.dv + E.x6 * X.dw + F.x1 * Y.du + F.x5 * Y.dv + F.x6 * Y.dw + Cc.s1 * Z.du + Cc.s5 * Z.dv + Cc.s7 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.NL[1], q, T(CF_VJF(mu_E * (E.x7 * X.du + E.x2 * X.dv + E.x8 * X.dw + F.x7 * Y.du + F.x2 * Y.dv + F.x8 * Y.dw + Cc.s5 * Z.du + Cc.s2 * Z.dv + Cc.s6 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.NL[2], q, T(CF_VJF(mu_E * (E.x9 * X.du + E.x10 * X.dv + E.x3 * X.dw + F.x9 * Y.du + F.x10 * Y.dv + F.x3 * Y.dw + Cc.s7 * Z.du + Cc.s6 * Z.dv + Cc.s3 * Z.dw))), a.f32_io);
+        rhs_put<T>(a.NL[3], q, T(CF_VJF(mu_E * (T(0.5) * Cc.s1 * Z.du2 + T(0.5) * Cc.s2 * Z.dv2 + T(0.5) * Cc.s3 * Z.dw2 + Cc.s5 * Z.duv + Cc.s6 * Z.dvw + Cc.s7 * Z.duw + CF_VPR(Cv * K * Cc.s4 * Z.dT) +
             T(0.5) * E.x1 * X.du2 + T(0.5) * E.x2 * X.dv2 + T(0.5) * E.x3 * X.dw2 + E.x5 * Uz * X.dv + E.x6 * Uz * X.dw + E.x7 * Vz * X.du + E.x8 * Vz * X.dw + E.x9 * Wz * X.du + E.x10 * Wz * X.dv + CF_VPR(Cv * K * E.x4 * X.dT) +
-            T(0.5) * F.x1 * Y.du2 + T(0.5) * F.x2 * Y.dv2 + T(0.5) * F.x3 * Y.dw2 + F.x5 * Uz * Y.dv + F.x6 * Uz * Y.dw + F.x7 * Vz * Y.du + F.x8 * Vz * Y.dw + F.x9 * Wz * Y.du + F.x10 * Wz * Y.dv + CF_VPR(Cv * K * F.x4 * Y.dT))));
+            T(0.5) * F.x1 * Y.du2 + T(0.5) * F.x2 * Y.dv2 + T(0.5) * F.x3 * Y.dw2 + F.x5 * Uz * Y.dv + F.x6 * Uz * Y.dw + F.x7 * Vz * Y.du + F.x8 * Vz * Y.dw + F.x9 * Wz * Y.du + F.x10 * Wz * Y.dv + CF_VPR(Cv * K * F.x4 * Y.dT)))), a.f32_io);
     }
 }
 
@@ -254,9 +254,13 @@ __global__ void k_visc_div(cf_dims d, cf_visc_args a, cf_box b)
     const T invXI = T(1.) / T(d.dXI), invET = T(1.) / T(d.dET), invZT = T(1.) / T(d.dZT);
     const size_t q = d.ix(i, j, k), qi = d.ix(i + 1, j, k), qj = d.ix(i, j + 1, k), qk = q + 1;
 #pragma unroll
-    for (int v = 0; v < 4; v++)
-        a.vF[v][q] = double((T(a.LL[v][qi]) - T(a.LL[v][q])) * invXI + (T(a.ML[v][qj]) - T(a.ML[v][q])) * invET +
-                            (T(a.NL[v][qk]) - T(a.NL[v][q])) * invZT);
+    for (int v = 0; v < 4; v++) {
+        const int f = a.f32_io;
+        rhs_put<T>(a.vF[v], q,
+                   (rhs_get<T>(a.LL[v], qi, f) - rhs_get<T>(a.LL[v], q, f)) * invXI +
+                       (rhs_get<T>(a.ML[v], qj, f) - rhs_get<T>(a.ML[v], q, f)) * invET +
+                       (rhs_get<T>(a.NL[v], qk, f) - rhs_get<T>(a.NL[v], q, f)) * invZT, f);
+    }
 }
 
 template <typename T>

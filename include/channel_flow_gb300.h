@@ -319,7 +319,9 @@ typedef struct {
  * below the tolerance (the maxima persist across steps, main.cpp:63, 387)
  * or max_iterations; then Driven_force (Q), Statistic when
  * statistic_step > 0, and Uq <- U, U <- U_.  Returns the iteration count,
- * the last normalised er1..er5 and Q (pointers may be NULL). */
+ * the last normalised er1..er5 and Q (pointers may be NULL).  In
+ * CF_PREC_FP32 the loop's right-hand-side arrays (inF, vF, LL, ML, NL) are
+ * its scratch and hold FP32 values in their FP64 allocation afterwards. */
 int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields *fields, int *iterations,
             double *er, double *Q);
 /* forget the running residual maxima */
