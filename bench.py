@@ -133,10 +133,13 @@ def rhs_calls(ctx, w, ptr):
     return calls
 
 
-# kernels launched per step: x halo 1, y wall 1, z periodic 1, Filter
+# kernels launched per RHS step: x halo 1, y wall 1, z periodic 1, Filter
 # (1 coefficients + 2 x 6 fused levels + 2 energy + 3 ghost fills + 3
-# thresholds = 21), 3 flux kernels, viscous 3
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 21 + 3 + 3
+# thresholds = 21), fluxes (FP64: x, y, z weights, z = 4; FP32: an FP32
+# copy of U and J before each of the three = 6), viscous (primitives,
+# three face sets, divergence = 5)
+LAUNCHES_PER_STEP = {"fp64": 1 + 1 + 1 + 21 + 4 + 5, "fp64_exact": 1 + 1 + 1 + 21 + 4 + 5,
+                     "fp32": 1 + 1 + 1 + 21 + 6 + 5}
 
 
 def run_calls(ctx, calls):
@@ -411,7 +414,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.precision != "fp32" else "f32", "data": "synthetic",
                 "config": cfg, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "secondary": extra,
-                "clocks": clocks.summary(), "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+                "clocks": clocks.summary(), "gpu_launches": LAUNCHES_PER_STEP[args.precision] * args.steps,
                 "parallelism": "replicas" if world > 1 else "single"}
         print(json.dumps(line))
     ctx.close()

@@ -59,6 +59,15 @@ __global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__
         T c_ = T(Yp[q]) - T(Yp[q - s]);
         cA[q] = ST(b_ / a_);
         cC[q] = ST(c_ / a_);
+    } else if (sizeof(T) == 4) {
+        // FP32 build: the differences of Y_point in FP64 (they cancel), the
+        // ratios in FP32 (FP64 divisions would dominate this kernel)
+        const float a_ = float(Yp[q + s] - Yp[q - s]);
+        const float b_ = float(Yp[q + s] - Yp[q]);
+        const float c_ = float(Yp[q] - Yp[q - s]);
+        const float ia = 1.0f / a_, iJ = 1.0f / float(J[q]);
+        cA[q] = ST(b_ * ia * (float(J[q - s]) * iJ));
+        cC[q] = ST(c_ * ia * (float(J[q + s]) * iJ));
     } else {
         const double a_ = Yp[q + s] - Yp[q - s];
         const double b_ = Yp[q + s] - Yp[q];

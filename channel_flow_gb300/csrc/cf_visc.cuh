@@ -140,9 +140,9 @@ __device__ __forceinline__ vcross<T> ccross(T p0, T p1, T p2, T q0, T q1, T q2)
     return c;
 }
 
-// FACE 0/1/2: the x, y or z face of every cell (one launch each keeps the
-// FP64 register footprint of one face, without spills); FACE 3: all three
-// in one pass (FP32, where the registers suffice)
+// FACE 0/1/2: the x, y or z face of every cell, one launch each (the
+// register footprint of one face: no spills in FP64, and in FP32 twice the
+// resident warps of a kernel doing all three faces, which measured slower)
 template <typename T, int FACE>
 __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
 {
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
     const vcell<T> jp = FACE != 1 ? ld<T>(a, d.ix(i, j + 1, k)) : c;
     const vcell<T> kp = FACE != 2 ? ld<T>(a, d.ix(i, j, k + 1)) : c;
     // ---- x face (Viscous_terms.cpp:398-547) ----
-    if (FACE == 0 || FACE == 3) {
+    if (FACE == 0) {
         const vcell<T> imjp = ld<T>(a, d.ix(i - 1, j + 1, k)), imkp = ld<T>(a, d.ix(i - 1, j, k + 1));
         const vcell<T> imjm = ld<T>(a, d.ix(i - 1, j - 1, k)), imkm = ld<T>(a, d.ix(i - 1, j, k - 1));
         vgrad<T> X = g2<T>(c, im, invXI);
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
             T(0.5) * E.x1 * Z.du2 + T(0.5) * E.x2 * Z.dv2 + T(0.5) * E.x3 * Z.dw2 + E.x5 * Vx * Z.du + E.x6 * Wx * Z.du + E.x7 * Ux * Z.dv + E.x8 * Wx * Z.dv + E.x9 * Ux * Z.dw + E.x10 * Vx * Z.dw + CF_VPR(Cv * K * E.x4 * Z.dT)))), a.f32_io);
     }
     // ---- y face (Viscous_terms.cpp:550-695) ----
-    if (FACE == 1 || FACE == 3) {
+    if (FACE == 1) {
         const vcell<T> ipjm = ld<T>(a, d.ix(i + 1, j - 1, k)), imjm = ld<T>(a, d.ix(i - 1, j - 1, k));
         const vcell<T> jmkp = ld<T>(a, d.ix(i, j - 1, k + 1)), jmkm = ld<T>(a, d.ix(i, j - 1, k - 1));
         vgrad<T> X = g4<T>(ip, ipjm, im, imjm, ipjm, inv4XI);
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
             T(0.5) * F.x1 * Z.du2 + T(0.5) * F.x2 * Z.dv2 + T(0.5) * F.x3 * Z.dw2 + F.x5 * Vy * Z.du + F.x6 * Wy * Z.du + F.x7 * Uy * Z.dv + F.x8 * Wy * Z.dv + F.x9 * Uy * Z.dw + F.x10 * Vy * Z.dw + CF_VPR(Cv * K * F.x4 * Z.dT)))), a.f32_io);
     }
     // ---- z face (Viscous_terms.cpp:698-841) ----
-    if (FACE == 2 || FACE == 3) {
+    if (FACE == 2) {
         const vcell<T> ipkm = ld<T>(a, d.ix(i + 1, j, k - 1)), imkm = ld<T>(a, d.ix(i - 1, j, k - 1));
         const vcell<T> jpkm = ld<T>(a, d.ix(i, j + 1, k - 1)), jmkm = ld<T>(a, d.ix(i, j - 1, k - 1));
         const vcell<T> imjp = ld<T>(a, d.ix(i - 1, j + 1, k));
@@ -269,13 +269,9 @@ cudaError_t launch_viscous(const cf_dims &d, const cf_visc_args &a, cudaStream_t
     const size_t n = d.total();
     k_visc_prim<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
     cf_box bf = make_box(3, d.gend + 1, 2, d.ny + 1, 2, d.nz + 1);
-    if constexpr (sizeof(T) == sizeof(double)) {
-        k_visc_faces<T, 0><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
-        k_visc_faces<T, 1><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
-        k_visc_faces<T, 2><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
-    } else {
-        k_visc_faces<T, 3><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
-    }
+    k_visc_faces<T, 0><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+    k_visc_faces<T, 1><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
+    k_visc_faces<T, 2><<<box_grid(bf), box_block(), 0, s>>>(d, a, bf);
     cf_box bd = make_box(3, d.gend, 2, d.ny, 2, d.nz);
     k_visc_div<T><<<box_grid(bd), box_block(), 0, s>>>(d, a, bd);
     return cudaGetLastError();
