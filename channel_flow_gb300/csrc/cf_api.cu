@@ -197,6 +197,7 @@ int cf_create(const cf_grid *g, int precision, cf_ctx **out)
     d.dXI = g->d_xi; d.dET = g->d_eta; d.dZT = g->d_zeta;
     d.K = g->gamma_gas; d.R = g->r_gas; d.e = g->beta_min; d.Cv = g->cv; d.mu_L = g->mu; d.Pr_L = g->prandtl;
     d.f = g->body_force; d.high = g->height;
+    cf_dims_fill_f32(d);
     c->q0 = g->bulk_flux;
     c->prec = precision;
     build_tables(c);

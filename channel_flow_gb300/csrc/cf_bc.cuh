@@ -30,7 +30,7 @@ __global__ void k_y_wall(cf_dims d, cf_ptr5 U, const double *__restrict__ J, cf_
     const int js = side == 0 ? 2 : d.ny;
     const int jg = side == 0 ? 1 : d.ny + 1;
     const size_t s = d.ix(i, js, k), q = d.ix(i, jg, k);
-    const T K = T(d.K), R = T(d.R);
+    const T K = CF_DC(T, d, K), R = CF_DC(T, d, R);
     T u1 = T(U.p[0][s]);
     T rho = u1 * T(J[s]);
     T Uu = T(U.p[1][s]) / u1;
@@ -76,14 +76,14 @@ __global__ void k_rk3(cf_dims d, cf_rk3_args a, cf_box b, int RK, double deltaT)
     const size_t q = d.ix(i, j, k);
     const size_t fx = d.ix(i, j - 1, k - 1), f0 = d.ix(i - 1, j - 1, k - 1);
     const size_t fy = d.ix(i - 1, j, k - 1), fz = d.ix(i - 1, j - 1, k);
-    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
+    const T dXI = CF_DC(T, d, dXI), dET = CF_DC(T, d, dET), dZT = CF_DC(T, d, dZT);
     T tmp = T(a.U_[1][q]) / T(a.U_[0][q]);
     T Rk[5];
 #pragma unroll
     for (int n = 0; n < 5; n++)
         Rk[n] = -((T(a.Fx[n][fx]) - T(a.Fx[n][f0])) / dXI + (T(a.Fy[n][fy]) - T(a.Fy[n][f0])) / dET +
                   (T(a.Fz[n][fz]) - T(a.Fz[n][f0])) / dZT);
-    const T f = T(d.f), Jq = T(a.J[q]);
+    const T f = CF_DC(T, d, f), Jq = T(a.J[q]);
     Rk[1] = Rk[1] + T(a.vF[0][q]) + f / Jq;
     Rk[2] = Rk[2] + T(a.vF[1][q]);
     Rk[3] = Rk[3] + T(a.vF[2][q]);

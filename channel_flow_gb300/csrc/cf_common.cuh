@@ -42,6 +42,10 @@ __device__ __forceinline__ T rhs_get(const double *p, size_t q, int f32)
 }
 
 
+// a grid constant of cf_dims in the compute type T (its FP32 copy for float)
+#define CF_DC(T, d, x) (sizeof(T) == 4 ? (T)((d).f_##x) : (T)((d).x))
+
+
 #define CF_BOX_INDEX(b, i, j, k)                                    \
     const int k = (b).k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); \
     const int j = (b).j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y); \

@@ -553,9 +553,9 @@ __global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
 #pragma unroll
     for (int n = 0; n < 9; n++) m[n] = T(a.m[n][q]);
     if (LIMITED)
-        fast_flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), T(d.K), T(d.e), F);
+        fast_flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), CF_DC(T, d, K), CF_DC(T, d, e), F);
     else
-        fast_flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), T(d.K), F);
+        fast_flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), CF_DC(T, d, K), F);
 #else
     if (DIR == 0) {
         if (LIMITED) states_x_limited<T>(d, a, i, j, k, mL, mR);
@@ -571,9 +571,9 @@ __global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
 #pragma unroll
     for (int n = 0; n < 9; n++) m[n] = T(a.m[n][q]);
     if (LIMITED)
-        flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), T(d.K), T(d.e), F);
+        flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), CF_DC(T, d, K), CF_DC(T, d, e), F);
     else
-        flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), T(d.K), F);
+        flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), CF_DC(T, d, K), F);
 #endif
     const int f32 = a.f32_out;
     if (DIR == 1 && (j == 1 || j == d.ny)) {

@@ -22,7 +22,7 @@ template <typename T>
 __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args &a, size_t q)
 {
     lstate<T> s;
-    const T K = T(d.K);
+    const T K = CF_DC(T, d, K);
     T u1 = T(a.U_[0][q]), Jq = T(a.J[q]);
     s.rho = u1 * Jq;
     s.u = T(a.U_[1][q]) / u1;
@@ -33,7 +33,7 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
     s.C = K * s.P / s.rho;
     s.Tt = s.P / s.rho;
     s.H = T(0.5) * s.VV + s.C / (K - T(1));
-    s.beta = rmax(s.VV / s.C, T(d.e));
+    s.beta = rmax(s.VV / s.C, CF_DC(T, d, e));
     return s;
 }
 
@@ -87,7 +87,7 @@ template <typename T>
 __device__ __forceinline__ ldiag<T> lu_diag(const cf_dims &d, const cf_lu_args &a, size_t q, lstate<T> s,
                                             T deltaT)
 {
-    const T K = T(d.K);
+    const T K = CF_DC(T, d, K);
     T xix = T(a.m[0][q]), xiy = T(a.m[1][q]), xiz = T(a.m[2][q]);
     T etx = T(a.m[3][q]), ety = T(a.m[4][q]), etz = T(a.m[5][q]);
     T ztx = T(a.m[6][q]), zty = T(a.m[7][q]), ztz = T(a.m[8][q]);
@@ -101,7 +101,7 @@ __device__ __forceinline__ ldiag<T> lu_diag(const cf_dims &d, const cf_lu_args &
     T lambdaX = ((beta + T(1)) * fabs(U) + Sx) / T(2);
     T lambdaY = ((beta + T(1)) * fabs(V) + Sy) / T(2);
     T lambdaZ = ((beta + T(1)) * fabs(W) + Sz) / T(2);
-    T lambda = lambdaX / T(d.dXI) + lambdaY / T(d.dET) + lambdaZ / T(d.dZT);
+    T lambda = lambdaX / CF_DC(T, d, dXI) + lambdaY / CF_DC(T, d, dET) + lambdaZ / CF_DC(T, d, dZT);
     ldiag<T> g;
     g.d11 = T(2) * deltaT / (T(3) * beta + T(2) * lambda * deltaT);
     g.d22 = T(2) * deltaT / (T(3) + T(2) * lambda * deltaT);
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
-    const T K = T(d.K), deltaT = T(dt);
+    const T K = CF_DC(T, d, K), deltaT = T(dt);
     lstate<T> s = lu_state<T>(d, a, q);
     T rho = s.rho, u = s.u, v = s.v, w = s.w, VV = s.VV, Tt = s.Tt, H = s.H, beta = s.beta;
     T temp = rho * K;
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     T d55 = (K - T(1)) * (T(1) + (K - T(1)) * beta) / temp;
     const size_t fx = d.ix(i, j - 1, k - 1), f0 = d.ix(i - 1, j - 1, k - 1);
     const size_t fy = d.ix(i - 1, j, k - 1), fz = d.ix(i - 1, j - 1, k);
-    const T dXI = T(d.dXI), dET = T(d.dET), dZT = T(d.dZT);
+    const T dXI = CF_DC(T, d, dXI), dET = CF_DC(T, d, dET), dZT = CF_DC(T, d, dZT);
     T Rk[5];
 #ifdef CF_FAST_MATH
     const double rdt2 = 0.5 / dt;     // one FP64 division per cell instead of five
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
                  (rhs_get<T>(a.Fz[n], fz, f32) - rhs_get<T>(a.Fz[n], f0, f32)) / dZT);
         Rk[n] = Rp + Rf;
     }
-    const T f = T(d.f), Jq = T(a.J[q]);
+    const T f = CF_DC(T, d, f), Jq = T(a.J[q]);
     Rk[1] = Rk[1] + rhs_get<T>(a.vF[0], q, a.f32_rhs) + f / Jq;
     Rk[2] = Rk[2] + rhs_get<T>(a.vF[1], q, a.f32_rhs);
     Rk[3] = Rk[3] + rhs_get<T>(a.vF[2], q, a.f32_rhs);
@@ -272,7 +272,7 @@ template <typename T>
 __device__ __forceinline__ void lu_lower(const cf_dims &d, const cf_lu_args &a, double *const *N, int i, int j,
                                          int k, T *LL)
 {
-    const T K = T(d.K);
+    const T K = CF_DC(T, d, K);
     const size_t qa = d.ix(i - 1, j, k), qb = d.ix(i, j - 1, k), qc = d.ix(i, j, k - 1);
     lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
     lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
@@ -281,7 +281,7 @@ __device__ __forceinline__ void lu_lower(const cf_dims &d, const cf_lu_args &a, 
     lu_load5<T>(N, qa, va);
     lu_load5<T>(N, qb, vb);
     lu_load5<T>(N, qc, vc);
-    lu_lower_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), LL);
+    lu_lower_sum<T>(A, B, C, va, vb, vc, CF_DC(T, d, dXI), CF_DC(T, d, dET), CF_DC(T, d, dZT), LL);
 }
 
 // U*N with the splits formed from the neighbours' states
@@ -289,7 +289,7 @@ template <typename T>
 __device__ __forceinline__ void lu_upper(const cf_dims &d, const cf_lu_args &a, double *const *N, int i, int j,
                                          int k, T *UU)
 {
-    const T K = T(d.K);
+    const T K = CF_DC(T, d, K);
     const size_t qa = d.ix(i + 1, j, k), qb = d.ix(i, j + 1, k), qc = d.ix(i, j, k + 1);
     lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
     lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
@@ -298,7 +298,7 @@ __device__ __forceinline__ void lu_upper(const cf_dims &d, const cf_lu_args &a, 
     lu_load5<T>(N, qa, va);
     lu_load5<T>(N, qb, vb);
     lu_load5<T>(N, qc, vc);
-    lu_upper_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), UU);
+    lu_upper_sum<T>(A, B, C, va, vb, vc, CF_DC(T, d, dXI), CF_DC(T, d, dET), CF_DC(T, d, dZT), UU);
 }
 
 // ---------------------------------------------------------------------------
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(256) k_lu_pack(cf_dims d, cf_lu_args a, double
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
-    const T K = T(d.K);
+    const T K = CF_DC(T, d, K);
     const lstate<T> s = lu_state<T>(d, a, q);
     double *P = pack + q * LU_PACK;
 #pragma unroll
@@ -388,7 +388,7 @@ __global__ void k_lu_forward_packed(cf_dims d, cf_lu_args a, const double *__res
     lu_load5<T>(a.NL, qa, va);
     lu_load5<T>(a.NL, qb, vb);
     lu_load5<T>(a.NL, qc, vc);
-    lu_lower_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), LL);
+    lu_lower_sum<T>(A, B, C, va, vb, vc, CF_DC(T, d, dXI), CF_DC(T, d, dET), CF_DC(T, d, dZT), LL);
     T r0 = T(a.MR[0][q]) - LL[0];
     a.NL[0][q] = double(g.d11 * r0);
     a.NL[1][q] = double(g.d22 * (T(a.MR[1][q]) - LL[1]));
@@ -415,7 +415,7 @@ __global__ void k_lu_backward_packed(cf_dims d, cf_lu_args a, const double *__re
     lu_load5<T>(a.NR, qa, va);
     lu_load5<T>(a.NR, qb, vb);
     lu_load5<T>(a.NR, qc, vc);
-    lu_upper_sum<T>(A, B, C, va, vb, vc, T(d.dXI), T(d.dET), T(d.dZT), UU);
+    lu_upper_sum<T>(A, B, C, va, vb, vc, CF_DC(T, d, dXI), CF_DC(T, d, dET), CF_DC(T, d, dZT), UU);
     a.NR[0][q] = double(T(a.NL[0][q]) - g.d11 * UU[0]);
     a.NR[1][q] = double(T(a.NL[1][q]) - g.d22 * UU[1]);
     a.NR[2][q] = double(T(a.NL[2][q]) - g.d22 * UU[2]);

@@ -19,6 +19,9 @@ struct cf_dims {
     double K, R, e;           // gamma, gas constant, preconditioning floor
     double Cv, mu_L, Pr_L;
     double f, high;           // body force, channel height 2h
+    // the same constants rounded to FP32, for the FP32 kernels (a per-thread
+    // FP64 -> FP32 conversion of a kernel parameter issues to the FP64 pipe)
+    float f_dXI, f_dET, f_dZT, f_K, f_R, f_e, f_Cv, f_mu_L, f_Pr_L, f_f, f_high;
 
     __host__ __device__ __forceinline__ size_t ix(int i, int j, int k) const
     {
@@ -27,6 +30,14 @@ struct cf_dims {
     __host__ __device__ __forceinline__ size_t plane() const { return (size_t)Ym * (size_t)Zm; }
     __host__ __device__ __forceinline__ size_t total() const { return (size_t)(X_out + 6) * plane(); }
 };
+
+// the FP32 copies of a cf_dims' constants
+static inline void cf_dims_fill_f32(cf_dims &d)
+{
+    d.f_dXI = (float)d.dXI; d.f_dET = (float)d.dET; d.f_dZT = (float)d.dZT;
+    d.f_K = (float)d.K; d.f_R = (float)d.R; d.f_e = (float)d.e; d.f_Cv = (float)d.Cv;
+    d.f_mu_L = (float)d.mu_L; d.f_Pr_L = (float)d.Pr_L; d.f_f = (float)d.f; d.f_high = (float)d.high;
+}
 
 struct cf_ptr5 {
     double *p[5];

@@ -33,7 +33,7 @@ __global__ void k_visc_prim(cf_dims d, cf_visc_args a, size_t n)
 {
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    const T K = T(d.K), R = T(d.R);
+    const T K = CF_DC(T, d, K), R = CF_DC(T, d, R);
     T rho = T(a.U[0][q]);
     T U = T(a.U[1][q]) / rho;
     T V = T(a.U[2][q]) / rho;
@@ -147,7 +147,7 @@ template <typename T, int FACE>
 __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
-    const T K = T(d.K), Cv = T(d.Cv), mu_E = T(d.mu_L), Pr_E = T(d.Pr_L);
+    const T K = CF_DC(T, d, K), Cv = CF_DC(T, d, Cv), mu_E = CF_DC(T, d, mu_L), Pr_E = CF_DC(T, d, Pr_L);
 #ifdef CF_FAST_MATH
     // the contracted and FP32 builds multiply by reciprocals of Pr and J_f
     const T iPr = T(1) / Pr_E;
@@ -157,9 +157,9 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
 #define CF_VPR(x) ((x) / (Pr_E))
 #define CF_VJF(x) ((x) / Jf)
 #endif
-    const T invXI = T(1.) / T(d.dXI), invET = T(1.) / T(d.dET), invZT = T(1.) / T(d.dZT);
-    const T inv4XI = T(1.) / (T(4) * T(d.dXI)), inv4ET = T(1.) / (T(4) * T(d.dET)),
-            inv4ZT = T(1.) / (T(4) * T(d.dZT));
+    const T invXI = T(1.) / CF_DC(T, d, dXI), invET = T(1.) / CF_DC(T, d, dET), invZT = T(1.) / CF_DC(T, d, dZT);
+    const T inv4XI = T(1.) / (T(4) * CF_DC(T, d, dXI)), inv4ET = T(1.) / (T(4) * CF_DC(T, d, dET)),
+            inv4ZT = T(1.) / (T(4) * CF_DC(T, d, dZT));
     const size_t q = d.ix(i, j, k), f = d.ix(i - 1, j - 1, k - 1);
     const vcell<T> c = ld<T>(a, q);
     const vcell<T> im = ld<T>(a, d.ix(i - 1, j, k)), jm = ld<T>(a, d.ix(i, j - 1, k)),
@@ -251,7 +251,7 @@ template <typename T>
 __global__ void k_visc_div(cf_dims d, cf_visc_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
-    const T invXI = T(1.) / T(d.dXI), invET = T(1.) / T(d.dET), invZT = T(1.) / T(d.dZT);
+    const T invXI = T(1.) / CF_DC(T, d, dXI), invET = T(1.) / CF_DC(T, d, dET), invZT = T(1.) / CF_DC(T, d, dZT);
     const size_t q = d.ix(i, j, k), qi = d.ix(i + 1, j, k), qj = d.ix(i, j + 1, k), qk = q + 1;
 #pragma unroll
     for (int v = 0; v < 4; v++) {

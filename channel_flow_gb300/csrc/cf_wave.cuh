@@ -141,7 +141,7 @@ template <typename T>
 __device__ __forceinline__ lsplit<T> wave_split(const cf_dims &d, const cf_lu_args &a, size_t q, const lstate<T> &s,
                                                 int dir)
 {
-    return lu_split<T>(s, T(a.m[3 * dir][q]), T(a.m[3 * dir + 1][q]), T(a.m[3 * dir + 2][q]), dir == 0, T(d.K));
+    return lu_split<T>(s, T(a.m[3 * dir][q]), T(a.m[3 * dir + 1][q]), T(a.m[3 * dir + 2][q]), dir == 0, CF_DC(T, d, K));
 }
 
 // face slots: x face cell (lj, lk) -> lj*8 + lk, y face (li, lk) -> li*8 + lk,
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
     const int li = c / (WV_TJ * WV_TK), lj = (c / WV_TK) % WV_TJ, lk = c % WV_TK;
     const int i = 3 + ta * WV_TI + li, j = 2 + tb * WV_TJ + lj, k = 2 + tc * WV_TK + lk;
     const bool in = i <= d.gend && j <= d.ny && k <= d.nz;
-    const lu_den<T> den[3] = {lu_den<T>(T(d.dXI)), lu_den<T>(T(d.dET)), lu_den<T>(T(d.dZT))};
+    const lu_den<T> den[3] = {lu_den<T>(CF_DC(T, d, dXI)), lu_den<T>(CF_DC(T, d, dET)), lu_den<T>(CF_DC(T, d, dZT))};
     T *P = sp + c;                                // value m of this cell at P[m * WV_CELLS]
     lsplit<T> A[3];
     ldiag<T> g;
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256) k_lu_tile_ghost_upper(cf_lu_args a, wave_
     const int ci = i - 3, cj = j - 2, ck = k - 2;
     const int tile = ((ci / WV_TI) * w.ntj + cj / WV_TJ) * w.ntk + ck / WV_TK;
     const int li = ci % WV_TI, lj = cj % WV_TJ, lk = ck % WV_TK;
-    const lu_den<T> dXI(T(d.dXI)), dET(T(d.dET)), dZT(T(d.dZT));
+    const lu_den<T> dXI(CF_DC(T, d, dXI)), dET(CF_DC(T, d, dET)), dZT(CF_DC(T, d, dZT));
     if (i == d.gend) wave_ghost_term<T, true>(d, a, q + d.plane(), 0, dXI, wave_face<T>(w, 0, tile), WV_FX,
                                               lj * WV_TK + lk);
     if (j == d.ny) wave_ghost_term<T, true>(d, a, q + (size_t)d.Zm, 1, dET, wave_face<T>(w, 1, tile), WV_FY,
