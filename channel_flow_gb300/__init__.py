@@ -130,11 +130,12 @@ class Context:
 
     def step(self, fields: dict, step: int = 1, deltaT: float = 0.00000005, max_iterations: int = 200,
              tolerance: float = 0.001, limiter: bool = True, filter: bool = True, roe_criterion: float = 0.007,
-             e_high: float = 1.0, e_low: float = 0.0, statistic_step: int = 0):
+             e_high: float = 1.0, e_low: float = 0.0, statistic_step: int = 0, static_metrics: bool = False):
         """One physical time step (cf_step).  ``fields`` maps the cf_fields
         member names to device tensors (lists for the multi-array members,
         a list of three lists for face_metric and inF).  Returns
-        (iterations, er[5], Q)."""
+        (iterations, er[5], Q).  ``static_metrics``: the metric arrays stay
+        unchanged between calls (the FP32 path then converts them once)."""
         f = _lib.cf_fields()
         for name, val in fields.items():
             slot = getattr(f, name)
@@ -148,7 +149,7 @@ class Context:
             else:
                 setattr(f, name, _ptr(val))
         prm = _lib.cf_step_params(deltaT, max_iterations, tolerance, int(limiter), int(filter), roe_criterion,
-                                  e_high, e_low, statistic_step)
+                                  e_high, e_low, statistic_step, int(static_metrics))
         it = C.c_int(0)
         er = np.zeros(5)
         q = np.zeros(1)

@@ -37,7 +37,8 @@ class cf_fields(C.Structure):
 class cf_step_params(C.Structure):
     _fields_ = [("deltaT", C.c_double), ("max_iterations", C.c_int), ("tolerance", C.c_double),
                 ("limiter", C.c_int), ("filter", C.c_int), ("roe_criterion", C.c_double),
-                ("e_high", C.c_double), ("e_low", C.c_double), ("statistic_step", C.c_int)]
+                ("e_high", C.c_double), ("e_low", C.c_double), ("statistic_step", C.c_int),
+                ("static_metrics", C.c_int)]
 
 
 class cf_wavy_wall(C.Structure):

@@ -28,6 +28,7 @@ struct cf_ctx {
     double sxy_bottom = 0, sxy_up = 0;
     double E[5] = {0, 0, 0, 0, 0};    // running maxima of the residual norms (main.cpp:63, 387-391)
     std::vector<double> er_hist;      // normalised er1..er5 of every iteration of the last cf_step
+    std::unordered_map<const double *, float *> met32;   // FP32 copies of fixed metric arrays (cf_step)
     std::unordered_map<const double *, double *> mirrors;
     std::unordered_map<std::string, std::pair<double *, size_t>> scratch;
     std::vector<int> nijk;            // plane tables, Hyperplane layout (host)
@@ -226,6 +227,7 @@ void cf_destroy(cf_ctx *c)
     if (c->tile_order) cudaFree(c->tile_order);
     if (c->trace) cudaFree(c->trace);
     if (c->cap) cudaStreamDestroy(c->cap);
+    for (auto &m : c->met32) cudaFree(m.second);
     delete c;
 }
 
@@ -386,12 +388,31 @@ int cf_X_periodic(cf_ctx *c, int, double *U1_, double *U2_, double *U3_, double 
 // ---------------------------------------------------------------------------
 // fluxes
 
+// The FP32 copy of a metric array that the caller keeps fixed across
+// cf_step calls (cf_step_params.static_metrics), made on first use; null
+// when it cannot be made (the kernels then read the FP64 array)
+static const float *met32_get(cf_ctx *c, const double *p)
+{
+    if (!p) return nullptr;
+    auto it = c->met32.find(p);
+    if (it != c->met32.end()) return it->second;
+    float *f = nullptr;
+    const size_t n = c->d.total();
+    if (cudaMalloc(&f, n * sizeof(float)) != cudaSuccess) return nullptr;
+    if (cf_fast::to_f32(n, p, f, c->stream) != cudaSuccess) {
+        cudaFree(f);
+        return nullptr;
+    }
+    c->met32[p] = f;
+    return f;
+}
+
 // reuse_shadow: the FP32 copies of U and J made by the previous FP32 flux
 // call are still current (the step driver's y and z fluxes after x)
 // f32_out: in FP32 mode, write inF as FP32 values into their FP64 arrays
 // (only the step driver, whose own Dual_time_stepping reads them)
 static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double *const *p32,
-                       bool reuse_shadow = false, bool f32_out = false)
+                       bool reuse_shadow = false, bool f32_out = false, bool static_metrics = false)
 {
     if (!c) return CF_ERR_ARG;
     // arrays 5..14 (ML/MR) are the reference's scratch and are not needed
@@ -422,8 +443,15 @@ static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double
         double *sh = scratch(c, "flux_f32", 4);
         if (!sh) return fail(c, CF_ERR_NOMEM, "%s: scratch allocation failed", who);
         if (!a.J && dir != 0) return fail(c, CF_ERR_ARG, "%s: J is NULL", who);
-        return cuda_check(c, cf_fast::flux_f32(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow, dir, limited,
-                                               c->stream), who);
+        const float *m32[10] = {nullptr};
+        if (static_metrics) {
+            m32[0] = met32_get(c, a.Jf);
+            for (int n = 0; n < 9; n++) m32[1 + n] = met32_get(c, a.m[n]);
+            for (int n = 0; n < 10; n++)
+                if (!m32[n]) return fail(c, CF_ERR_NOMEM, "%s: FP32 metric copy allocation failed", who);
+        }
+        return cuda_check(c, cf_fast::flux_f32(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow,
+                                               static_metrics ? m32 : nullptr, dir, limited, c->stream), who);
     }
     cudaError_t e = exact(c) ? cf_exact::flux(c->d, a, dir, limited, 0, c->stream)
                              : cf_fast::flux(c->d, a, dir, limited, 0, c->stream);
@@ -452,7 +480,7 @@ CF_FLUX_ENTRY(Flux_Z, 2, false)
 // viscous terms
 
 // f32_io: in FP32 mode, LL/ML/NL and vF hold FP32 values (the step driver)
-static int viscous_common(cf_ctx *c, double **p, bool f32_io)
+static int viscous_common(cf_ctx *c, double **p, bool f32_io, bool static_metrics = false)
 {
     if (!c || !p) return CF_ERR_ARG;
     // read: U (0-4), J (9), face metric sets (19-48); written: vF (5-8),
@@ -480,6 +508,14 @@ static int viscous_common(cf_ctx *c, double **p, bool f32_io)
     for (int n = 0; n < 4; n++) a.prim[n] = prim + (size_t)n * c->d.total();
     a.f32_io = (f32_io && kprec(c) == 1) ? 1 : 0;
     a.reserved = 0;
+    const bool m32 = static_metrics && kprec(c) == 1;
+    for (int f = 0; f < 3; f++) {
+        a.Jf32[f] = m32 ? met32_get(c, a.Jf[f]) : nullptr;
+        for (int n = 0; n < 9; n++) a.mf32[f][n] = m32 ? met32_get(c, a.mf[f][n]) : nullptr;
+        if (m32 && !a.Jf32[f]) return fail(c, CF_ERR_NOMEM, "Viscous_terms: FP32 metric copy allocation failed");
+        for (int n = 0; n < 9; n++)
+            if (m32 && !a.mf32[f][n]) return fail(c, CF_ERR_NOMEM, "Viscous_terms: FP32 metric copy allocation failed");
+    }
     cudaError_t e = exact(c) ? cf_exact::viscous(c->d, a, 0, c->stream)
                              : cf_fast::viscous(c->d, a, kprec(c), c->stream);
     return cuda_check(c, e, "Viscous_terms");
@@ -581,6 +617,7 @@ static int lu_args(cf_ctx *c, double **p, const char *who, cf_lu_args &a)
     for (int n = 0; n < 4; n++) a.vF[n] = R(c, p[40 + n]);
     a.f32_rhs = 0;
     a.reserved = 0;
+    for (int n = 0; n < 9; n++) a.m32[n] = nullptr;
     cf_dims &d = c->d;
     const size_t np = cf_fast::lu_partial_count(d);
     auto &e = c->scratch["lu_partial"];
@@ -778,7 +815,7 @@ static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, const cf_wa
 
 // f32_rhs: in FP32 mode, Fx/Fy/Fz and vF hold FP32 values (the step driver)
 static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,
-                      int *Nijk, int *ijk, double **p, bool f32_rhs)
+                      int *Nijk, int *ijk, double **p, bool f32_rhs, bool static_metrics = false)
 {
     if (!c || !p) return CF_ERR_ARG;
     // the plane tables are a fixed function of the grid; the context holds
@@ -791,6 +828,11 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     cf_lu_args a;
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
     a.f32_rhs = (f32_rhs && kprec(c) == 1) ? 1 : 0;
+    if (static_metrics && kprec(c) == 1)
+        for (int n = 0; n < 9; n++) {
+            a.m32[n] = met32_get(c, a.m[n]);
+            if (!a.m32[n]) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: FP32 metric copy allocation failed");
+        }
     double *pack = nullptr;
     cf_wave_args w{};
     if (c->lu_schedule == CF_LU_WAVEFRONT) {
@@ -1079,6 +1121,11 @@ int cf_step_reset(cf_ctx *c)
 {
     if (!c) return CF_ERR_ARG;
     for (double &e : c->E) e = 0;
+    if (!c->met32.empty()) {
+        cudaStreamSynchronize(c->stream);
+        for (auto &m : c->met32) cudaFree(m.second);
+        c->met32.clear();
+    }
     return CF_OK;
 }
 
@@ -1147,6 +1194,8 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
     // pass the right-hand-side arrays as FP32 values (the caller's inF, vF,
     // LL/ML/NL are the loop's own scratch here)
     const bool f32_rhs = kprec(c) == 1;
+    // fixed metric arrays: their FP32 copies are made once and kept
+    const bool static_m = f32_rhs && pp->static_metrics != 0;
     c->er_hist.clear();
     int it = 1;
     for (;; it++) {
@@ -1169,12 +1218,12 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
             static const char *names[2][3] = {{"Flux_X", "Flux_Y", "Flux_Z"},
                                               {"Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter"}};
             if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32, dir > 0,
-                                     f32_rhs))
+                                     f32_rhs, static_m))
                 return rc;
         }
-        if (int rc = viscous_common(c, visc, f32_rhs)) return rc;
+        if (int rc = viscous_common(c, visc, f32_rhs, static_m)) return rc;
         if (int rc = dts_common(c, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr, nullptr, dts,
-                                f32_rhs)) return rc;
+                                f32_rhs, static_m)) return rc;
         for (int n = 0; n < 5; n++) {
             c->E[n] = std::max(c->E[n], er[n]);
             er[n] = er[n] / c->E[n];

@@ -42,6 +42,16 @@ __device__ __forceinline__ T rhs_get(const double *p, size_t q, int f32)
 }
 
 
+// a metric value in the compute type: from its FP32 copy when the caller
+// has one (the step driver's cache of the fixed metric arrays, FP32 build),
+// else from the FP64 array
+template <typename T>
+__device__ __forceinline__ T met_ld(const double *p, const float *p32, size_t q)
+{
+    if (sizeof(T) == 4 && p32) return T(p32[q]);
+    return T(p[q]);
+}
+
 // a grid constant of cf_dims in the compute type T (its FP32 copy for float)
 #define CF_DC(T, d, x) (sizeof(T) == 4 ? (T)((d).f_##x) : (T)((d).x))
 

@@ -15,6 +15,17 @@
 
 namespace CF_NS {
 
+// face metrics and face Jacobian of a flux kernel's arguments
+template <typename T>
+__device__ __forceinline__ T fmet(const cf_flux_args &a, int n, size_t q) { return T(a.m[n][q]); }
+template <typename T>
+__device__ __forceinline__ T fmet(const cf_flux_args_f &a, int n, size_t q) { return met_ld<T>(a.m[n], a.m32[n], q); }
+template <typename T>
+__device__ __forceinline__ T fjf(const cf_flux_args &a, size_t q) { return T(a.Jf[q]); }
+template <typename T>
+__device__ __forceinline__ T fjf(const cf_flux_args_f &a, size_t q) { return met_ld<T>(a.Jf, a.Jf32, q); }
+
+
 // ---------------------------------------------------------------------------
 // limiter pieces (Flux_X_limiter.cpp:149-159, 247-262)
 // ---------------------------------------------------------------------------
@@ -118,7 +129,7 @@ __device__ __forceinline__ void states_x_limited(const cf_dims &d, const A &a, i
                                                  int k, T *mL, T *mR)
 {
     const ptrdiff_t s = (ptrdiff_t)d.plane();
-    const T jf = T(a.Jf[d.ix(i, j, k)]);
+    const T jf = fjf<T>(a, d.ix(i, j, k));
     const size_t qL = d.ix(i, j + 1, k + 1), qR = d.ix(i + 1, j + 1, k + 1);
     const bool lo3 = (i <= 3) || (i >= d.gend);
     const bool hi3 = (i + 1 <= 3) || (i + 1 >= d.gend);
@@ -160,7 +171,7 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const A &a, i
 {
     const ptrdiff_t s = d.Zm;
     const int ny = d.ny;
-    const T jf = T(a.Jf[d.ix(i, j, k)]);
+    const T jf = fjf<T>(a, d.ix(i, j, k));
     const size_t qL = d.ix(i + 1, j, k + 1), qR = d.ix(i + 1, j + 1, k + 1);
     // left state: cell j (face 1 is the wall average of cells 1, 2)
     if (j == 1) {
@@ -551,11 +562,11 @@ __global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
     }
     const size_t q = d.ix(i, j, k);
 #pragma unroll
-    for (int n = 0; n < 9; n++) m[n] = T(a.m[n][q]);
+    for (int n = 0; n < 9; n++) m[n] = fmet<T>(a, n, q);
     if (LIMITED)
-        fast_flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), CF_DC(T, d, K), CF_DC(T, d, e), F);
+        fast_flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), fjf<T>(a, q), CF_DC(T, d, K), CF_DC(T, d, e), F);
     else
-        fast_flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), CF_DC(T, d, K), F);
+        fast_flux_roe<T>(mL, mR, m, DIR, fjf<T>(a, q), CF_DC(T, d, K), F);
 #else
     if (DIR == 0) {
         if (LIMITED) states_x_limited<T>(d, a, i, j, k, mL, mR);
@@ -569,11 +580,11 @@ __global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
     }
     const size_t q = d.ix(i, j, k);
 #pragma unroll
-    for (int n = 0; n < 9; n++) m[n] = T(a.m[n][q]);
+    for (int n = 0; n < 9; n++) m[n] = fmet<T>(a, n, q);
     if (LIMITED)
-        flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), T(a.Jf[q]), CF_DC(T, d, K), CF_DC(T, d, e), F);
+        flux_precond_roe<T>(mL, mR, m, DIR, T(a.Ep[q]), fjf<T>(a, q), CF_DC(T, d, K), CF_DC(T, d, e), F);
     else
-        flux_roe<T>(mL, mR, m, DIR, T(a.Jf[q]), CF_DC(T, d, K), F);
+        flux_roe<T>(mL, mR, m, DIR, fjf<T>(a, q), CF_DC(T, d, K), F);
 #endif
     const int f32 = a.f32_out;
     if (DIR == 1 && (j == 1 || j == d.ny)) {
@@ -669,8 +680,8 @@ __global__ void __launch_bounds__(256) k_flux_shadow(size_t n, cf_ptr5 U, const 
 
 // FP32 fluxes from the FP32 copies in sh (7 fields: U1..U5, J, 1/J);
 // convert = false reuses copies made by an earlier call for the same U, J
-inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, float *sh, bool convert, int dir,
-                                   bool limited, cudaStream_t s)
+inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, float *sh, bool convert,
+                                   const float *const *met32, int dir, bool limited, cudaStream_t s)
 {
     const size_t n = d.total();
     if (convert) {
@@ -686,6 +697,8 @@ inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, floa
     fa.wz[1] = nullptr;
     fa.Jf = a.Jf;
     for (int v = 0; v < 9; v++) fa.m[v] = a.m[v];
+    fa.Jf32 = met32 ? met32[0] : nullptr;
+    for (int v = 0; v < 9; v++) fa.m32[v] = met32 ? met32[1 + v] : nullptr;
     fa.Ep = a.Ep;
     for (int v = 0; v < 5; v++) fa.F[v] = a.F[v];
     fa.f32_out = a.f32_out;

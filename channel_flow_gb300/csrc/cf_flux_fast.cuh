@@ -118,7 +118,7 @@ __device__ __forceinline__ void fast_states_x_limited(const cf_dims &d, const A 
                                                       int k, T *mL, T *mR)
 {
     const ptrdiff_t s = (ptrdiff_t)d.plane();
-    const T jf = T(a.Jf[d.ix(i, j, k)]);
+    const T jf = fjf<T>(a, d.ix(i, j, k));
     const size_t qc = d.ix(i, j + 1, k + 1);
     const bool lo3 = (i <= 3) || (i >= d.gend);
     const bool hi3 = (i + 1 <= 3) || (i + 1 >= d.gend);
@@ -136,7 +136,7 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A 
 {
     const ptrdiff_t s = d.Zm;
     const int ny = d.ny;
-    const T jf = T(a.Jf[d.ix(i, j, k)]);
+    const T jf = fjf<T>(a, d.ix(i, j, k));
     const size_t qL = d.ix(i + 1, j, k + 1), qR = qL + s;
     const bool wallL = (j <= 2) || (j >= ny - 1);
     const bool wallR = (j + 1 <= 2) || (j + 1 >= ny - 1);

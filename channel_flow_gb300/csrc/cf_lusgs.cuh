@@ -88,9 +88,9 @@ __device__ __forceinline__ ldiag<T> lu_diag(const cf_dims &d, const cf_lu_args &
                                             T deltaT)
 {
     const T K = CF_DC(T, d, K);
-    T xix = T(a.m[0][q]), xiy = T(a.m[1][q]), xiz = T(a.m[2][q]);
-    T etx = T(a.m[3][q]), ety = T(a.m[4][q]), etz = T(a.m[5][q]);
-    T ztx = T(a.m[6][q]), zty = T(a.m[7][q]), ztz = T(a.m[8][q]);
+    T xix = met_ld<T>(a.m[0], a.m32[0], q), xiy = met_ld<T>(a.m[1], a.m32[1], q), xiz = met_ld<T>(a.m[2], a.m32[2], q);
+    T etx = met_ld<T>(a.m[3], a.m32[3], q), ety = met_ld<T>(a.m[4], a.m32[4], q), etz = met_ld<T>(a.m[5], a.m32[5], q);
+    T ztx = met_ld<T>(a.m[6], a.m32[6], q), zty = met_ld<T>(a.m[7], a.m32[7], q), ztz = met_ld<T>(a.m[8], a.m32[8], q);
     T beta = s.beta, C = s.C;
     T U = xix * s.u + xiy * s.v + xiz * s.w;
     T V = etx * s.u + ety * s.v + etz * s.w;
@@ -274,9 +274,9 @@ __device__ __forceinline__ void lu_lower(const cf_dims &d, const cf_lu_args &a, 
 {
     const T K = CF_DC(T, d, K);
     const size_t qa = d.ix(i - 1, j, k), qb = d.ix(i, j - 1, k), qc = d.ix(i, j, k - 1);
-    lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
-    lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
-    lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), T(a.m[6][qc]), T(a.m[7][qc]), T(a.m[8][qc]), false, K);
+    lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), met_ld<T>(a.m[0], a.m32[0], qa), met_ld<T>(a.m[1], a.m32[1], qa), met_ld<T>(a.m[2], a.m32[2], qa), true, K);
+    lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), met_ld<T>(a.m[3], a.m32[3], qb), met_ld<T>(a.m[4], a.m32[4], qb), met_ld<T>(a.m[5], a.m32[5], qb), false, K);
+    lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), met_ld<T>(a.m[6], a.m32[6], qc), met_ld<T>(a.m[7], a.m32[7], qc), met_ld<T>(a.m[8], a.m32[8], qc), false, K);
     T va[5], vb[5], vc[5];
     lu_load5<T>(N, qa, va);
     lu_load5<T>(N, qb, vb);
@@ -291,9 +291,9 @@ __device__ __forceinline__ void lu_upper(const cf_dims &d, const cf_lu_args &a, 
 {
     const T K = CF_DC(T, d, K);
     const size_t qa = d.ix(i + 1, j, k), qb = d.ix(i, j + 1, k), qc = d.ix(i, j, k + 1);
-    lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), T(a.m[0][qa]), T(a.m[1][qa]), T(a.m[2][qa]), true, K);
-    lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), T(a.m[3][qb]), T(a.m[4][qb]), T(a.m[5][qb]), false, K);
-    lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), T(a.m[6][qc]), T(a.m[7][qc]), T(a.m[8][qc]), false, K);
+    lsplit<T> A = lu_split<T>(lu_state<T>(d, a, qa), met_ld<T>(a.m[0], a.m32[0], qa), met_ld<T>(a.m[1], a.m32[1], qa), met_ld<T>(a.m[2], a.m32[2], qa), true, K);
+    lsplit<T> B = lu_split<T>(lu_state<T>(d, a, qb), met_ld<T>(a.m[3], a.m32[3], qb), met_ld<T>(a.m[4], a.m32[4], qb), met_ld<T>(a.m[5], a.m32[5], qb), false, K);
+    lsplit<T> C = lu_split<T>(lu_state<T>(d, a, qc), met_ld<T>(a.m[6], a.m32[6], qc), met_ld<T>(a.m[7], a.m32[7], qc), met_ld<T>(a.m[8], a.m32[8], qc), false, K);
     T va[5], vb[5], vc[5];
     lu_load5<T>(N, qa, va);
     lu_load5<T>(N, qb, vb);
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(256) k_lu_pack(cf_dims d, cf_lu_args a, double
     double *P = pack + q * LU_PACK;
 #pragma unroll
     for (int dir = 0; dir < 3; dir++) {
-        const lsplit<T> A = lu_split<T>(s, T(a.m[3 * dir][q]), T(a.m[3 * dir + 1][q]), T(a.m[3 * dir + 2][q]),
+        const lsplit<T> A = lu_split<T>(s, met_ld<T>(a.m[3 * dir], a.m32[3 * dir], q), met_ld<T>(a.m[3 * dir + 1], a.m32[3 * dir + 1], q), met_ld<T>(a.m[3 * dir + 2], a.m32[3 * dir + 2], q),
                                         dir == 0, K);
         double2 *o = reinterpret_cast<double2 *>(P + 16 * dir);
         o[0] = make_double2(double(A.p11), double(A.p22));

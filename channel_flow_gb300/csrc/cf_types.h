@@ -87,6 +87,7 @@ struct cf_flux_args_f {
     const float *wz[2];   // wz[0]: 1/J per cell
     int f32_out;          // inF hold FP32 values
     int reserved;
+    const float *Jf32, *m32[9];   // FP32 copies of Jf and m (or null)
 };
 
 struct cf_visc_args {
@@ -99,6 +100,7 @@ struct cf_visc_args {
     double *prim[4];           // scratch: u, v, w, T of every cell
     int f32_io;                // FP32 build: LL/ML/NL and vF hold FP32 values (the step driver's internal use)
     int reserved;
+    const float *Jf32[3], *mf32[3][9];   // FP32 copies of the face sets (or null)
 };
 
 struct cf_filter_args {
@@ -124,6 +126,7 @@ struct cf_lu_args {
     double *partial;         // scratch: per-block partial norm sums (5 per block)
     int f32_rhs;             // FP32 build: Fx/Fy/Fz and vF hold FP32 values (the step driver's internal use)
     int reserved;
+    const float *m32[9];     // FP32 copies of the cell metrics (or null)
 };
 
 // tiled wavefront of the hyperplane sweeps (cf_wave.cuh)

@@ -50,16 +50,31 @@ cudaError_t flux(const cf_dims &d, const cf_flux_args &a, int dir, bool limited,
     return prec == 1 ? cudaErrorNotSupported : launch_flux<double>(d, a, dir, limited, s);
 }
 
-// shadow: 7 FP32 fields (U1..U5, J, 1/J) of d.total() values each
-cudaError_t flux_f32(const cf_dims &d, const cf_flux_args &a, float *shadow, bool convert, int dir, bool limited,
-                     cudaStream_t s)
+// shadow: 7 FP32 fields (U1..U5, J, 1/J) of d.total() values each; met32:
+// FP32 copies of J_f and the 9 face metrics, or null
+cudaError_t flux_f32(const cf_dims &d, const cf_flux_args &a, float *shadow, bool convert, const float *const *met32,
+                     int dir, bool limited, cudaStream_t s)
 {
 #ifdef CF_WITH_FLOAT
-    return launch_flux_f32(d, a, shadow, convert, dir, limited, s);
+    return launch_flux_f32(d, a, shadow, convert, met32, dir, limited, s);
 #else
-    (void)d; (void)a; (void)shadow; (void)convert; (void)dir; (void)limited; (void)s;
+    (void)d; (void)a; (void)shadow; (void)convert; (void)met32; (void)dir; (void)limited; (void)s;
     return cudaErrorNotSupported;
 #endif
+}
+
+__global__ void k_to_f32(size_t n, const double *__restrict__ src, float *__restrict__ dst)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) dst[q] = float(src[q]);
+}
+
+// dst[0..n) = src rounded to FP32
+cudaError_t to_f32(size_t n, const double *src, float *dst, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_to_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, dst);
+    return cudaGetLastError();
 }
 
 cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStream_t s)

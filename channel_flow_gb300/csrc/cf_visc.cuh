@@ -175,12 +175,13 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         vgrad<T> Y = g4<T>(jp, imjp, jm, imjm, imjp, inv4ET);
         vgrad<T> Z = g4<T>(kp, imkp, km, imkm, imkp, inv4ZT);
         const double *const *m = a.mf[0];
-        T m0 = T(m[0][f]), m1 = T(m[1][f]), m2 = T(m[2][f]);
+        const float *const *m32 = a.mf32[0];
+        T m0 = met_ld<T>(m[0], m32[0], f), m1 = met_ld<T>(m[1], m32[1], f), m2 = met_ld<T>(m[2], m32[2], f);
         vsym<T> A = csym<T>(m0, m1, m2);
-        vcross<T> D = ccross<T>(m0, m1, m2, T(m[3][f]), T(m[4][f]), T(m[5][f]));
-        vcross<T> E = ccross<T>(m0, m1, m2, T(m[6][f]), T(m[7][f]), T(m[8][f]));
+        vcross<T> D = ccross<T>(m0, m1, m2, met_ld<T>(m[3], m32[3], f), met_ld<T>(m[4], m32[4], f), met_ld<T>(m[5], m32[5], f));
+        vcross<T> E = ccross<T>(m0, m1, m2, met_ld<T>(m[6], m32[6], f), met_ld<T>(m[7], m32[7], f), met_ld<T>(m[8], m32[8], f));
         T Ux = T(0.5) * (c.u + im.u), Vx = T(0.5) * (c.v + im.v), Wx = T(0.5) * (c.w + im.w);
-        T Jf = T(a.Jf[0][f]);
+        T Jf = met_ld<T>(a.Jf[0], a.Jf32[0], f);
 #ifdef CF_FAST_MATH
         const T iJf = T(1) / Jf;
 #endif
@@ -199,13 +200,14 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         vgrad<T> Y = g2<T>(c, jm, invET);
         vgrad<T> Z = g4<T>(kp, jmkp, km, jmkm, jmkp, inv4ZT);
         const double *const *m = a.mf[1];
-        T m0 = T(m[0][f]), m1 = T(m[1][f]), m2 = T(m[2][f]);
-        T e0 = T(m[3][f]), e1 = T(m[4][f]), e2 = T(m[5][f]);
+        const float *const *m32 = a.mf32[1];
+        T m0 = met_ld<T>(m[0], m32[0], f), m1 = met_ld<T>(m[1], m32[1], f), m2 = met_ld<T>(m[2], m32[2], f);
+        T e0 = met_ld<T>(m[3], m32[3], f), e1 = met_ld<T>(m[4], m32[4], f), e2 = met_ld<T>(m[5], m32[5], f);
         vsym<T> B = csym<T>(e0, e1, e2);
         vcross<T> D = ccross<T>(m0, m1, m2, e0, e1, e2);
-        vcross<T> F = ccross<T>(e0, e1, e2, T(m[6][f]), T(m[7][f]), T(m[8][f]));
+        vcross<T> F = ccross<T>(e0, e1, e2, met_ld<T>(m[6], m32[6], f), met_ld<T>(m[7], m32[7], f), met_ld<T>(m[8], m32[8], f));
         T Uy = T(0.5) * (c.u + jm.u), Vy = T(0.5) * (c.v + jm.v), Wy = T(0.5) * (c.w + jm.w);
-        T Jf = T(a.Jf[1][f]);
+        T Jf = met_ld<T>(a.Jf[1], a.Jf32[1], f);
 #ifdef CF_FAST_MATH
         const T iJf = T(1) / Jf;
 #endif
@@ -225,12 +227,13 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         vgrad<T> Y = g4<T>(jp, jpkm, jm, jmkm, imjp, inv4ET);
         vgrad<T> Z = g2<T>(c, km, invZT);
         const double *const *m = a.mf[2];
-        T z0 = T(m[6][f]), z1 = T(m[7][f]), z2 = T(m[8][f]);
+        const float *const *m32 = a.mf32[2];
+        T z0 = met_ld<T>(m[6], m32[6], f), z1 = met_ld<T>(m[7], m32[7], f), z2 = met_ld<T>(m[8], m32[8], f);
         vsym<T> Cc = csym<T>(z0, z1, z2);
-        vcross<T> E = ccross<T>(T(m[0][f]), T(m[1][f]), T(m[2][f]), z0, z1, z2);
-        vcross<T> F = ccross<T>(T(m[3][f]), T(m[4][f]), T(m[5][f]), z0, z1, z2);
+        vcross<T> E = ccross<T>(met_ld<T>(m[0], m32[0], f), met_ld<T>(m[1], m32[1], f), met_ld<T>(m[2], m32[2], f), z0, z1, z2);
+        vcross<T> F = ccross<T>(met_ld<T>(m[3], m32[3], f), met_ld<T>(m[4], m32[4], f), met_ld<T>(m[5], m32[5], f), z0, z1, z2);
         T Uz = T(0.5) * (c.u + km.u), Vz = T(0.5) * (c.v + km.v), Wz = T(0.5) * (c.w + km.w);
-        T Jf = T(a.Jf[2][f]);
+        T Jf = met_ld<T>(a.Jf[2], a.Jf32[2], f);
 #ifdef CF_FAST_MATH
         const T iJf = T(1) / Jf;
 #endif

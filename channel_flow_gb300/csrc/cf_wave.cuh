@@ -141,7 +141,7 @@ template <typename T>
 __device__ __forceinline__ lsplit<T> wave_split(const cf_dims &d, const cf_lu_args &a, size_t q, const lstate<T> &s,
                                                 int dir)
 {
-    return lu_split<T>(s, T(a.m[3 * dir][q]), T(a.m[3 * dir + 1][q]), T(a.m[3 * dir + 2][q]), dir == 0, CF_DC(T, d, K));
+    return lu_split<T>(s, met_ld<T>(a.m[3 * dir], a.m32[3 * dir], q), met_ld<T>(a.m[3 * dir + 1], a.m32[3 * dir + 1], q), met_ld<T>(a.m[3 * dir + 2], a.m32[3 * dir + 2], q), dir == 0, CF_DC(T, d, K));
 }
 
 // face slots: x face cell (lj, lk) -> lj*8 + lk, y face (li, lk) -> li*8 + lk,

@@ -30,6 +30,10 @@ class Stepper:
         self.ctx = ctx
         self.f = fields
         self.online = online
+        # a new run: the residual maxima start over, and the metric arrays
+        # are fixed for the run (the FP32 path keeps FP32 copies of them)
+        ctx.step_reset()
+        step_kw.setdefault("static_metrics", True)
         self.kw = step_kw
         self.n = 0
         self.hist = deque(maxlen=3)

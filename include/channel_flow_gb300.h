@@ -311,6 +311,9 @@ typedef struct {
     int filter;                /* 1: Filter (its Ep switches the limited fluxes' dissipation) */
     double roe_criterion, e_high, e_low;
     int statistic_step;        /* > 0: Statistic after the step */
+    int static_metrics;        /* 1: the metric arrays (J, cell and face metrics) stay unchanged between
+                                  cf_step calls, so the FP32 path converts them to FP32 once and keeps
+                                  the copies (cf_step_reset drops them) */
 } cf_step_params;
 
 /* One physical time step: pseudo-time iterations of x halo, wall and
@@ -324,7 +327,7 @@ typedef struct {
  * its scratch and hold FP32 values in their FP64 allocation afterwards. */
 int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields *fields, int *iterations,
             double *er, double *Q);
-/* forget the running residual maxima */
+/* forget the running residual maxima and the FP32 metric copies */
 int cf_step_reset(cf_ctx *ctx);
 /* read (set = 0) or replace (set = 1) the running residual maxima E1..E5 */
 int cf_step_scale(cf_ctx *ctx, double *E, int set);
