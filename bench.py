@@ -282,10 +282,12 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess physical-step comparison")
     ap.add_argument("--no-wavy", action="store_true", help="skip the 512x256x384 wavy-wall measurement")
-    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs", "mlp"],
+    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs", "mlp", "physical"],
                     help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
                          "(one LU-SGS pseudo-iteration per step, for profiling); mlp: the learned guess's "
-                         "tensor-core GEMMs on --mlp-rows feature rows")
+                         "tensor-core GEMMs on --mlp-rows feature rows; physical: whole physical steps "
+                         "(cf_step, sub-iterations to the 1e-6 tolerance, extrapolated start) of the stable "
+                         "scheme, for profiling")
     ap.add_argument("--mlp-rows", type=int, default=2097152, help="rows (cells) of the --step mlp GEMMs")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
@@ -327,6 +329,12 @@ def main():
     if args.step == "mlp":
         torch.cuda.set_device(local)
         r = mlp_gemms(torch, args.mlp_rows, max(2, args.steps), max(1, args.warmup))
+        if rank == 0:
+            print(json.dumps(r))
+        return 0
+    if args.step == "physical":
+        torch.cuda.set_device(local)
+        r = physical_steps(torch, g, args.precision, args.steps, args.warmup)
         if rank == 0:
             print(json.dumps(r))
         return 0
@@ -506,6 +514,37 @@ def stat_profiles(acc, g, steps):
     U, V, W = row("U"), row("V"), row("W")
     return {"U": U, "V": V, "W": W, "uu": row("UU") - U * U, "vv": row("VV") - V * V,
             "ww": row("WW") - W * W, "uv": row("UV") - U * V}
+
+
+def physical_steps(torch, g, precision, steps, warmup):
+    """`warmup` then `steps` timed physical steps (cf_step to the tolerance
+    1e-6 from the extrapolated start) of the stable scheme on grid g: CUDA
+    event time per step and per sub-iteration."""
+    import channel_flow_gb300 as cf
+    from channel_flow_gb300 import stepper, synthetic as syn
+    cm = syn.flat_metrics(g, GAMMA, "cell")
+    J = cm["J"]
+    host = {"U": syn.channel_state(g, J, seed=SEED, mach=0.05, noise=0.01, jitter=0.001, gamma=GAMMA),
+            "J": J, "cm": [cm[n] for n in syn.METRIC_NAMES], "Yp": syn.y_points(g, gamma=GAMMA)}
+    ctx = cf.Context(g, precision=precision, gamma=GAMMA)
+    w = DeviceWorkload(ctx, g, host, torch)
+    st = stepper.Stepper(ctx, stepper.fields_from_workload(w, torch, g), deltaT=5e-9, max_iterations=200,
+                         tolerance=1e-6, limiter=False, filter=False)
+    for _ in range(max(warmup, 3)):
+        st.step("extrapolate")
+    its, ms = [], []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        it = st.step("extrapolate")[0]
+        e1.record()
+        torch.cuda.synchronize()
+        its.append(it)
+        ms.append(e0.elapsed_time(e1))
+    ctx.close()
+    return {"step": "physical", "grid": [g.X_out, g.Y_out, g.Z_out], "precision": precision,
+            "subiterations": its, "ms_per_step": ms, "ms_per_subiteration": sum(ms) / max(1, sum(its))}
 
 
 def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=12, evals=3, tolerance=1e-6,
