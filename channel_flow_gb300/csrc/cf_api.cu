@@ -616,7 +616,7 @@ static int lu_args(cf_ctx *c, double **p, const char *who, cf_lu_args &a)
     for (int n = 0; n < 9; n++) a.m[n] = R(c, p[16 + n]);
     for (int n = 0; n < 4; n++) a.vF[n] = R(c, p[40 + n]);
     a.f32_rhs = 0;
-    a.reserved = 0;
+    a.f32_lu = 0;
     for (int n = 0; n < 9; n++) a.m32[n] = nullptr;
     cf_dims &d = c->d;
     const size_t np = cf_fast::lu_partial_count(d);
@@ -828,6 +828,9 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     cf_lu_args a;
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
     a.f32_rhs = (f32_rhs && kprec(c) == 1) ? 1 : 0;
+    // with the wavefront, MR, NL and NR pass between the step driver's own
+    // FP32 kernels only (the fused update reads NR from shared memory)
+    a.f32_lu = (a.f32_rhs && c->lu_schedule == CF_LU_WAVEFRONT) ? 1 : 0;
     if (static_metrics && kprec(c) == 1)
         for (int n = 0; n < 9; n++) {
             a.m32[n] = met32_get(c, a.m[n]);

@@ -191,14 +191,15 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     T MR3 = (d31 * Rk[0] + d22 * Rk[2]);
     T MR4 = (d41 * Rk[0] + d22 * Rk[3]);
     T MR5 = (d51 * Rk[0] + d52 * Rk[1] + d53 * Rk[2] + d54 * Rk[3] + d55 * Rk[4]);
-    a.MR[0][q] = double(MR1); a.MR[1][q] = double(MR2); a.MR[2][q] = double(MR3);
-    a.MR[3][q] = double(MR4); a.MR[4][q] = double(MR5);
+    const int f32 = a.f32_lu;
+    rhs_put<T>(a.MR[0], q, MR1, f32); rhs_put<T>(a.MR[1], q, MR2, f32); rhs_put<T>(a.MR[2], q, MR3, f32);
+    rhs_put<T>(a.MR[3], q, MR4, f32); rhs_put<T>(a.MR[4], q, MR5, f32);
     ldiag<T> g = lu_diag<T>(d, a, q, s, deltaT);
     T nl[5] = {g.d11 * MR1, g.d22 * MR2, g.d22 * MR3, g.d22 * MR4, g.d51 * MR1 + g.d22 * MR5};
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        a.NL[n][q] = double(nl[n]);
-        if (copy_nr) a.NR[n][q] = double(nl[n]);
+        rhs_put<T>(a.NL[n], q, nl[n], f32);
+        if (copy_nr) rhs_put<T>(a.NR[n], q, nl[n], f32);
     }
 }
 
@@ -500,7 +501,8 @@ __device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_arg
     const double K = d.K, Jq = a.J[q];
     double rhoold = a.U_[0][q] * Jq;
 #ifdef CF_FAST_MATH
-    // FP64 with four divisions instead of ten (reciprocals of U1, J)
+    // FP64 with three divisions instead of ten (reciprocals of U1 and J,
+    // 1/(K-1) from the host, 1/rho_old = (1/U1)(1/J))
     const double iu1 = 1.0 / a.U_[0][q], iJ = 1.0 / Jq;
     double Uold = a.U_[1][q] * iu1;
     double Vold = a.U_[2][q] * iu1;
@@ -512,7 +514,11 @@ __device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_arg
 #endif
     double VVold = Uold * Uold + Vold * Vold + Wold * Wold;
     double Pold = (a.U_[4][q] * Jq - 0.5 * rhoold * VVold) * (K - 1);
+#ifdef CF_FAST_MATH
+    double Told = Pold * (iu1 * iJ);
+#else
     double Told = Pold / rhoold;
+#endif
     double P = Pold + nr[0] * Jq;
     double U = Uold + nr[1] * Jq;
     double V = Vold + nr[2] * Jq;
@@ -525,7 +531,7 @@ __device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_arg
     a.U_[1][q] = rJ * U;
     a.U_[2][q] = rJ * V;
     a.U_[3][q] = rJ * W;
-    a.U_[4][q] = (P * (1.0 / (K - 1)) + 0.5 * rho * (U * U + V * V + W * W)) * iJ;
+    a.U_[4][q] = (P * d.ikm1 + 0.5 * rho * (U * U + V * V + W * W)) * iJ;
 #else
     a.U_[0][q] = rho / Jq;
     a.U_[1][q] = rho * U / Jq;

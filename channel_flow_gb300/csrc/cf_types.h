@@ -22,6 +22,7 @@ struct cf_dims {
     // the same constants rounded to FP32, for the FP32 kernels (a per-thread
     // FP64 -> FP32 conversion of a kernel parameter issues to the FP64 pipe)
     float f_dXI, f_dET, f_dZT, f_K, f_R, f_e, f_Cv, f_mu_L, f_Pr_L, f_f, f_high;
+    double ikm1;              // 1 / (K - 1), for the contracted build's state update
 
     __host__ __device__ __forceinline__ size_t ix(int i, int j, int k) const
     {
@@ -37,6 +38,7 @@ static inline void cf_dims_fill_f32(cf_dims &d)
     d.f_dXI = (float)d.dXI; d.f_dET = (float)d.dET; d.f_dZT = (float)d.dZT;
     d.f_K = (float)d.K; d.f_R = (float)d.R; d.f_e = (float)d.e; d.f_Cv = (float)d.Cv;
     d.f_mu_L = (float)d.mu_L; d.f_Pr_L = (float)d.Pr_L; d.f_f = (float)d.f; d.f_high = (float)d.high;
+    d.ikm1 = 1.0 / (d.K - 1.0);
 }
 
 struct cf_ptr5 {
@@ -125,7 +127,7 @@ struct cf_lu_args {
     double *MR[5], *NR[5], *NL[5], *Res[5];
     double *partial;         // scratch: per-block partial norm sums (5 per block)
     int f32_rhs;             // FP32 build: Fx/Fy/Fz and vF hold FP32 values (the step driver's internal use)
-    int reserved;
+    int f32_lu;              // FP32 build, wavefront: MR, NL, NR hold FP32 values (the step driver)
     const float *m32[9];     // FP32 copies of the cell metrics (or null)
 };
 

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
         }
         P[36 * WV_CELLS] = g.d11; P[37 * WV_CELLS] = g.d22; P[38 * WV_CELLS] = g.d51;
 #pragma unroll
-        for (int n = 0; n < 5; n++) P[(39 + n) * WV_CELLS] = T(a.MR[n][q]);
+        for (int n = 0; n < 5; n++) P[(39 + n) * WV_CELLS] = rhs_get<T>(a.MR[n], q, a.f32_lu);
     }
     const unsigned bytes = (unsigned)(WV_CELLS * WV_PACK * sizeof(T));
     __syncthreads();
@@ -528,8 +528,8 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
             if (FWD) static_cast<T *>(w.nl)[(size_t)tile * WV_SM_NL + v] = x;
             if (li < ti && lj < tj && lk < tk) {
                 const size_t q = d.ix(i0 + li, j0 + lj, k0 + lk);
-                if (FWD) a.NL[n][q] = double(x);
-                else a.NR[n][q] = double(x);
+                if (FWD) rhs_put<T>(a.NL[n], q, x, a.f32_lu);
+                else rhs_put<T>(a.NR[n], q, x, a.f32_lu);
             }
         }
         if (!FWD && w.partial) {
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
 #pragma unroll
                     for (int n = 0; n < 5; n++) {
                         nr[n] = double(sN[n * WV_CELLS + c]);
-                        a.NL[n][q] = nr[n];
+                        rhs_put<T>(a.NL[n], q, sN[n * WV_CELLS + c], a.f32_lu);
                     }
                     lu_update_cell(d, a, q, nr, rr);
 #pragma unroll

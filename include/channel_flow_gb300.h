@@ -323,8 +323,8 @@ typedef struct {
  * or max_iterations; then Driven_force (Q), Statistic when
  * statistic_step > 0, and Uq <- U, U <- U_.  Returns the iteration count,
  * the last normalised er1..er5 and Q (pointers may be NULL).  In
- * CF_PREC_FP32 the loop's right-hand-side arrays (inF, vF, LL, ML, NL) are
- * its scratch and hold FP32 values in their FP64 allocation afterwards. */
+ * CF_PREC_FP32 the loop's intermediate arrays (inF, vF, LL, ML, MR, NR, NL)
+ * are its scratch and hold FP32 values in their FP64 allocation afterwards. */
 int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields *fields, int *iterations,
             double *er, double *Q);
 /* forget the running residual maxima and the FP32 metric copies */
