@@ -738,19 +738,25 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
     const cf_dims &d = c->d;
     const bool ex = exact(c);
     const int pr = ex ? 0 : kprec(c);
-    cudaError_t e = ex ? cf_exact::lu_prepare(d, a, dt, true, 0, s) : cf_fast::lu_prepare(d, a, dt, true, pr, s);
+    cudaError_t e = cudaSuccess;
     if (c->lu_schedule == CF_LU_WAVEFRONT) {
+        // FP64: the assembly happens inside the forward tile pack (one pass
+        // over the cells less); FP32: its own box kernel, which measured
+        // faster than the heavier FP32 pack kernel doing both
+        const bool asm_in_pack = pr != 1;
+        e = asm_in_pack ? (ex ? cf_exact::lu_zero(d, a, s) : cf_fast::lu_zero(d, a, s))
+                        : cf_fast::lu_prepare(d, a, dt, true, pr, s);
         const size_t fl = ((size_t)w.ntiles + 1) * sizeof(int);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.err, 0, sizeof(int), s);
-        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, false, 0, s)
-                                     : cf_fast::lu_wave_pack(d, a, w, dt, false, pr, s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, false, true, 0, s)
+                                     : cf_fast::lu_wave_pack(d, a, w, dt, false, asm_in_pack, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, w, true, 0, s)
                                      : cf_fast::lu_wave_sweep(a, w, true, pr, s);
         cf_wave_args wb = w;
         if (w.trace) wb.trace = w.trace + 4 * (size_t)w.ntiles;
-        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, 0, s)
-                                     : cf_fast::lu_wave_pack(d, a, w, dt, true, pr, s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, false, 0, s)
+                                     : cf_fast::lu_wave_pack(d, a, w, dt, true, false, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
         // FP32: the backward sweep also updates the state (FP64), copies
         // NL <- NR and leaves per-tile norm partial sums; its blocks have
@@ -765,6 +771,7 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
             return e;
         }
     } else {
+        e = ex ? cf_exact::lu_prepare(d, a, dt, true, 0, s) : cf_fast::lu_prepare(d, a, dt, true, pr, s);
         if (e == cudaSuccess) e = ex ? cf_exact::lu_pack(d, a, pack, dt, 0, s) : cf_fast::lu_pack(d, a, pack, dt, pr, s);
         const int mlast = d.gend + d.ny + d.nz;
         for (int m = 7; m <= mlast && e == cudaSuccess; m++) {

@@ -134,14 +134,13 @@ __global__ void k_lu_zero(cf_dims d, cf_lu_args a, size_t n)
     }
 }
 
-// BDF2 residual, Gamma^-1 R and the diagonal solve (Dual_time_stepping.cpp:339-506)
+// BDF2 residual R and MR = Gamma^-1 R of cell (i, j, k) at q, from its
+// state s (Dual_time_stepping.cpp:339-490)
 template <typename T>
-__global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf_box b, double dt, int copy_nr)
+__device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int i, int j, int k, size_t q,
+                                      double dt, const lstate<T> &s, T *MR)
 {
-    CF_BOX_INDEX(b, i, j, k);
-    const size_t q = d.ix(i, j, k);
-    const T K = CF_DC(T, d, K), deltaT = T(dt);
-    lstate<T> s = lu_state<T>(d, a, q);
+    const T K = CF_DC(T, d, K);
     T rho = s.rho, u = s.u, v = s.v, w = s.w, VV = s.VV, Tt = s.Tt, H = s.H, beta = s.beta;
     T temp = rho * K;
     T d11 = -(H * (K - T(1)) + VV - K * (Tt + VV)) * beta;
@@ -186,16 +185,28 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     Rk[2] = Rk[2] + rhs_get<T>(a.vF[1], q, a.f32_rhs);
     Rk[3] = Rk[3] + rhs_get<T>(a.vF[2], q, a.f32_rhs);
     Rk[4] = Rk[4] + rhs_get<T>(a.vF[3], q, a.f32_rhs) + f * u / Jq;
-    T MR1 = (d11 * Rk[0] + d12 * Rk[1] + d13 * Rk[2] + d14 * Rk[3] + d15 * Rk[4]);
-    T MR2 = (d21 * Rk[0] + d22 * Rk[1]);
-    T MR3 = (d31 * Rk[0] + d22 * Rk[2]);
-    T MR4 = (d41 * Rk[0] + d22 * Rk[3]);
-    T MR5 = (d51 * Rk[0] + d52 * Rk[1] + d53 * Rk[2] + d54 * Rk[3] + d55 * Rk[4]);
+    MR[0] = (d11 * Rk[0] + d12 * Rk[1] + d13 * Rk[2] + d14 * Rk[3] + d15 * Rk[4]);
+    MR[1] = (d21 * Rk[0] + d22 * Rk[1]);
+    MR[2] = (d31 * Rk[0] + d22 * Rk[2]);
+    MR[3] = (d41 * Rk[0] + d22 * Rk[3]);
+    MR[4] = (d51 * Rk[0] + d52 * Rk[1] + d53 * Rk[2] + d54 * Rk[3] + d55 * Rk[4]);
+}
+
+// BDF2 residual, Gamma^-1 R and the diagonal solve (Dual_time_stepping.cpp:339-506)
+template <typename T>
+__global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf_box b, double dt, int copy_nr)
+{
+    CF_BOX_INDEX(b, i, j, k);
+    const size_t q = d.ix(i, j, k);
+    const T deltaT = T(dt);
+    lstate<T> s = lu_state<T>(d, a, q);
+    T MR[5];
+    lu_mr<T>(d, a, i, j, k, q, dt, s, MR);
     const int f32 = a.f32_lu;
-    rhs_put<T>(a.MR[0], q, MR1, f32); rhs_put<T>(a.MR[1], q, MR2, f32); rhs_put<T>(a.MR[2], q, MR3, f32);
-    rhs_put<T>(a.MR[3], q, MR4, f32); rhs_put<T>(a.MR[4], q, MR5, f32);
+#pragma unroll
+    for (int n = 0; n < 5; n++) rhs_put<T>(a.MR[n], q, MR[n], f32);
     ldiag<T> g = lu_diag<T>(d, a, q, s, deltaT);
-    T nl[5] = {g.d11 * MR1, g.d22 * MR2, g.d22 * MR3, g.d22 * MR4, g.d51 * MR1 + g.d22 * MR5};
+    T nl[5] = {g.d11 * MR[0], g.d22 * MR[1], g.d22 * MR[2], g.d22 * MR[3], g.d51 * MR[0] + g.d22 * MR[4]};
 #pragma unroll
     for (int n = 0; n < 5; n++) {
         rhs_put<T>(a.NL[n], q, nl[n], f32);

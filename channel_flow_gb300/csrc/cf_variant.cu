@@ -169,7 +169,7 @@ cudaError_t lu_plane_packed(const cf_dims &d, const cf_lu_args &a, const double 
 
 template <typename T>
 static cudaError_t lu_wave_pack_t(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt,
-                                  bool upper, cudaStream_t s)
+                                  bool upper, bool assemble, cudaStream_t s)
 {
     if (upper) {
         cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
@@ -177,16 +177,26 @@ static cudaError_t lu_wave_pack_t(const cf_dims &d, const cf_lu_args &a, const c
         return cudaGetLastError();
     }
     const size_t smem = (size_t)WV_CELLS * WV_PACK * sizeof(T);
-    cudaError_t e = cudaFuncSetAttribute(k_lu_tile_pack<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    void (*kf)(cf_lu_args, wave_args, double) = assemble ? k_lu_tile_pack<T, true> : k_lu_tile_pack<T, false>;
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_lu_tile_pack<T><<<w.ntiles, WV_CELLS, smem, s>>>(a, w, dt);
+    kf<<<w.ntiles, WV_CELLS, smem, s>>>(a, w, dt);
     return cudaGetLastError();
 }
+// assemble: the forward pack also assembles MR (no lu_prepare assembly pass)
 cudaError_t lu_wave_pack(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt, bool upper,
-                         int prec, cudaStream_t s)
+                         bool assemble, int prec, cudaStream_t s)
 {
-    return CF_DISPATCH(prec, lu_wave_pack_t<double>(d, a, w, dt, upper, s),
-                       lu_wave_pack_t<float>(d, a, w, dt, upper, s));
+    return CF_DISPATCH(prec, lu_wave_pack_t<double>(d, a, w, dt, upper, assemble, s),
+                       lu_wave_pack_t<float>(d, a, w, dt, upper, assemble, s));
+}
+
+// the zeroing of lu_prepare alone (NL, NR of every index, ghosts included)
+cudaError_t lu_zero(const cf_dims &d, const cf_lu_args &a, cudaStream_t s)
+{
+    const size_t n = d.total();
+    k_lu_zero<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
+    return cudaGetLastError();
 }
 
 template <typename T>

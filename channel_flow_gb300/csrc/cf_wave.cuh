@@ -218,7 +218,10 @@ __device__ __forceinline__ void wave_bulk_store(void *gdst, const void *ssrc, un
 // k_lu_assemble (MR written); each pack is assembled in shared memory and
 // stored with one bulk copy.  Also the terms of the ghost neighbours on
 // the three lower faces of the domain.
-template <typename T>
+// ASM: also the assembly of the tile's cells (lu_mr, MR written), which the
+// wavefront then needs no separate pass for; the initial NL, NR of the
+// assembly kernel are not formed (the sweeps overwrite every interior cell)
+template <typename T, bool ASM>
 __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w, double dt)
 {
     extern __shared__ __align__(128) unsigned char pack_smem[];
@@ -253,7 +256,14 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
         }
         P[36 * WV_CELLS] = g.d11; P[37 * WV_CELLS] = g.d22; P[38 * WV_CELLS] = g.d51;
 #pragma unroll
-        for (int n = 0; n < 5; n++) P[(39 + n) * WV_CELLS] = rhs_get<T>(a.MR[n], q, a.f32_lu);
+        T MR[5];
+        if (ASM) lu_mr<T>(d, a, i, j, k, q, dt, s, MR);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+            if (ASM) rhs_put<T>(a.MR[n], q, MR[n], a.f32_lu);
+            else MR[n] = rhs_get<T>(a.MR[n], q, a.f32_lu);
+            P[(39 + n) * WV_CELLS] = MR[n];
+        }
     }
     const unsigned bytes = (unsigned)(WV_CELLS * WV_PACK * sizeof(T));
     __syncthreads();
