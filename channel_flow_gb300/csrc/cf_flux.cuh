@@ -544,8 +544,10 @@ namespace CF_NS {
 // A is cf_flux_args (FP64 cell arrays) or, in the FP32 build,
 // cf_flux_args_f (FP32 copies of U, J and 1/J made once per call, so the
 // stencil reads convert nothing; the face arrays stay FP64).
+// FP32: at least four blocks per SM (64 registers; a few bytes of spill,
+// measured 15 % faster than three blocks without)
 template <int DIR, bool LIMITED, typename T, typename A = cf_flux_args>
-__global__ void __launch_bounds__(256) k_flux(cf_dims d, A a, cf_box b)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_flux(cf_dims d, A a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     T mL[5], mR[5], m[9], F[6];
