@@ -41,3 +41,81 @@ def test_gpu_step_equals_oracle_loop(dims, port, cuda_lib):
                 assert np.array_equal(dev[key][n].cpu().numpy(), f[key][n], equal_nan=True), (key, n)
     finally:
         ctx.close()
+
+
+def _routine_loop(ctx, dev, deltaT, max_iterations, tolerance, E, limiter=True, filt=True):
+    """One physical step composed of the drop-in routine calls (FP64
+    arrays between them), in the context's precision: the loop of cf_step
+    written out.  E (running maxima) is updated in place."""
+    import torch
+    U_, J = dev["U_"], dev["J"]
+    Nijk, ijk = ctx.Hyperplane()
+    names = ("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter") if limiter else ("Flux_X", "Flux_Y", "Flux_Z")
+    visc = [None] * 79
+    visc[0:5] = U_
+    visc[5:9] = dev["vF"]
+    visc[9] = J
+    visc[10:19] = dev["cell_metric"]
+    for s in range(3):
+        visc[19 + 10 * s] = dev["face_J"][s]
+        visc[20 + 10 * s:29 + 10 * s] = dev["face_metric"][s]
+    visc[55:59] = dev["LL"]
+    visc[65:69] = dev["ML"]
+    visc[75:79] = dev["NL"][1:5]
+    dts = U_ + dev["U"] + dev["Uq"] + [J] + dev["cell_metric"] + dev["inF"][0] + dev["inF"][1] + dev["inF"][2] + \
+        dev["vF"] + dev["MR"] + dev["NR"] + dev["NL"] + dev["Residual"]
+    it = 0
+    while True:
+        it += 1
+        ctx.X_periodic(*U_)
+        ctx.Y_boundary_condition(*U_, J)
+        ctx.Z_boundary_condition(*U_, J)
+        if filt:
+            ctx.Filter(0.007, 1.0, 0.0, *U_, dev["Y_point"], *dev["Ep"], J)
+        for d in range(3):
+            ctx.flux(names[d], U_ + [None] * 10 + [J, dev["face_J"][d]] + dev["face_metric"][d] + dev["inF"][d] +
+                     [dev["Ep"][d]])
+        ctx.Viscous_terms(*visc)
+        er = ctx.Dual_time_stepping(deltaT, *dts, Nijk=Nijk, ijk=ijk)
+        for n in range(5):
+            E[n] = max(E[n], er[n])
+        ern = [er[n] / E[n] for n in range(5)]
+        if all(ern[n] < tolerance for n in range(4)) or it >= max_iterations:
+            break
+    q, _ = ctx.Driven_force(dev["U"][1], J)
+    g = ctx.grid
+    box = (slice(3, g.gend + 1), slice(2, g.ny + 1), slice(2, g.nz + 1))
+    for n in range(5):
+        dev["Uq"][n][box] = dev["U"][n][box]
+        dev["U"][n][box] = U_[n][box]
+    torch.cuda.synchronize()
+    return it, np.array(ern), q
+
+
+@pytest.mark.parametrize("static_metrics", [False, True])
+def test_gpu_fp32_step_equals_routine_loop(static_metrics, cuda_lib):
+    """In FP32 the step driver passes its intermediate arrays as FP32 values
+    and (static_metrics) reads FP32 copies of the fixed metrics; the drop-in
+    routines exchange FP64 arrays.  Every FP32 value is exact in FP64, so
+    the two give the same state bit for bit."""
+    import channel_flow_gb300 as cf
+    g = cases.grid((13, 9, 17))
+    f = cases.step_case(g, seed=5)
+    a, b = _to_dev(f), _to_dev(f)
+    ctx_a = cf.Context(g, precision="fp32")
+    ctx_b = cf.Context(g, precision="fp32")
+    try:
+        E = [0.0] * 5
+        for step in (1, 2):
+            it_a, er_a, q_a = ctx_a.step(a, step=step, max_iterations=3, tolerance=1e-3,
+                                         static_metrics=static_metrics)
+            it_b, er_b, q_b = _routine_loop(ctx_b, b, 0.00000005, 3, 1e-3, E)
+            assert it_a == it_b
+            np.testing.assert_allclose(er_a, er_b, rtol=1e-12, atol=0)
+            assert abs(q_a - q_b) <= 1e-12 * abs(q_b)
+        for key in ("U_", "U", "Uq"):
+            for n in range(5):
+                assert np.array_equal(a[key][n].cpu().numpy(), b[key][n].cpu().numpy(), equal_nan=True), (key, n)
+    finally:
+        ctx_a.close()
+        ctx_b.close()
