@@ -135,11 +135,11 @@ def rhs_calls(ctx, w, ptr):
 
 # kernels launched per RHS step: x halo 1, y wall 1, z periodic 1, Filter
 # (1 coefficients + 2 x 6 fused levels + 2 energy + 3 ghost fills + 3
-# thresholds = 21), fluxes (FP64: x, y, z weights, z = 4; FP32: an FP32
-# copy of U and J before each of the three = 6), viscous (primitives,
-# three face sets, divergence = 5)
-LAUNCHES_PER_STEP = {"fp64": 1 + 1 + 1 + 21 + 4 + 5, "fp64_exact": 1 + 1 + 1 + 21 + 4 + 5,
-                     "fp32": 1 + 1 + 1 + 21 + 6 + 5}
+# thresholds = 21), fluxes (FP64: x, y, z weights, z interior, z edges = 5;
+# FP32: an FP32 copy of U and J before each of the three, z in two parts =
+# 7), viscous (primitives, three face sets, divergence = 5)
+LAUNCHES_PER_STEP = {"fp64": 1 + 1 + 1 + 21 + 5 + 5, "fp64_exact": 1 + 1 + 1 + 21 + 5 + 5,
+                     "fp32": 1 + 1 + 1 + 21 + 7 + 5}
 
 
 def run_calls(ctx, calls):

@@ -546,10 +546,31 @@ namespace CF_NS {
 // stencil reads convert nothing; the face arrays stay FP64).
 // FP32: at least four blocks per SM (64 registers; a few bytes of spill,
 // measured 15 % faster than three blocks without)
-template <int DIR, bool LIMITED, typename T, typename A = cf_flux_args>
+//
+// ZP (z faces only): 0 every face of the box; 1 the interior faces k =
+// 3..nz-2 of the box (their warps never take the edge branches); 2 the four
+// edge faces k = 1, 2, nz-1, nz of every (i, j) of the box, four lanes per
+// row.  A warp of the z box spans 32 consecutive k, so with ZP 0 the warps
+// holding a row's edges execute the edge and the interior code one after
+// the other.
+template <int DIR, bool LIMITED, typename T, typename A = cf_flux_args, int ZP = 0>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_flux(cf_dims d, A a, cf_box b)
 {
-    CF_BOX_INDEX(b, i, j, k);
+    int i, j, k;
+    if (ZP == 2) {
+        const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        const int e = (int)(t & 3);
+        const long long r = t >> 2;
+        j = b.j0 + (int)(r % b.nj);
+        i = b.i0 + (int)(r / b.nj);
+        if (i >= b.i0 + b.ni) return;
+        k = e < 2 ? 1 + e : d.nz - 3 + e;
+    } else {
+        k = b.k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+        j = b.j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+        i = b.i0 + (int)blockIdx.z;
+        if (k >= b.k0 + b.nk || j >= b.j0 + b.nj) return;
+    }
     T mL[5], mR[5], m[9], F[6];
 #ifdef CF_FAST_MATH
     if (DIR == 0) {
@@ -559,8 +580,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_flux(cf_dims d,
         if (LIMITED) fast_states_y_limited<T>(d, a, i, j, k, mL, mR);
         else fast_states_y_linear<T>(d, a, i, j, k, mL, mR);
     } else {
-        if (LIMITED) fast_states_z_limited<T>(d, a, i, j, k, mL, mR);
-        else fast_states_z_linear<T>(d, a, i, j, k, mL, mR);
+        if (LIMITED) fast_states_z_limited<T, A, ZP == 1>(d, a, i, j, k, mL, mR);
+        else fast_states_z_linear<T, A, ZP == 1>(d, a, i, j, k, mL, mR);
     }
     const size_t q = d.ix(i, j, k);
 #pragma unroll
@@ -630,6 +651,24 @@ __global__ void __launch_bounds__(256) k_flux_zweights(cf_dims d, const double *
 #endif
 }
 
+// the z faces of box b: interior faces k = 3..nz-2 in one launch, the four
+// edge faces of every row in another (small grids: one launch of all)
+template <bool LIM, typename T, typename A>
+cudaError_t launch_flux_z(const cf_dims &d, const A &a, const cf_box &b, cudaStream_t s)
+{
+    if (d.nz < 6 || b.k0 != 1 || b.nk != d.nz) {
+        k_flux<2, LIM, T, A><<<box_grid(b), box_block(), 0, s>>>(d, a, b);
+        return cudaGetLastError();
+    }
+    cf_box bi = b;
+    bi.k0 = 3;
+    bi.nk = d.nz - 4;
+    k_flux<2, LIM, T, A, 1><<<box_grid(bi), box_block(), 0, s>>>(d, a, bi);
+    const long long n = 4LL * b.ni * b.nj;
+    k_flux<2, LIM, T, A, 2><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, b);
+    return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_flux(const cf_dims &d, const cf_flux_args &a, int dir, bool limited, cudaStream_t s)
 {
@@ -645,14 +684,13 @@ cudaError_t launch_flux(const cf_dims &d, const cf_flux_args &a, int dir, bool l
 #endif
         if (bw.nk > 0) k_flux_zweights<<<box_grid(bw), t, 0, s>>>(d, a.J, a.wz[0], a.wz[1], bw);
     }
+    if (dir == 2) return limited ? launch_flux_z<true, T>(d, a, b, s) : launch_flux_z<false, T>(d, a, b, s);
     if (limited) {
         if (dir == 0) k_flux<0, true, T><<<g, t, 0, s>>>(d, a, b);
-        else if (dir == 1) k_flux<1, true, T><<<g, t, 0, s>>>(d, a, b);
-        else k_flux<2, true, T><<<g, t, 0, s>>>(d, a, b);
+        else k_flux<1, true, T><<<g, t, 0, s>>>(d, a, b);
     } else {
         if (dir == 0) k_flux<0, false, T><<<g, t, 0, s>>>(d, a, b);
-        else if (dir == 1) k_flux<1, false, T><<<g, t, 0, s>>>(d, a, b);
-        else k_flux<2, false, T><<<g, t, 0, s>>>(d, a, b);
+        else k_flux<1, false, T><<<g, t, 0, s>>>(d, a, b);
     }
     return cudaGetLastError();
 }
@@ -707,14 +745,14 @@ inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, floa
     cf_box b = flux_box(d, dir);
     if (b.ni == 0 || b.nj == 0 || b.nk == 0) return cudaGetLastError();
     dim3 g = box_grid(b), t = box_block();
+    if (dir == 2)
+        return limited ? launch_flux_z<true, float>(d, fa, b, s) : launch_flux_z<false, float>(d, fa, b, s);
     if (limited) {
         if (dir == 0) k_flux<0, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-        else if (dir == 1) k_flux<1, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-        else k_flux<2, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+        else k_flux<1, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
     } else {
         if (dir == 0) k_flux<0, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-        else if (dir == 1) k_flux<1, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-        else k_flux<2, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+        else k_flux<1, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
     }
     return cudaGetLastError();
 }

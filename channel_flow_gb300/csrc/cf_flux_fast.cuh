@@ -196,14 +196,16 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A 
     }
 }
 
-template <typename T, typename A>
+// INTERIOR: the caller launches faces k = 3..nz-2 only, where both states
+// are limited (the edge branches are then not compiled in)
+template <typename T, typename A, bool INTERIOR = false>
 __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A &a, int i, int j,
                                                       int k, T *mL, T *mR)
 {
     const int nz = d.nz, ny = d.ny;
     const size_t qL = d.ix(i + 1, j + 1, k), qR = qL + 1;
-    const bool limL = k >= 3 && k <= nz - 1;          // cell k takes a limited state
-    const bool limR = k + 1 >= 3 && k + 1 <= nz - 1;  // cell k+1 takes a limited state
+    const bool limL = INTERIOR || (k >= 3 && k <= nz - 1);          // cell k takes a limited state
+    const bool limR = INTERIOR || (k + 1 >= 3 && k + 1 <= nz - 1);  // cell k+1 takes a limited state
     const bool lo3 = k >= ny, hi3 = k + 1 >= ny;      // the reference compares with the y extent
     const auto *iJp = a.wz[0];      // 1/J per cell
     if (limL && limR) {
@@ -305,11 +307,11 @@ __device__ __forceinline__ void fast_states_y_linear(const cf_dims &d, const A &
     fast_lin_pair<T>(a, d.ix(i + 1, j, k + 1), d.Zm, mL, mR);
 }
 
-template <typename T, typename A>
+template <typename T, typename A, bool INTERIOR = false>
 __device__ __forceinline__ void fast_states_z_linear(const cf_dims &d, const A &a, int i, int j,
                                                      int k, T *mL, T *mR)
 {
-    if (k <= 2 || k >= d.nz - 1) {
+    if (!INTERIOR && (k <= 2 || k >= d.nz - 1)) {
         states_z_linear<T>(d, a, i, j, k, mL, mR);
         return;
     }
