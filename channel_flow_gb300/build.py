@@ -6,7 +6,9 @@ Translation units, compiled in parallel with nvcc:
   kernels without fused multiply-add, whose results equal the reference's
   bit for bit;
 * ``cf_variant.cu`` as namespace ``cf_fast`` with contraction on, the
-  reduced-division face fluxes (CF_FAST_MATH) and the FP32 instantiations;
+  reduced-division face fluxes (CF_FAST_MATH) and the FP32 instantiations,
+  whose divisions and square roots take the approximate hardware forms
+  (``-prec-div=false -prec-sqrt=false``; these flags leave FP64 alone);
 * ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h);
 * ``cf_noalloc.cu``: the allocation-free DPLUSGS entry point (its scratch is
   a file-scope device array);
@@ -62,7 +64,8 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         base += ["-Xptxas", "-v"]
     units = [
         ("cf_variant.cu", "cf_exact.o", ["-DCF_NS=cf_exact", "--fmad=false"]),
-        ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "-DCF_FAST_MATH", "--fmad=true"]),
+        ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "-DCF_FAST_MATH", "--fmad=true",
+                                         "-prec-div=false", "-prec-sqrt=false"]),
         ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
         ("cf_noalloc.cu", "cf_noalloc.o", ["-DCF_NS=cf_noalloc", "--fmad=false"]),
         ("cf_mlp.cu", "cf_mlp.o", []),

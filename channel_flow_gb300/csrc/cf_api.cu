@@ -646,8 +646,8 @@ static int lu_read_norms(cf_ctx *c, double *er[5], const char *who)
 
 static int lu_finish_host(cf_ctx *c, const cf_lu_args &a, double *er[5], const char *who)
 {
-    cudaError_t e = exact(c) ? cf_exact::lu_finish(c->d, a, c->er_dev, c->stream)
-                             : cf_fast::lu_finish(c->d, a, c->er_dev, c->stream);
+    cudaError_t e = exact(c) ? cf_exact::lu_finish(c->d, a, c->er_dev, 0, c->stream)
+                             : cf_fast::lu_finish(c->d, a, c->er_dev, kprec(c), c->stream);
     if (int rc = cuda_check(c, e, who)) return rc;
     return lu_read_norms(c, er, who);
 }
@@ -758,10 +758,11 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, false, 0, s)
                                      : cf_fast::lu_wave_pack(d, a, w, dt, true, false, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
-        // FP32: the backward sweep also updates the state (FP64), copies
-        // NL <- NR and leaves per-tile norm partial sums; its blocks have
-        // FP64 issue slots to spare while they wait on their neighbours.
-        // The FP64 sweeps keep their FP64 pipe for the sweep itself.
+        // FP32: the backward sweep also updates the state (the FP32 change
+        // added to the FP64 state), copies NL <- NR and leaves per-tile norm
+        // partial sums; its blocks have issue slots to spare while they
+        // wait on their neighbours.  The FP64 sweeps keep their FP64 pipe
+        // for the sweep itself.
         const bool fuse = pr == 1;
         if (!fuse) wb.partial = nullptr;
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, wb, false, 0, s)
@@ -786,7 +787,7 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
         }
     }
     if (e == cudaSuccess) e = cf_fast::lu_copy(d, a, s);
-    if (e == cudaSuccess) e = ex ? cf_exact::lu_finish(d, a, c->er_dev, s) : cf_fast::lu_finish(d, a, c->er_dev, s);
+    if (e == cudaSuccess) e = ex ? cf_exact::lu_finish(d, a, c->er_dev, 0, s) : cf_fast::lu_finish(d, a, c->er_dev, pr, s);
     return e;
 }
 

@@ -117,7 +117,7 @@ extern "C" int cf_DPLUSGS_noalloc(const cf_grid *g, void *stream, double deltaT,
         CF_NS::k_lu_jacobi<double><<<grid, block, 0, st>>>(d, a, b, deltaT);
         CF_NS::k_lu_copy<<<grid, block, 0, st>>>(d, a, b);
     }
-    CF_NS::k_lu_update<<<grid, block, 0, st>>>(d, a, b);
+    CF_NS::k_lu_update<double><<<grid, block, 0, st>>>(d, a, b);
     const double DN = 1. / (d.X_out * d.Y_out * d.Z_out);
     CF_NS::k_lu_norm<<<1, 256, 0, st>>>(s.partial, nblk, DN, s.er);
     if (cudaGetLastError() != cudaSuccess) return CF_ERR_CUDA;

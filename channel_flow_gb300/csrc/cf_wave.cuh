@@ -543,8 +543,9 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
             }
         }
         if (!FWD && w.partial) {
-            // The tile's cells are final: the FP64 state update, NL <- NR
-            // and the tile's norm partial sums here, after the done flag,
+            // The tile's cells are final: the state update (FP32 change,
+            // FP64 state; lu_update_cell_f32), NL <- NR and the tile's norm
+            // partial sums here, after the done flag,
             // where they overlap the sweep's dependency waits instead of
             // taking a pass of their own (no tile of this sweep reads U_)
             double r2[5] = {0, 0, 0, 0, 0};
@@ -552,15 +553,13 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
                 const int li = c >> 6, lj = (c >> 3) & 7, lk = c & 7;
                 if (li < ti && lj < tj && lk < tk) {
                     const size_t q = d.ix(i0 + li, j0 + lj, k0 + lk);
-                    double nr[5], rr[5];
+                    float nr[5];
 #pragma unroll
                     for (int n = 0; n < 5; n++) {
-                        nr[n] = double(sN[n * WV_CELLS + c]);
+                        nr[n] = float(sN[n * WV_CELLS + c]);
                         rhs_put<T>(a.NL[n], q, sN[n * WV_CELLS + c], a.f32_lu);
                     }
-                    lu_update_cell(d, a, q, nr, rr);
-#pragma unroll
-                    for (int n = 0; n < 5; n++) r2[n] += rr[n];
+                    lu_update_cell_f32(d, a, q, nr, r2);
                 }
             }
             // fixed-order tree over the block in the incoming-term buffer,
