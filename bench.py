@@ -44,11 +44,13 @@ FILTER_ARGS = (0.007, 1.0, 0.0)        # Roe_criterion, E_high, E_low (main.cpp:
 ALG_BYTES = {"Filter": 80, "Flux_X_limiter": 168, "Flux_Y_limiter": 176, "Flux_Z_limiter": 176,
              "Viscous_terms": 320, "Dual_time_stepping": 2680}
 # single-kernel routines eligible as "the dominant kernel" of the roofline
-ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>",
-                "Flux_Z_limiter": "k_flux<2,true,double>"}
+# (Flux_Z_limiter is three launches: z weights, interior faces, edge faces)
+ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>"}
 # DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
-# launch on the 96^3 case divided by its cells; profiles/k_flux_z_limiter_96.md)
-NCU_TRAFFIC_PER_CELL = {"Flux_Z_limiter": (82.365440e6 + 13.323008e6) / (96 * 96 * 96)}
+# launch on the 96^3 case divided by its cells) and FP64-pipe activity
+# (profiles/k_flux_y_limiter_96.md)
+NCU_TRAFFIC_PER_CELL = {"Flux_Y_limiter": (76.383744e6 + 12.138496e6) / (96 * 96 * 96)}
+NCU_FP64_PIPE_PCT = {"Flux_Y_limiter": 84.3}
 LU_SUBITERATIONS = 10   # LU-SGS sub-iterations of one physical step of the fixed-count schedule
 L2_BYTES = 129 * 2 ** 20
 
@@ -385,10 +387,10 @@ def main():
             "alg_bytes_per_cell": ALG_BYTES[dom], "launch_ms": per_routine[dom],
             "traffic": traffic * g.cells if traffic else None,
             "traffic_source": "ncu dram bytes of one launch at 96^3 scaled by cells" if traffic else None,
-            "fp64_pipe_active_pct": 88.1 if dom == "Flux_Z_limiter" else None,
+            "fp64_pipe_active_pct": NCU_FP64_PIPE_PCT.get(dom),
             "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
-            "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 88% pipe busy, "
-                    "DRAM 0.5%); the HBM fraction is the byte-model figure"}
+            "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 84% pipe busy, "
+                    "DRAM 1%); the HBM fraction is the byte-model figure"}
 
     # secondary measurements on the same workload: FP32 kernels, and one
     # dual-time pseudo-iteration (RHS + hyperplane LU-SGS) per precision

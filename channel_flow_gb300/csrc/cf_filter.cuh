@@ -18,8 +18,12 @@
 // EXACT (no-FMA build) keeps the reference's expression trees, with the
 // metric ratios b/a and c/a of the y pass formed once per call; otherwise
 // the y pass uses per-cell weights A = (b/a) J(j-1)/J(j), C = (c/a)
-// J(j+1)/J(j) and no division.  ST is the storage type of the level and
-// accumulator fields (float in the FP32 build).
+// J(j+1)/J(j) and no division, and the passes carry their normalisations
+// forward (x: NX = 4 or 8 times the filtered value, y: 1/c0 more, z: NX
+// more) to one exact scaling by c0/NX^2 at the end: two FP64 (or FP32)
+// operations per value and pass instead of three or four.  ST is the
+// storage type of the level and accumulator fields (float in the FP32
+// build).
 #pragma once
 #include <algorithm>
 
@@ -125,9 +129,15 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
             for (int v = 0; v < 4; v++) {
                 sp[v][o] = filt_load<T, SRC>(d, f.U[v], f.src[v], i + 1, pj[o], pk[o]);
                 T g = s0[v][o];
-                if (in)
-                    g = WIDE ? T(0.25) * (sm[v][o] + T(2) * s0[v][o] + sp[v][o])
-                             : T(0.125) * (sm[v][o] + T(6) * s0[v][o] + sp[v][o]);
+                if (EXACT) {
+                    if (in)
+                        g = WIDE ? T(0.25) * (sm[v][o] + T(2) * s0[v][o] + sp[v][o])
+                                 : T(0.125) * (sm[v][o] + T(6) * s0[v][o] + sp[v][o]);
+                } else {
+                    // NX times the filtered value (cells outside the box:
+                    // NX times the cell's value), one add and one FMA
+                    g = (in ? T(WIDE ? 2 : 6) : T(WIDE ? 4 : 8)) * s0[v][o] + (in ? sm[v][o] + sp[v][o] : T(0));
+                }
                 sgx[v][r][c] = g;
             }
         }
@@ -141,7 +151,8 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
                 if (c >= FT_HK || kk > d.nz + 1) continue;
                 if (kk < 2 || kk > d.nz) {
 #pragma unroll
-                    for (int v = 0; v < 4; v++) sgy[v][ty][c] = sgx[v][ty + 1][c];
+                    for (int v = 0; v < 4; v++)
+                        sgy[v][ty][c] = EXACT ? sgx[v][ty + 1][c] : T(WIDE ? 2.0 : 4.0 / 3.0) * sgx[v][ty + 1][c];
                     continue;
                 }
                 const size_t q = d.ix(i, jy, kk);
@@ -156,11 +167,13 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
                                              : T(0.125) * (T(2) * A * gm * Jm + T(6) * g0 * J0 + T(2) * C * gp * Jp) / J0;
                     }
                 } else {
-                    const T cw = WIDE ? T(0.5) : T(0.25), c0 = WIDE ? T(0.5) : T(0.75);
+                    // cw (A gm + C gp) + c0 g0 over c0: two FMAs per value
+                    // (cw/c0 = 1 wide, 1/3 narrow)
+                    const T As = WIDE ? A : A * T(1.0 / 3.0), Cs = WIDE ? C : C * T(1.0 / 3.0);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
                         const T gm = sgx[v][ty][c], g0 = sgx[v][ty + 1][c], gp = sgx[v][ty + 2][c];
-                        sgy[v][ty][c] = cw * (A * gm + C * gp) + c0 * g0;
+                        sgy[v][ty][c] = As * gm + (Cs * gp + g0);
                     }
                 }
             }
@@ -173,7 +186,11 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
 #pragma unroll
             for (int v = 0; v < 4; v++) {
                 const T gm = sgy[v][ty][tx], g0 = sgy[v][ty][tx + 1], gp = sgy[v][ty][tx + 2];
-                const T r = WIDE ? T(0.25) * (gm + T(2) * g0 + gp) : T(0.125) * (gm + T(6) * g0 + gp);
+                // the contracted build's passes carry the factors NX (x),
+                // NX / c0 (y) and NX (z); c0 / NX^2 is 1/32 (wide) or 3/256
+                // (narrow), both exact
+                const T r = EXACT ? (WIDE ? T(0.25) * (gm + T(2) * g0 + gp) : T(0.125) * (gm + T(6) * g0 + gp))
+                                  : T(WIDE ? 1.0 / 32.0 : 3.0 / 256.0) * (T(WIDE ? 2 : 6) * g0 + (gm + gp));
                 if (!last) f.dst[v][q] = ST(r);
                 T s;
                 switch (level) {
@@ -210,9 +227,17 @@ __global__ void k_filter_energy4(cf_dims d, cf_ptr5 U, filt_ptr4<ST> acc, double
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
     T u1 = T(U.p[0][q]), f1 = T(acc.p[0][q]);
+#ifdef CF_FAST_MATH
+    // two reciprocals instead of six divisions
+    const T iu = T(1) / u1, iff = T(1) / f1;
+    T Ue = T(U.p[1][q]) * iu - T(acc.p[1][q]) * iff;
+    T Ve = T(U.p[2][q]) * iu - T(acc.p[2][q]) * iff;
+    T We = T(U.p[3][q]) * iu - T(acc.p[3][q]) * iff;
+#else
     T Ue = T(U.p[1][q]) / u1 - T(acc.p[1][q]) / f1;
     T Ve = T(U.p[2][q]) / u1 - T(acc.p[2][q]) / f1;
     T We = T(U.p[3][q]) / u1 - T(acc.p[3][q]) / f1;
+#endif
     E[q] = double(Ue * Ue + Ve * Ve + We * We);
 }
 
