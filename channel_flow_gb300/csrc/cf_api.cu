@@ -618,6 +618,8 @@ static int lu_args(cf_ctx *c, double **p, const char *who, cf_lu_args &a)
     a.f32_rhs = 0;
     a.f32_lu = 0;
     for (int n = 0; n < 9; n++) a.m32[n] = nullptr;
+    for (int n = 0; n < 5; n++) a.U32[n] = a.dUq32[n] = nullptr;
+    a.J32 = nullptr;
     cf_dims &d = c->d;
     const size_t np = cf_fast::lu_partial_count(d);
     auto &e = c->scratch["lu_partial"];
@@ -822,8 +824,12 @@ static int capture_dts(cf_ctx *c, const cf_lu_args &a, double *pack, const cf_wa
 }
 
 // f32_rhs: in FP32 mode, Fx/Fy/Fz and vF hold FP32 values (the step driver)
+// step_copies (FP32 step driver): the FP32 copies of U_ and J that this
+// sub-iteration's fluxes made, and float(U - Uq) of the physical step, are
+// current; the LU-SGS kernels read them instead of converting
 static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double *er3, double *er4, double *er5,
-                      int *Nijk, int *ijk, double **p, bool f32_rhs, bool static_metrics = false)
+                      int *Nijk, int *ijk, double **p, bool f32_rhs, bool static_metrics = false,
+                      bool step_copies = false)
 {
     if (!c || !p) return CF_ERR_ARG;
     // the plane tables are a fixed function of the grid; the context holds
@@ -833,7 +839,7 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
             return fail(c, CF_ERR_ARG, "Dual_time_stepping: Nijk differs from the Hyperplane tables of this grid");
         c->tables_checked = true;
     }
-    cf_lu_args a;
+    cf_lu_args a{};
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
     a.f32_rhs = (f32_rhs && kprec(c) == 1) ? 1 : 0;
     // with the wavefront, MR, NL and NR pass between the step driver's own
@@ -844,6 +850,17 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
             a.m32[n] = met32_get(c, a.m[n]);
             if (!a.m32[n]) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: FP32 metric copy allocation failed");
         }
+    if (step_copies && kprec(c) == 1) {
+        const float *sh = reinterpret_cast<const float *>(scratch(c, "flux_f32", 4));
+        const float *dq = reinterpret_cast<const float *>(scratch(c, "step_duq", 3));
+        if (!sh || !dq) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: scratch allocation failed");
+        const size_t n = c->d.total();
+        for (int v = 0; v < 5; v++) {
+            a.U32[v] = sh + v * n;
+            a.dUq32[v] = dq + v * n;
+        }
+        a.J32 = sh + 5 * n;
+    }
     double *pack = nullptr;
     cf_wave_args w{};
     if (c->lu_schedule == CF_LU_WAVEFRONT) {
@@ -896,7 +913,7 @@ int cf_DPLUSGS(cf_ctx *c, int, double deltaT, double *er1, double *er2, double *
                double **p)
 {
     if (!c || !p) return CF_ERR_ARG;
-    cf_lu_args a;
+    cf_lu_args a{};
     if (int rc = lu_args(c, p, "DPLUSGS", a)) return rc;
     const cf_dims &d = c->d;
     const bool ex = exact(c);
@@ -1208,6 +1225,17 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
     // fixed metric arrays: their FP32 copies are made once and kept
     const bool static_m = f32_rhs && pp->static_metrics != 0;
     c->er_hist.clear();
+    if (f32_rhs) {
+        // U - Uq is fixed over the step: its FP32 value once, for the BDF2 term
+        float *dq = reinterpret_cast<float *>(scratch(c, "step_duq", 3));
+        if (!dq) return fail(c, CF_ERR_NOMEM, "cf_step: scratch allocation failed");
+        cf_ptr5 u, uq;
+        for (int n = 0; n < 5; n++) {
+            u.p[n] = R(c, f->U[n]);
+            uq.p[n] = R(c, f->Uq[n]);
+        }
+        if (int rc = cuda_check(c, cf_fast::diff_f32(c->d.total(), u, uq, dq, c->stream), "cf_step")) return rc;
+    }
     int it = 1;
     for (;; it++) {
         if (int rc = cf_X_periodic(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4])) return rc;
@@ -1234,7 +1262,7 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         }
         if (int rc = viscous_common(c, visc, f32_rhs, static_m)) return rc;
         if (int rc = dts_common(c, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr, nullptr, dts,
-                                f32_rhs, static_m)) return rc;
+                                f32_rhs, static_m, f32_rhs)) return rc;
         for (int n = 0; n < 5; n++) {
             c->E[n] = std::max(c->E[n], er[n]);
             er[n] = er[n] / c->E[n];

@@ -554,7 +554,7 @@ namespace CF_NS {
 // holding a row's edges execute the edge and the interior code one after
 // the other.
 template <int DIR, bool LIMITED, typename T, typename A = cf_flux_args, int ZP = 0>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_flux(cf_dims d, A a, cf_box b)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_flux(cf_dims d, A a, cf_box b)
 {
     int i, j, k;
     if (ZP == 2) {

@@ -18,6 +18,7 @@ constexpr int CF_LU_PACK = 52;   // doubles per cell of the sweep coefficient pa
     cudaError_t flux_f32(const cf_dims &d, const cf_flux_args &a, float *shadow, bool convert,           \
                          const float *const *met32, int dir, bool limited, cudaStream_t s);             \
     cudaError_t to_f32(size_t n, const double *src, float *dst, cudaStream_t s);                        \
+    cudaError_t diff_f32(size_t n, const cf_ptr5 &a, const cf_ptr5 &b, float *dst, cudaStream_t s);    \
     cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStream_t s);            \
     cudaError_t filter(const cf_dims &d, const cf_filter_args &a, double crit, double hi, double lo,   \
                        int prec, cudaStream_t s);                                                       \

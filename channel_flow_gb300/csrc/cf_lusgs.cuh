@@ -23,13 +23,20 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
 {
     lstate<T> s;
     const T K = CF_DC(T, d, K);
-    T u1 = T(a.U_[0][q]), Jq = T(a.J[q]);
+    // FP32 build: the step driver's FP32 copies of U_ and J when it has
+    // them (the same values as converting here, without the conversions)
+    const bool cp = sizeof(T) == 4 && a.U32[0];
+    T u[5], Jq;
+#pragma unroll
+    for (int n = 0; n < 5; n++) u[n] = cp ? T(a.U32[n][q]) : T(a.U_[n][q]);
+    Jq = cp ? T(a.J32[q]) : T(a.J[q]);
+    const T u1 = u[0];
     s.rho = u1 * Jq;
-    s.u = T(a.U_[1][q]) / u1;
-    s.v = T(a.U_[2][q]) / u1;
-    s.w = T(a.U_[3][q]) / u1;
+    s.u = u[1] / u1;
+    s.v = u[2] / u1;
+    s.w = u[3] / u1;
     s.VV = s.u * s.u + s.v * s.v + s.w * s.w;
-    s.P = (T(a.U_[4][q]) * Jq - T(0.5) * s.rho * s.VV) * (K - T(1));
+    s.P = (u[4] * Jq - T(0.5) * s.rho * s.VV) * (K - T(1));
     s.C = K * s.P / s.rho;
     s.Tt = s.P / s.rho;
     s.H = T(0.5) * s.VV + s.C / (K - T(1));
@@ -138,7 +145,7 @@ __global__ void k_lu_zero(cf_dims d, cf_lu_args a, size_t n)
 // state s (Dual_time_stepping.cpp:339-490)
 template <typename T>
 __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int i, int j, int k, size_t q,
-                                      double dt, const lstate<T> &s, T *MR)
+                                      T dt, const lstate<T> &s, T *MR)
 {
     const T K = CF_DC(T, d, K);
     T rho = s.rho, u = s.u, v = s.v, w = s.w, VV = s.VV, Tt = s.Tt, H = s.H, beta = s.beta;
@@ -161,16 +168,27 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
     const T dXI = CF_DC(T, d, dXI), dET = CF_DC(T, d, dET), dZT = CF_DC(T, d, dZT);
     T Rk[5];
 #ifdef CF_FAST_MATH
-    const double rdt2 = 0.5 / dt;     // one FP64 division per cell instead of five
+    const double rdt2 = sizeof(T) == 4 ? 0.0 : 0.5 / dt;   // one FP64 division per cell instead of five
 #endif
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        // the BDF2 time term combines three nearly equal FP64 states: it is
-        // formed in FP64 in every build (the same operations as the
-        // reference's expression when T is double) and only then rounded,
-        // so an FP32 build keeps the digits that the difference resolves
+        // the BDF2 time term combines three nearly equal FP64 states: their
+        // differences are formed in FP64 in every build (the reference's
+        // expression when T is double) before any rounding to FP32, so an
+        // FP32 build keeps the digits that the difference resolves
 #ifdef CF_FAST_MATH
-        T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) * rdt2);
+        T Rp;
+        if (sizeof(T) == 4) {
+            // FP32 build: 3 U_ - 4 U + Uq = 3 (U_ - U) - (U - Uq), the two
+            // differences formed in FP64 (nearly equal states: exact) and
+            // combined in FP32; U - Uq is fixed over a physical step, the
+            // step driver keeps it in FP32
+            const float d1 = float(a.U_[n][q] - a.U[n][q]);
+            const float d2 = a.dUq32[0] ? a.dUq32[n][q] : float(a.U[n][q] - a.Uq[n][q]);
+            Rp = T(-(3.0f * d1 - d2) * (0.5f / float(dt)));   // dt is FP32 here
+        } else {
+            Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) * rdt2);
+        }
 #else
         T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) / (2.0 * dt));
 #endif
@@ -180,7 +198,7 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
                  (rhs_get<T>(a.Fz[n], fz, f32) - rhs_get<T>(a.Fz[n], f0, f32)) / dZT);
         Rk[n] = Rp + Rf;
     }
-    const T f = CF_DC(T, d, f), Jq = T(a.J[q]);
+    const T f = CF_DC(T, d, f), Jq = (sizeof(T) == 4 && a.J32) ? T(a.J32[q]) : T(a.J[q]);
     Rk[1] = Rk[1] + rhs_get<T>(a.vF[0], q, a.f32_rhs) + f / Jq;
     Rk[2] = Rk[2] + rhs_get<T>(a.vF[1], q, a.f32_rhs);
     Rk[3] = Rk[3] + rhs_get<T>(a.vF[2], q, a.f32_rhs);
@@ -194,11 +212,11 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
 
 // BDF2 residual, Gamma^-1 R and the diagonal solve (Dual_time_stepping.cpp:339-506)
 template <typename T>
-__global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf_box b, double dt, int copy_nr)
+__global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf_box b, T dt, int copy_nr)
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
-    const T deltaT = T(dt);
+    const T deltaT = dt;
     lstate<T> s = lu_state<T>(d, a, q);
     T MR[5];
     lu_mr<T>(d, a, i, j, k, q, dt, s, MR);
@@ -577,13 +595,14 @@ __device__ __forceinline__ void lu_update_cell_f32(const cf_dims &d, const cf_lu
 {
     double u[5];
     float f[5];
+    const bool cp = a.U32[0] != nullptr;     // the step driver's FP32 copies of U_ and J
 #pragma unroll
     for (int n = 0; n < 5; n++) {
         u[n] = a.U_[n][q];
-        f[n] = float(u[n]);
+        f[n] = cp ? a.U32[n][q] : float(u[n]);
     }
     const float Km1 = d.f_K - 1.0f;
-    const float J = float(a.J[q]), iJ = 1.0f / J, iu0 = 1.0f / f[0];
+    const float J = cp ? a.J32[q] : float(a.J[q]), iJ = 1.0f / J, iu0 = 1.0f / f[0];
     const float rho = f[0] * J;
     const float uo = f[1] * iu0, vo = f[2] * iu0, wo = f[3] * iu0;
     const float VV = uo * uo + vo * vo + wo * wo;
@@ -647,15 +666,28 @@ __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_b
 }
 
 // final reduction of the block partial sums, one block, fixed order;
-// er[n] = sqrt(sum) * DN (Dual_time_stepping.cpp:1348-1352)
+// er[n] = sqrt(sum) * DN (Dual_time_stepping.cpp:1348-1352).  Each thread
+// sums a contiguous run of partials with eight loads in flight.
 __global__ void k_lu_norm(const double *partial, size_t nblk, double DN, double *er)
 {
     __shared__ double sh[5][256];
     const int tid = threadIdx.x;
     double s[5] = {0, 0, 0, 0, 0};
-    for (size_t b = tid; b < nblk; b += 256)
+    const size_t per = (nblk + 255) / 256, b0 = tid * per, b1 = b0 + per < nblk ? b0 + per : nblk;
+    const double *p = partial + 5 * b0;
+    size_t b = b0;
+    for (; b + 8 <= b1; b += 8, p += 40) {
+        double v[40];
 #pragma unroll
-        for (int n = 0; n < 5; n++) s[n] += partial[5 * b + n];
+        for (int m = 0; m < 40; m++) v[m] = p[m];
+#pragma unroll
+        for (int m = 0; m < 8; m++)
+#pragma unroll
+            for (int n = 0; n < 5; n++) s[n] += v[5 * m + n];
+    }
+    for (; b < b1; b++, p += 5)
+#pragma unroll
+        for (int n = 0; n < 5; n++) s[n] += p[n];
 #pragma unroll
     for (int n = 0; n < 5; n++) sh[n][tid] = s[n];
     __syncthreads();

@@ -91,7 +91,7 @@ extern "C" int cf_DPLUSGS_noalloc(const cf_grid *g, void *stream, double deltaT,
     scratch_ptrs s;
     if (int rc = scratch_for_current_device(s)) return rc;
 
-    cf_lu_args a;
+    cf_lu_args a{};   // FP32-only fields stay null
     for (int n = 0; n < 5; n++) {
         a.U_[n] = p[n];
         a.U[n] = p[5 + n];

@@ -129,6 +129,10 @@ struct cf_lu_args {
     int f32_rhs;             // FP32 build: Fx/Fy/Fz and vF hold FP32 values (the step driver's internal use)
     int f32_lu;              // FP32 build, wavefront: MR, NL, NR hold FP32 values (the step driver)
     const float *m32[9];     // FP32 copies of the cell metrics (or null)
+    // FP32 build, step driver only (null otherwise): FP32 copies of U_ and J
+    // made for this sub-iteration's fluxes, and float(U - Uq) of the step
+    const float *U32[5], *J32;
+    const float *dUq32[5];
 };
 
 // tiled wavefront of the hyperplane sweeps (cf_wave.cuh)

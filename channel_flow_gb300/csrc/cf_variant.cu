@@ -77,6 +77,22 @@ cudaError_t to_f32(size_t n, const double *src, float *dst, cudaStream_t s)
     return cudaGetLastError();
 }
 
+__global__ void k_diff_f32(size_t n, cf_ptr5 a, cf_ptr5 b, float *__restrict__ dst)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+#pragma unroll
+    for (int v = 0; v < 5; v++) dst[v * n + q] = float(a.p[v][q] - b.p[v][q]);
+}
+
+// dst[v * n + q] = float(a[v][q] - b[v][q]), five fields of n values
+cudaError_t diff_f32(size_t n, const cf_ptr5 &a, const cf_ptr5 &b, float *dst, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_diff_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, a, b, dst);
+    return cudaGetLastError();
+}
+
 cudaError_t viscous(const cf_dims &d, const cf_visc_args &a, int prec, cudaStream_t s)
 {
     return CF_DISPATCH(prec, launch_viscous<double>(d, a, s), launch_viscous<float>(d, a, s));
@@ -112,7 +128,7 @@ static cudaError_t lu_prepare_t(const cf_dims &d, const cf_lu_args &a, double dt
     const size_t n = d.total();
     k_lu_zero<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, a, n);
     cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
-    k_lu_assemble<T><<<box_grid(b), box_block(), 0, s>>>(d, a, b, dt, copy_nr ? 1 : 0);
+    k_lu_assemble<T><<<box_grid(b), box_block(), 0, s>>>(d, a, b, T(dt), copy_nr ? 1 : 0);
     return cudaGetLastError();
 }
 cudaError_t lu_prepare(const cf_dims &d, const cf_lu_args &a, double dt, bool copy_nr, int prec, cudaStream_t s)
@@ -177,10 +193,10 @@ static cudaError_t lu_wave_pack_t(const cf_dims &d, const cf_lu_args &a, const c
         return cudaGetLastError();
     }
     const size_t smem = (size_t)WV_CELLS * WV_PACK * sizeof(T);
-    void (*kf)(cf_lu_args, wave_args, double) = assemble ? k_lu_tile_pack<T, true> : k_lu_tile_pack<T, false>;
+    void (*kf)(cf_lu_args, wave_args, T) = assemble ? k_lu_tile_pack<T, true> : k_lu_tile_pack<T, false>;
     cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kf<<<w.ntiles, WV_CELLS, smem, s>>>(a, w, dt);
+    kf<<<w.ntiles, WV_CELLS, smem, s>>>(a, w, T(dt));
     return cudaGetLastError();
 }
 // assemble: the forward pack also assembles MR (no lu_prepare assembly pass)

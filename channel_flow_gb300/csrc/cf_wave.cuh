@@ -222,7 +222,7 @@ __device__ __forceinline__ void wave_bulk_store(void *gdst, const void *ssrc, un
 // wavefront then needs no separate pass for; the initial NL, NR of the
 // assembly kernel are not formed (the sweeps overwrite every interior cell)
 template <typename T, bool ASM>
-__global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w, double dt)
+__global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w, T dt)
 {
     extern __shared__ __align__(128) unsigned char pack_smem[];
     T *sp = reinterpret_cast<T *>(pack_smem);     // [WV_CELLS][WV_PACK]
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
         const lstate<T> s = lu_state<T>(d, a, q);
 #pragma unroll
         for (int dir = 0; dir < 3; dir++) A[dir] = wave_split<T>(d, a, q, s, dir);
-        g = lu_diag<T>(d, a, q, s, T(dt));
+        g = lu_diag<T>(d, a, q, s, dt);
         // forward pack
 #pragma unroll
         for (int dir = 0; dir < 3; dir++) {
