@@ -41,6 +41,7 @@ struct filt_fields {
     const void *src[4];     // level input: U (level 0) or the previous level (ST)
     ST *dst[4];             // level output (unused at the last level)
     ST *acc[4];             // deconvolution sum
+    ST *lev[2][4];          // both level fields: level 0 copies U into their ghost ring
     const ST *cA, *cC;      // y-pass coefficients (b/a, c/a when EXACT)
     const double *J;
 };
@@ -82,15 +83,32 @@ __global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__
     }
 }
 
-template <typename T, typename SRC>
-__device__ __forceinline__ T filt_load(const cf_dims &d, const double *U, const void *src, int i, int j, int k)
+// Every value a pass reads outside the box is the cell's U.  Level 0 reads
+// U itself and copies the values it reads outside the box into the ghost
+// ring of both level fields (as ST), so the later levels read their input
+// field alone, with no per-load choice between two arrays.  Offsets are
+// 32-bit (the launcher checks the array size).
+template <typename T, typename SRC, typename ST, bool L0>
+__device__ __forceinline__ void filt_load4(const filt_fields<ST> &f, bool ghost, unsigned q, T *x)
 {
-    const size_t q = d.ix(i, j, k);
-    return filt_inside(d, i, j, k) ? T(static_cast<const SRC *>(src)[q]) : T(U[q]);
+#pragma unroll
+    for (int v = 0; v < 4; v++) x[v] = T(static_cast<const SRC *>(f.src[v])[q]);
+    if (L0 && ghost) {
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            f.lev[0][v][q] = ST(x[v]);
+            f.lev[1][v][q] = ST(x[v]);
+        }
+    }
 }
 
-template <typename T, typename SRC, typename ST, bool WIDE, bool EXACT>
-__global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST> f, int level, int fti)
+// One filter level.  The block's input planes roll through registers: at
+// plane i the thread holds planes i-1, i, i+1 of its halo positions and
+// has plane i+2 in flight, and the y-pass coefficients and the
+// deconvolution sum of plane i are requested before the x pass, so the
+// passes wait on no global load.
+template <typename T, typename SRC, typename ST, bool WIDE, bool EXACT, bool L0>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf_dims d, filt_fields<ST> f, int level, int fti)
 {
     __shared__ T sgx[4][FT_HJ][FT_HK];     // x pass, rows j0-1..j0+8, columns k0-1..k0+32
     __shared__ T sgy[4][FT_J][FT_HK];      // y pass, rows j0..j0+7
@@ -98,66 +116,105 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
     const int k0 = 2 + (int)blockIdx.x * FT_K, j0 = 2 + (int)blockIdx.y * FT_J;
     const int i0 = 3 + (int)blockIdx.z * fti;
     const int i1 = min(i0 + fti - 1, d.gend);
-    // halo positions owned by this thread: tid and tid + 256
-    int pj[2], pk[2];
-    bool pv[2];
+    const bool level0 = L0;
+    const unsigned P = (unsigned)d.plane(), Zm = (unsigned)d.Zm;
+    // halo positions owned by this thread: tid and tid + 256; qh = offset
+    // in plane 0, hin = inside the box in (j, k)
+    bool pv[2], hin[2];
+    unsigned qh[2];
 #pragma unroll
     for (int o = 0; o < 2; o++) {
         const int p = tid + 256 * o;
-        pj[o] = j0 - 1 + p / FT_HK;
-        pk[o] = k0 - 1 + p % FT_HK;
-        pv[o] = p < FT_HALO && pj[o] <= d.ny + 1 && pk[o] <= d.nz + 1;
+        const int pj = j0 - 1 + p / FT_HK, pk = k0 - 1 + p % FT_HK;
+        pv[o] = p < FT_HALO && pj <= d.ny + 1 && pk <= d.nz + 1;
+        hin[o] = pj >= 2 && pj <= d.ny && pk >= 2 && pk <= d.nz;
+        qh[o] = (unsigned)pj * Zm + (unsigned)pk;
     }
-    T sm[4][2], s0[4][2], sp[4][2];
+    // level 0 copies the values outside the box (outside in (j, k), or on
+    // the planes 2 and gend+1) into the level fields' ghost ring
+    T sm[2][4], s0[2][4], sp[2][4], sn[2][4];
 #pragma unroll
-    for (int o = 0; o < 2; o++)
+    for (int o = 0; o < 2; o++) {
 #pragma unroll
-        for (int v = 0; v < 4; v++) {
-            sm[v][o] = pv[o] ? filt_load<T, SRC>(d, f.U[v], f.src[v], i0 - 1, pj[o], pk[o]) : T(0);
-            s0[v][o] = pv[o] ? filt_load<T, SRC>(d, f.U[v], f.src[v], i0, pj[o], pk[o]) : T(0);
+        for (int v = 0; v < 4; v++) sm[o][v] = s0[o][v] = sp[o][v] = sn[o][v] = T(0);
+        if (pv[o]) {
+            filt_load4<T, SRC, ST, L0>(f, level0 && (!hin[o] || i0 - 1 < 3), (unsigned)(i0 - 1) * P + qh[o], sm[o]);
+            filt_load4<T, SRC, ST, L0>(f, level0 && !hin[o], (unsigned)i0 * P + qh[o], s0[o]);
+            filt_load4<T, SRC, ST, L0>(f, level0 && (!hin[o] || i0 + 1 > d.gend), (unsigned)(i0 + 1) * P + qh[o], sp[o]);
         }
+    }
     const int jy = j0 + ty;                  // y-pass / output row of this thread
+    const int kz = k0 + tx;                  // z-pass / output column
     const bool last = level == 5;
+    const bool outp = jy <= d.ny && kz <= d.nz;
+    const bool rowp = jy <= d.ny;
+    const unsigned qy = (unsigned)jy * Zm + (unsigned)(k0 - 1 + tx);   // y-pass column tx (plane 0)
+    const unsigned qz = (unsigned)jy * Zm + (unsigned)kz;              // output cell (plane 0)
+    bool ycol[2];
+#pragma unroll
+    for (int o = 0; o < 2; o++) {
+        const int kk = k0 - 1 + tx + 32 * o;
+        ycol[o] = rowp && tx + 32 * o < FT_HK && kk >= 2 && kk <= d.nz;
+    }
     for (int i = i0; i <= i1; i++) {
-        // x pass (Filter.cpp:156-170, 835-849)
+        const unsigned qi = (unsigned)i * P;
+        // requests for this plane's y-pass coefficients and sum, and the
+        // input plane i+2
+        T cAv[2] = {T(0), T(0)}, cCv[2] = {T(0), T(0)}, ac[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int o = 0; o < 2; o++)
+            if (ycol[o]) {
+                cAv[o] = T(f.cA[qi + qy + 32 * o]);
+                cCv[o] = T(f.cC[qi + qy + 32 * o]);
+            }
+        if (outp && level > 0) {
+#pragma unroll
+            for (int v = 0; v < 4; v++) ac[v] = T(f.acc[v][qi + qz]);
+        }
+        if (i + 2 <= i1 + 1) {
+#pragma unroll
+            for (int o = 0; o < 2; o++)
+                if (pv[o])
+                    filt_load4<T, SRC, ST, L0>(f, level0 && (!hin[o] || i + 2 > d.gend), qi + 2 * P + qh[o], sn[o]);
+        }
+        // x pass (Filter.cpp:156-170, 835-849); plane i lies inside the box
 #pragma unroll
         for (int o = 0; o < 2; o++) {
             if (!pv[o]) continue;
-            const bool in = filt_inside(d, i, pj[o], pk[o]);
+            const bool in = hin[o];
             const int r = (tid + 256 * o) / FT_HK, c = (tid + 256 * o) % FT_HK;
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                sp[v][o] = filt_load<T, SRC>(d, f.U[v], f.src[v], i + 1, pj[o], pk[o]);
-                T g = s0[v][o];
+                T g = s0[o][v];
                 if (EXACT) {
                     if (in)
-                        g = WIDE ? T(0.25) * (sm[v][o] + T(2) * s0[v][o] + sp[v][o])
-                                 : T(0.125) * (sm[v][o] + T(6) * s0[v][o] + sp[v][o]);
+                        g = WIDE ? T(0.25) * (sm[o][v] + T(2) * s0[o][v] + sp[o][v])
+                                 : T(0.125) * (sm[o][v] + T(6) * s0[o][v] + sp[o][v]);
                 } else {
                     // NX times the filtered value (cells outside the box:
                     // NX times the cell's value), one add and one FMA
-                    g = (in ? T(WIDE ? 2 : 6) : T(WIDE ? 4 : 8)) * s0[v][o] + (in ? sm[v][o] + sp[v][o] : T(0));
+                    g = (in ? T(WIDE ? 2 : 6) : T(WIDE ? 4 : 8)) * s0[o][v] + (in ? sm[o][v] + sp[o][v] : T(0));
                 }
                 sgx[v][r][c] = g;
             }
         }
         __syncthreads();
         // stretched y pass (Filter.cpp:186-208, 863-883)
-        if (jy <= d.ny) {
+        if (rowp) {
 #pragma unroll
             for (int o = 0; o < 2; o++) {
                 const int c = tx + 32 * o;
                 const int kk = k0 - 1 + c;
                 if (c >= FT_HK || kk > d.nz + 1) continue;
-                if (kk < 2 || kk > d.nz) {
+                if (!ycol[o]) {
 #pragma unroll
                     for (int v = 0; v < 4; v++)
                         sgy[v][ty][c] = EXACT ? sgx[v][ty + 1][c] : T(WIDE ? 2.0 : 4.0 / 3.0) * sgx[v][ty + 1][c];
                     continue;
                 }
-                const size_t q = d.ix(i, jy, kk);
-                const T A = T(f.cA[q]), C = T(f.cC[q]);
+                const T A = cAv[o], C = cCv[o];
                 if (EXACT) {
+                    const size_t q = d.ix(i, jy, kk);
                     const size_t s = d.Zm;
                     const T Jm = T(f.J[q - s]), J0 = T(f.J[q]), Jp = T(f.J[q + s]);
 #pragma unroll
@@ -180,9 +237,8 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
         }
         __syncthreads();
         // z pass (Filter.cpp:224-239, 896-910) and the deconvolution sum
-        const int kz = k0 + tx;
-        if (jy <= d.ny && kz <= d.nz) {
-            const size_t q = d.ix(i, jy, kz);
+        if (outp) {
+            const unsigned q = qi + qz;
 #pragma unroll
             for (int v = 0; v < 4; v++) {
                 const T gm = sgy[v][ty][tx], g0 = sgy[v][ty][tx + 1], gp = sgy[v][ty][tx + 2];
@@ -195,11 +251,11 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
                 T s;
                 switch (level) {
                 case 0: s = T(6) * r; break;
-                case 1: s = T(f.acc[v][q]) - T(15) * r; break;
-                case 2: s = T(f.acc[v][q]) + T(20) * r; break;
-                case 3: s = T(f.acc[v][q]) - T(15) * r; break;
-                case 4: s = T(f.acc[v][q]) + T(6) * r; break;
-                default: s = T(f.acc[v][q]) - r; break;
+                case 1: s = ac[v] - T(15) * r; break;
+                case 2: s = ac[v] + T(20) * r; break;
+                case 3: s = ac[v] - T(15) * r; break;
+                case 4: s = ac[v] + T(6) * r; break;
+                default: s = ac[v] - r; break;
                 }
                 f.acc[v][q] = ST(s);
             }
@@ -208,8 +264,9 @@ __global__ void __launch_bounds__(256) k_filter_level(cf_dims d, filt_fields<ST>
         for (int o = 0; o < 2; o++)
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                sm[v][o] = s0[v][o];
-                s0[v][o] = sp[v][o];
+                sm[o][v] = s0[o][v];
+                s0[o][v] = sp[o][v];
+                sp[o][v] = sn[o][v];
             }
         // sgx is rewritten next plane only after every thread passed the
         // second barrier (y pass done); sgy after the next first barrier
@@ -285,9 +342,11 @@ __global__ void k_filter_ep(cf_dims d, const double *__restrict__ Eh, const doub
 }
 
 template <typename T, typename SRC, typename ST, bool EXACT>
-static void filter_level_launch(const cf_dims &d, const filt_fields<ST> &f, bool wide, int level, cudaStream_t s)
+static cudaError_t filter_level_launch(const cf_dims &d, const filt_fields<ST> &f, bool wide, int level,
+                                       cudaStream_t s)
 {
-    // planes per block: enough blocks for about four per SM
+    // planes per block: one wave of the resident blocks (4 per SM in FP32,
+    // 2 in FP64), x cut into as many chunks as fill it
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -296,12 +355,27 @@ static void filter_level_launch(const cf_dims &d, const filt_fields<ST> &f, bool
         if (sms <= 0) sms = 132;
     }
     const int tk = (d.Z_out + FT_K - 1) / FT_K, tj = (d.Y_out + FT_J - 1) / FT_J;
-    const int chunks = std::max(1, std::min(d.X_out, (4 * sms + tk * tj - 1) / (tk * tj)));
+    if (d.total() >= (size_t(1) << 31)) return cudaErrorInvalidValue;   // 32-bit offsets
+    // chunks minimising (waves of resident blocks) x (planes per block +
+    // the two extra planes a block loads before its first)
+    const int slots = sms * (sizeof(T) == 4 ? 4 : 2);
+    int chunks = 1;
+    long best = -1;
+    for (int c = 1; c <= d.X_out; c++) {
+        const long waves = ((long)tk * tj * c + slots - 1) / slots, planes = (d.X_out + c - 1) / c;
+        if (best < 0 || waves * (planes + 2) < best) { best = waves * (planes + 2); chunks = c; }
+    }
     const int fti = (d.X_out + chunks - 1) / chunks;
     const dim3 g((unsigned)tk, (unsigned)tj, (unsigned)((d.X_out + fti - 1) / fti));
     const dim3 t(32, 8);
-    if (wide) k_filter_level<T, SRC, ST, true, EXACT><<<g, t, 0, s>>>(d, f, level, fti);
-    else k_filter_level<T, SRC, ST, false, EXACT><<<g, t, 0, s>>>(d, f, level, fti);
+    if (level == 0) {
+        if (wide) k_filter_level<T, SRC, ST, true, EXACT, true><<<g, t, 0, s>>>(d, f, level, fti);
+        else k_filter_level<T, SRC, ST, false, EXACT, true><<<g, t, 0, s>>>(d, f, level, fti);
+    } else {
+        if (wide) k_filter_level<T, SRC, ST, true, EXACT, false><<<g, t, 0, s>>>(d, f, level, fti);
+        else k_filter_level<T, SRC, ST, false, EXACT, false><<<g, t, 0, s>>>(d, f, level, fti);
+    }
+    return cudaSuccess;
 }
 
 // T: arithmetic type, ST: storage of the scratch levels, EXACT: reference
@@ -327,14 +401,17 @@ cudaError_t launch_filter(const cf_dims &d, const cf_filter_args &a, double crit
     filt_ptr4<ST> acc;
     for (int v = 0; v < 5; v++) U.p[v] = const_cast<double *>(a.U[v]);
     for (int v = 0; v < 4; v++) acc.p[v] = static_cast<ST *>(a.acc[v]);
+    for (int l = 0; l < 2; l++)
+        for (int v = 0; v < 4; v++) f.lev[l][v] = static_cast<ST *>(a.lev[l][v]);
     for (int wide = 0; wide < 2; wide++) {
         for (int lev = 0; lev < 6; lev++) {
             for (int v = 0; v < 4; v++) {
                 f.src[v] = lev == 0 ? static_cast<const void *>(a.U[v]) : a.lev[(lev - 1) & 1][v];
                 f.dst[v] = static_cast<ST *>(a.lev[lev & 1][v]);
             }
-            if (lev == 0) filter_level_launch<T, double, ST, EXACT>(d, f, wide != 0, lev, s);
-            else filter_level_launch<T, ST, ST, EXACT>(d, f, wide != 0, lev, s);
+            const cudaError_t e = lev == 0 ? filter_level_launch<T, double, ST, EXACT>(d, f, wide != 0, lev, s)
+                                           : filter_level_launch<T, ST, ST, EXACT>(d, f, wide != 0, lev, s);
+            if (e != cudaSuccess) return e;
         }
         k_filter_energy4<T, ST><<<g, t, 0, s>>>(d, U, acc, wide ? a.E2h : a.Eh, bi);
     }

@@ -322,6 +322,72 @@ constexpr int WV_SM_NL = 5 * WV_CELLS;              // [5][cells] forward N (bac
 constexpr int WV_SM_OUT = 5 * (WV_FX + WV_FY + WV_FZ);
 constexpr int WV_SM_TOTAL = WV_SM_PACK + WV_SM_IN + WV_SM_N + WV_SM_NL + WV_SM_OUT;
 
+// The local-plane steps of one tile for the warp with role W: W = 0, 1, 2
+// form the terms owed along x, y, z, W = 3 keeps N.  The role is a template
+// parameter, so every offset and bound is a constant; the four warps meet
+// at named barrier 1 once per step (every role takes the same L steps).
+template <typename T, bool FWD, int W>
+__device__ __forceinline__ void wave_steps(int L, bool full, int ti, int tj, int tk, const short (*s_cell)[32],
+                                           const T *spack, T *sin, T *sN, const T *snl, T *sout,
+                                           const lu_den<T> &dw, int lane)
+{
+    for (int s = 0; s < L; s++) {
+        const int l = FWD ? s : L - 1 - s;
+        const int c = s_cell[l][lane];
+        const int li = c >> 6, lj = (c >> 3) & 7, lk = c & 7;
+        if (c >= 0 && (full || (li < ti && lj < tj && lk < tk))) {
+            const T *P = spack + c;                    // value m at P[m * WV_CELLS]
+            T S[5], N[5];
+#pragma unroll
+            for (int n = 0; n < 5; n++)
+                S[n] = (sin[(0 * 5 + n) * WV_CELLS + c] + sin[(1 * 5 + n) * WV_CELLS + c]) +
+                       sin[(2 * 5 + n) * WV_CELLS + c];
+            const T d11 = P[36 * WV_CELLS], d22 = P[37 * WV_CELLS], d51 = P[38 * WV_CELLS];
+            if (FWD) {
+                const T r0 = P[39 * WV_CELLS] - S[0];
+                N[0] = d11 * r0;
+                N[1] = d22 * (P[40 * WV_CELLS] - S[1]);
+                N[2] = d22 * (P[41 * WV_CELLS] - S[2]);
+                N[3] = d22 * (P[42 * WV_CELLS] - S[3]);
+                N[4] = d51 * r0 + d22 * (P[43 * WV_CELLS] - S[4]);
+            } else {
+                N[0] = snl[0 * WV_CELLS + c] - d11 * S[0];
+                N[1] = snl[1 * WV_CELLS + c] - d22 * S[1];
+                N[2] = snl[2 * WV_CELLS + c] - d22 * S[2];
+                N[3] = snl[3 * WV_CELLS + c] - d22 * S[3];
+                N[4] = snl[4 * WV_CELLS + c] - (d51 * S[0] + d22 * S[4]);
+            }
+            if (W == 3) {
+#pragma unroll
+                for (int n = 0; n < 5; n++) sN[n * WV_CELLS + c] = N[n];
+            } else {
+                // the terms owed to the next cell along direction W
+                T o[5], cw[12];
+#pragma unroll
+                for (int m = 0; m < 12; m++) cw[m] = P[(12 * W + m) * WV_CELLS];
+                if (FWD) wave_lower_terms<T>(cw, N, dw, o);
+                else wave_upper_terms<T>(cw, N, dw, o);
+                constexpr int cstep = W == 0 ? WV_TJ * WV_TK : W == 1 ? WV_TK : 1;
+                const int lc = W == 0 ? li : W == 1 ? lj : lk;
+                const int tcw = W == 0 ? ti : W == 1 ? tj : tk;
+                if (FWD ? lc + 1 < tcw : lc >= 1) {
+                    const int cn = FWD ? c + cstep : c - cstep;
+#pragma unroll
+                    for (int n = 0; n < 5; n++) sin[(W * 5 + n) * WV_CELLS + cn] = o[n];
+                } else {
+                    // leaves the tile: shared face buffer of this direction
+                    constexpr int off = W == 0 ? 0 : W == 1 ? 5 * WV_FX : 5 * (WV_FX + WV_FY);
+                    constexpr int ns = W == 0 ? WV_FX : W == 1 ? WV_FY : WV_FZ;
+                    const int f = W == 0 ? lj * WV_TK + lk : W == 1 ? li * WV_TK + lk : li * WV_TJ + lj;
+#pragma unroll
+                    for (int n = 0; n < 5; n++) sout[off + n * ns + f] = o[n];
+                }
+            }
+        }
+        asm volatile("bar.sync 1, %0;" :: "n"(32 * WV_WARPS) : "memory");
+    }
+}
+
 // FWD: forward sweep (NL), else backward (NR).  Four warps per block: all
 // four form the cell's N from the incoming terms; warps 0, 1, 2 then form
 // the terms owed along x, y, z and warp 3 keeps N.  Terms for cells of the
@@ -456,60 +522,11 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
         if (tr && tid == 0) tr[2] = wave_clock();
         const int L = ti + tj + tk - 2;
         const bool full = ti == WV_TI && tj == WV_TJ && tk == WV_TK;
-        for (int s = 0; s < L; s++) {
-            const int l = FWD ? s : L - 1 - s;
-            const int c = s_cell[l][lane];
-            const int li = c >> 6, lj = (c >> 3) & 7, lk = c & 7;
-            if (c >= 0 && (full || (li < ti && lj < tj && lk < tk))) {
-                const T *P = spack + c;                    // value m at P[m * WV_CELLS]
-                T S[5], N[5];
-#pragma unroll
-                for (int n = 0; n < 5; n++)
-                    S[n] = (sin[(0 * 5 + n) * WV_CELLS + c] + sin[(1 * 5 + n) * WV_CELLS + c]) +
-                           sin[(2 * 5 + n) * WV_CELLS + c];
-                const T d11 = P[36 * WV_CELLS], d22 = P[37 * WV_CELLS], d51 = P[38 * WV_CELLS];
-                if (FWD) {
-                    const T r0 = P[39 * WV_CELLS] - S[0];
-                    N[0] = d11 * r0;
-                    N[1] = d22 * (P[40 * WV_CELLS] - S[1]);
-                    N[2] = d22 * (P[41 * WV_CELLS] - S[2]);
-                    N[3] = d22 * (P[42 * WV_CELLS] - S[3]);
-                    N[4] = d51 * r0 + d22 * (P[43 * WV_CELLS] - S[4]);
-                } else {
-                    N[0] = snl[0 * WV_CELLS + c] - d11 * S[0];
-                    N[1] = snl[1 * WV_CELLS + c] - d22 * S[1];
-                    N[2] = snl[2 * WV_CELLS + c] - d22 * S[2];
-                    N[3] = snl[3 * WV_CELLS + c] - d22 * S[3];
-                    N[4] = snl[4 * WV_CELLS + c] - (d51 * S[0] + d22 * S[4]);
-                }
-                if (warp == 3) {
-#pragma unroll
-                    for (int n = 0; n < 5; n++) sN[n * WV_CELLS + c] = N[n];
-                } else {
-                    // the terms owed to the next cell along direction `warp`
-                    T o[5], cw[12];
-#pragma unroll
-                    for (int m = 0; m < 12; m++) cw[m] = P[(12 * warp + m) * WV_CELLS];
-                    if (FWD) wave_lower_terms<T>(cw, N, dw, o);
-                    else wave_upper_terms<T>(cw, N, dw, o);
-                    const int lc = warp == 0 ? li : warp == 1 ? lj : lk;
-                    const int tcw = warp == 0 ? ti : warp == 1 ? tj : tk;
-                    const int cstep = warp == 0 ? WV_TJ * WV_TK : warp == 1 ? WV_TK : 1;
-                    if (FWD ? lc + 1 < tcw : lc >= 1) {
-                        const int cn = FWD ? c + cstep : c - cstep;
-#pragma unroll
-                        for (int n = 0; n < 5; n++) sin[(warp * 5 + n) * WV_CELLS + cn] = o[n];
-                    } else {
-                        // leaves the tile: shared face buffer of this direction
-                        T *so = sout + (warp == 0 ? 0 : warp == 1 ? 5 * WV_FX : 5 * (WV_FX + WV_FY));
-                        const int f = warp == 0 ? lj * WV_TK + lk : warp == 1 ? li * WV_TK + lk : li * WV_TJ + lj;
-                        const int ns = warp == 0 ? WV_FX : warp == 1 ? WV_FY : WV_FZ;
-#pragma unroll
-                        for (int n = 0; n < 5; n++) so[n * ns + f] = o[n];
-                    }
-                }
-            }
-            __syncthreads();
+        switch (warp) {
+        case 0: wave_steps<T, FWD, 0>(L, full, ti, tj, tk, s_cell, spack, sin, sN, snl, sout, dw, lane); break;
+        case 1: wave_steps<T, FWD, 1>(L, full, ti, tj, tk, s_cell, spack, sin, sN, snl, sout, dw, lane); break;
+        case 2: wave_steps<T, FWD, 2>(L, full, ti, tj, tk, s_cell, spack, sin, sN, snl, sout, dw, lane); break;
+        default: wave_steps<T, FWD, 3>(L, full, ti, tj, tk, s_cell, spack, sin, sN, snl, sout, dw, lane); break;
         }
         // terms for the next tiles into their entry-face slots, then the flag
         {
