@@ -9,6 +9,8 @@ Translation units, compiled in parallel with nvcc:
   reduced-division face fluxes (CF_FAST_MATH) and the FP32 instantiations,
   whose divisions and square roots take the approximate hardware forms
   (``-prec-div=false -prec-sqrt=false``; these flags leave FP64 alone);
+* ``cf_variant.cu`` as namespace ``cf_drv``: the ``cf_fast`` kernels with
+  the step driver's FP32 array layout fixed at compile time (CF_STEP_LAYOUT);
 * ``cf_api.cu``: the C-ABI layer (include/channel_flow_gb300.h);
 * ``cf_noalloc.cu``: the allocation-free DPLUSGS entry point (its scratch is
   a file-scope device array);
@@ -66,6 +68,8 @@ def build(verbose: bool = False, ptxas: bool = False, force: bool = False) -> Pa
         ("cf_variant.cu", "cf_exact.o", ["-DCF_NS=cf_exact", "--fmad=false"]),
         ("cf_variant.cu", "cf_fast.o", ["-DCF_NS=cf_fast", "-DCF_WITH_FLOAT", "-DCF_FAST_MATH", "--fmad=true",
                                          "-prec-div=false", "-prec-sqrt=false"]),
+        ("cf_variant.cu", "cf_drv.o", ["-DCF_NS=cf_drv", "-DCF_WITH_FLOAT", "-DCF_FAST_MATH", "-DCF_STEP_LAYOUT",
+                                         "--fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
         ("cf_api.cu", "cf_api.o", ["-DCF_NS=cf_api_unused"]),
         ("cf_noalloc.cu", "cf_noalloc.o", ["-DCF_NS=cf_noalloc", "--fmad=false"]),
         ("cf_mlp.cu", "cf_mlp.o", []),

@@ -450,8 +450,11 @@ static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double
             for (int n = 0; n < 10; n++)
                 if (!m32[n]) return fail(c, CF_ERR_NOMEM, "%s: FP32 metric copy allocation failed", who);
         }
-        return cuda_check(c, cf_fast::flux_f32(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow,
-                                               static_metrics ? m32 : nullptr, dir, limited, c->stream), who);
+        // the step driver's layout (FP32 outputs, FP32 metric copies): the
+        // variant compiled for it
+        auto fn = (a.f32_out && static_metrics) ? cf_drv::flux_f32 : cf_fast::flux_f32;
+        return cuda_check(c, fn(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow, static_metrics ? m32 : nullptr,
+                                dir, limited, c->stream), who);
     }
     cudaError_t e = exact(c) ? cf_exact::flux(c->d, a, dir, limited, 0, c->stream)
                              : cf_fast::flux(c->d, a, dir, limited, 0, c->stream);
@@ -517,7 +520,8 @@ static int viscous_common(cf_ctx *c, double **p, bool f32_io, bool static_metric
             if (m32 && !a.mf32[f][n]) return fail(c, CF_ERR_NOMEM, "Viscous_terms: FP32 metric copy allocation failed");
     }
     cudaError_t e = exact(c) ? cf_exact::viscous(c->d, a, 0, c->stream)
-                             : cf_fast::viscous(c->d, a, kprec(c), c->stream);
+                    : (a.f32_io && m32) ? cf_drv::viscous(c->d, a, kprec(c), c->stream)
+                                        : cf_fast::viscous(c->d, a, kprec(c), c->stream);
     return cuda_check(c, e, "Viscous_terms");
 }
 
@@ -746,19 +750,25 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
         // over the cells less); FP32: its own box kernel, which measured
         // faster than the heavier FP32 pack kernel doing both
         const bool asm_in_pack = pr != 1;
+        // the step driver's FP32 layout (every FP32 copy set up): the kernels
+        // compiled for it
+        const bool st = pr == 1 && a.f32_rhs && a.f32_lu && a.m32[0] && a.U32[0] && a.J32 && a.dUq32[0];
+        auto prepare = st ? cf_drv::lu_prepare : cf_fast::lu_prepare;
+        auto wpack = st ? cf_drv::lu_wave_pack : cf_fast::lu_wave_pack;
+        auto wsweep = st ? cf_drv::lu_wave_sweep : cf_fast::lu_wave_sweep;
         e = asm_in_pack ? (ex ? cf_exact::lu_zero(d, a, s) : cf_fast::lu_zero(d, a, s))
-                        : cf_fast::lu_prepare(d, a, dt, true, pr, s);
+                        : prepare(d, a, dt, true, pr, s);
         const size_t fl = ((size_t)w.ntiles + 1) * sizeof(int);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.err, 0, sizeof(int), s);
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, false, true, 0, s)
-                                     : cf_fast::lu_wave_pack(d, a, w, dt, false, asm_in_pack, pr, s);
+                                     : wpack(d, a, w, dt, false, asm_in_pack, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, w, true, 0, s)
-                                     : cf_fast::lu_wave_sweep(a, w, true, pr, s);
+                                     : wsweep(a, w, true, pr, s);
         cf_wave_args wb = w;
         if (w.trace) wb.trace = w.trace + 4 * (size_t)w.ntiles;
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, false, 0, s)
-                                     : cf_fast::lu_wave_pack(d, a, w, dt, true, false, pr, s);
+                                     : wpack(d, a, w, dt, true, false, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
         // FP32: the backward sweep also updates the state (the FP32 change
         // added to the FP64 state), copies NL <- NR and leaves per-tile norm
@@ -768,7 +778,7 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
         const bool fuse = pr == 1;
         if (!fuse) wb.partial = nullptr;
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, wb, false, 0, s)
-                                     : cf_fast::lu_wave_sweep(a, wb, false, pr, s);
+                                     : wsweep(a, wb, false, pr, s);
         if (fuse) {
             if (e == cudaSuccess) e = cf_fast::lu_wave_norm(d, w, c->er_dev, s);
             return e;

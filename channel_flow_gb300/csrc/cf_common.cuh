@@ -28,16 +28,31 @@ __device__ __forceinline__ T rmax(T a, T b) { return (a > b) ? a : b; }
 // FP32 values in their FP64 allocation (flag f32, warp-uniform): no FP64 ->
 // FP32 conversion, which issues to GB300's slow FP64 pipe, on either side.
 // In the FP64 kernels (T = double) the flag is ignored.
+//
+// The choice must not be a runtime branch in the kernels the step driver
+// runs: the compiler turns such short branches into predicated code, and a
+// predicated-off conversion still issues to the FP64 pipe (measured: 60-87 %
+// FP64-pipe activity in FP32 kernels that convert nothing).  The build
+// therefore compiles the kernels a third time with CF_STEP_LAYOUT (namespace
+// cf_drv), where the FP32 intermediates and the FP32 copies of metrics, U_
+// and J are known at compile time to be present; the step driver calls that
+// variant when it has set all of them up.
+#ifdef CF_STEP_LAYOUT
+constexpr bool cf_step_layout = true;
+#else
+constexpr bool cf_step_layout = false;
+#endif
+
 template <typename T>
 __device__ __forceinline__ void rhs_put(double *p, size_t q, T v, int f32)
 {
-    if (sizeof(T) == 4 && f32) reinterpret_cast<float *>(p)[q] = float(v);
+    if (sizeof(T) == 4 && (cf_step_layout || f32)) reinterpret_cast<float *>(p)[q] = float(v);
     else p[q] = double(v);
 }
 template <typename T>
 __device__ __forceinline__ T rhs_get(const double *p, size_t q, int f32)
 {
-    if (sizeof(T) == 4 && f32) return T(reinterpret_cast<const float *>(p)[q]);
+    if (sizeof(T) == 4 && (cf_step_layout || f32)) return T(reinterpret_cast<const float *>(p)[q]);
     return T(p[q]);
 }
 
@@ -48,7 +63,7 @@ __device__ __forceinline__ T rhs_get(const double *p, size_t q, int f32)
 template <typename T>
 __device__ __forceinline__ T met_ld(const double *p, const float *p32, size_t q)
 {
-    if (sizeof(T) == 4 && p32) return T(p32[q]);
+    if (sizeof(T) == 4 && (cf_step_layout || p32)) return T(p32[q]);
     return T(p[q]);
 }
 

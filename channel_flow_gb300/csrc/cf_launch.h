@@ -1,7 +1,9 @@
 // Host launchers of one build variant of the kernels.  cf_variant.cu is
-// compiled twice: namespace cf_exact with --fmad=false (every FP64 result
-// equals the reference's bit for bit) and namespace cf_fast with fused
-// multiply-add (FP64 within 1e-12; also the FP32 instantiations).
+// compiled three times: namespace cf_exact with --fmad=false (every FP64
+// result equals the reference's bit for bit), namespace cf_fast with fused
+// multiply-add (FP64 within 1e-12; also the FP32 instantiations), and
+// namespace cf_drv, the cf_fast kernels with the step driver's FP32 array
+// layout fixed at compile time (CF_STEP_LAYOUT, cf_common.cuh).
 // prec: 0 = double, 1 = float arithmetic inside the kernel.
 #pragma once
 #include "cf_types.h"
@@ -58,3 +60,4 @@ constexpr int CF_LU_PACK = 52;   // doubles per cell of the sweep coefficient pa
 
 CF_DECLARE_LAUNCHERS(cf_exact)
 CF_DECLARE_LAUNCHERS(cf_fast)
+CF_DECLARE_LAUNCHERS(cf_drv)

@@ -25,7 +25,7 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
     const T K = CF_DC(T, d, K);
     // FP32 build: the step driver's FP32 copies of U_ and J when it has
     // them (the same values as converting here, without the conversions)
-    const bool cp = sizeof(T) == 4 && a.U32[0];
+    const bool cp = sizeof(T) == 4 && (cf_step_layout || a.U32[0]);
     T u[5], Jq;
 #pragma unroll
     for (int n = 0; n < 5; n++) u[n] = cp ? T(a.U32[n][q]) : T(a.U_[n][q]);
@@ -184,7 +184,7 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
             // combined in FP32; U - Uq is fixed over a physical step, the
             // step driver keeps it in FP32
             const float d1 = float(a.U_[n][q] - a.U[n][q]);
-            const float d2 = a.dUq32[0] ? a.dUq32[n][q] : float(a.U[n][q] - a.Uq[n][q]);
+            const float d2 = (cf_step_layout || a.dUq32[0]) ? a.dUq32[n][q] : float(a.U[n][q] - a.Uq[n][q]);
             Rp = T(-(3.0f * d1 - d2) * (0.5f / float(dt)));   // dt is FP32 here
         } else {
             Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) * rdt2);
@@ -198,7 +198,7 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
                  (rhs_get<T>(a.Fz[n], fz, f32) - rhs_get<T>(a.Fz[n], f0, f32)) / dZT);
         Rk[n] = Rp + Rf;
     }
-    const T f = CF_DC(T, d, f), Jq = (sizeof(T) == 4 && a.J32) ? T(a.J32[q]) : T(a.J[q]);
+    const T f = CF_DC(T, d, f), Jq = (sizeof(T) == 4 && (cf_step_layout || a.J32)) ? T(a.J32[q]) : T(a.J[q]);
     Rk[1] = Rk[1] + rhs_get<T>(a.vF[0], q, a.f32_rhs) + f / Jq;
     Rk[2] = Rk[2] + rhs_get<T>(a.vF[1], q, a.f32_rhs);
     Rk[3] = Rk[3] + rhs_get<T>(a.vF[2], q, a.f32_rhs);
@@ -595,7 +595,7 @@ __device__ __forceinline__ void lu_update_cell_f32(const cf_dims &d, const cf_lu
 {
     double u[5];
     float f[5];
-    const bool cp = a.U32[0] != nullptr;     // the step driver's FP32 copies of U_ and J
+    const bool cp = cf_step_layout || a.U32[0] != nullptr;     // the step driver's FP32 copies of U_ and J
 #pragma unroll
     for (int n = 0; n < 5; n++) {
         u[n] = a.U_[n][q];
