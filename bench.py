@@ -48,9 +48,10 @@ ALG_BYTES = {"Filter": 80, "Flux_X_limiter": 168, "Flux_Y_limiter": 176, "Flux_Z
 ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>"}
 # DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
 # launch on the 96^3 case divided by its cells) and FP64-pipe activity
-# (profiles/k_flux_y_limiter_96.md)
-NCU_TRAFFIC_PER_CELL = {"Flux_Y_limiter": (76.383744e6 + 12.138496e6) / (96 * 96 * 96)}
-NCU_FP64_PIPE_PCT = {"Flux_Y_limiter": 84.3}
+# (profiles/k_flux_x_limiter_96.md, profiles/k_flux_y_limiter_96.md)
+NCU_TRAFFIC_PER_CELL = {"Flux_X_limiter": (76.710656e6 + 10.772736e6) / (96 * 96 * 96),
+                        "Flux_Y_limiter": (76.383744e6 + 12.138496e6) / (96 * 96 * 96)}
+NCU_FP64_PIPE_PCT = {"Flux_X_limiter": 87.7, "Flux_Y_limiter": 84.3}
 LU_SUBITERATIONS = 10   # LU-SGS sub-iterations of one physical step of the fixed-count schedule
 L2_BYTES = 129 * 2 ** 20
 
@@ -389,7 +390,7 @@ def main():
             "traffic_source": "ncu dram bytes of one launch at 96^3 scaled by cells" if traffic else None,
             "fp64_pipe_active_pct": NCU_FP64_PIPE_PCT.get(dom),
             "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
-            "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 84% pipe busy, "
+            "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 84-88% pipe busy, "
                     "DRAM 1%); the HBM fraction is the byte-model figure"}
 
     # secondary measurements on the same workload: FP32 kernels, and one

@@ -666,28 +666,28 @@ __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_b
 }
 
 // final reduction of the block partial sums, one block, fixed order;
-// er[n] = sqrt(sum) * DN (Dual_time_stepping.cpp:1348-1352).  Each thread
-// sums a contiguous run of partials with eight loads in flight.
+// er[n] = sqrt(sum) * DN (Dual_time_stepping.cpp:1348-1352).  Thread t sums
+// partials t, t + 256, ... in order, eight of them in flight (coalesced).
 __global__ void k_lu_norm(const double *partial, size_t nblk, double DN, double *er)
 {
     __shared__ double sh[5][256];
     const int tid = threadIdx.x;
     double s[5] = {0, 0, 0, 0, 0};
-    const size_t per = (nblk + 255) / 256, b0 = tid * per, b1 = b0 + per < nblk ? b0 + per : nblk;
-    const double *p = partial + 5 * b0;
-    size_t b = b0;
-    for (; b + 8 <= b1; b += 8, p += 40) {
-        double v[40];
-#pragma unroll
-        for (int m = 0; m < 40; m++) v[m] = p[m];
+    size_t b = tid;
+    for (; b + 7 * 256 < nblk; b += 8 * 256) {
+        double v[8][5];
 #pragma unroll
         for (int m = 0; m < 8; m++)
 #pragma unroll
-            for (int n = 0; n < 5; n++) s[n] += v[5 * m + n];
-    }
-    for (; b < b1; b++, p += 5)
+            for (int n = 0; n < 5; n++) v[m][n] = partial[5 * (b + 256 * m) + n];
 #pragma unroll
-        for (int n = 0; n < 5; n++) s[n] += p[n];
+        for (int m = 0; m < 8; m++)
+#pragma unroll
+            for (int n = 0; n < 5; n++) s[n] += v[m][n];
+    }
+    for (; b < nblk; b += 256)
+#pragma unroll
+        for (int n = 0; n < 5; n++) s[n] += partial[5 * b + n];
 #pragma unroll
     for (int n = 0; n < 5; n++) sh[n][tid] = s[n];
     __syncthreads();
