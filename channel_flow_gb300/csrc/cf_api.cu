@@ -693,9 +693,8 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     const size_t fz = (size_t)w.ntiles * 5 * CF_WAVE_TI * CF_WAVE_TJ * T8;
     const size_t nl = (size_t)w.ntiles * 5 * cells * T8;
     const size_t flags = (((size_t)w.ntiles + 2) * sizeof(int) + 255) / 256 * 256;
-    const size_t part = (size_t)w.ntiles * 5 * sizeof(double);
     unsigned char *base = static_cast<unsigned char *>(
-        scratch_bytes(c, "lu_wave", 2 * pack + fx + fy + fz + nl + flags + part));
+        scratch_bytes(c, "lu_wave", 2 * pack + fx + fy + fz + nl + flags));
     if (!base) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: wavefront scratch allocation failed");
     w.packF = base;
     w.packB = base + pack;
@@ -707,7 +706,6 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     w.flags = reinterpret_cast<int *>(f);
     w.counter = w.flags + w.ntiles;
     w.err = w.flags + w.ntiles + 1;
-    w.partial = reinterpret_cast<double *>(f + flags);
     w.trace = nullptr;
     if (c->trace_tiles) {
         if (c->trace_tiles != (size_t)w.ntiles) {
@@ -770,17 +768,15 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_pack(d, a, w, dt, true, false, 0, s)
                                      : wpack(d, a, w, dt, true, false, pr, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
-        // FP32: the backward sweep also updates the state (the FP32 change
-        // added to the FP64 state), copies NL <- NR and leaves per-tile norm
-        // partial sums; its blocks have issue slots to spare while they
-        // wait on their neighbours.  The FP64 sweeps keep their FP64 pipe
-        // for the sweep itself.
-        const bool fuse = pr == 1;
-        if (!fuse) wb.partial = nullptr;
         if (e == cudaSuccess) e = ex ? cf_exact::lu_wave_sweep(a, wb, false, 0, s)
                                      : wsweep(a, wb, false, pr, s);
-        if (fuse) {
-            if (e == cudaSuccess) e = cf_fast::lu_wave_norm(d, w, c->er_dev, s);
+        // the state update and the norms as their own pass over the cells
+        // (in FP32 it also copies NL <- NR; fused into the backward sweep's
+        // tiles it took the blocks' time between tiles, which at
+        // 256x192x192 cost more than the pass)
+        if (pr == 1) {
+            auto finish = st ? cf_drv::lu_finish : cf_fast::lu_finish;
+            if (e == cudaSuccess) e = finish(d, a, c->er_dev, pr, s);
             return e;
         }
     } else {
@@ -853,7 +849,7 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     if (int rc = lu_args(c, p, "Dual_time_stepping", a)) return rc;
     a.f32_rhs = (f32_rhs && kprec(c) == 1) ? 1 : 0;
     // with the wavefront, MR, NL and NR pass between the step driver's own
-    // FP32 kernels only (the fused update reads NR from shared memory)
+    // FP32 kernels only
     a.f32_lu = (a.f32_rhs && c->lu_schedule == CF_LU_WAVEFRONT) ? 1 : 0;
     if (static_metrics && kprec(c) == 1)
         for (int n = 0; n < 9; n++) {

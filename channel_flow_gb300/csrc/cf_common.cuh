@@ -67,8 +67,37 @@ __device__ __forceinline__ T met_ld(const double *p, const float *p32, size_t q)
     return T(p[q]);
 }
 
+// 1/d for the contracted builds.  FP64: the hardware's approximate
+// reciprocal (about 20 correct bits) refined by two Newton-Raphson steps
+// x <- x + x (1 - d x), each doubling the correct bits, so the result lies
+// within about one unit in the last place of the rounded quotient, in fewer
+// FP64-pipe operations than an IEEE-rounded division.  d = 0 gives NaN
+// (callers guard ties).  FP32: the approximate division of the FP32 build.
+template <typename T>
+__device__ __forceinline__ T frcp(T d);
+template <>
+__device__ __forceinline__ float frcp<float>(float d) { return 1.0f / d; }
+template <>
+__device__ __forceinline__ double frcp<double>(double d)
+{
+    double x;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
+    double e = fma(-d, x, 1.0);
+    x = fma(x, e, x);
+    e = fma(-d, x, 1.0);
+    return fma(x, e, x);
+}
+
 // a grid constant of cf_dims in the compute type T (its FP32 copy for float)
 #define CF_DC(T, d, x) (sizeof(T) == 4 ? (T)((d).f_##x) : (T)((d).x))
+// 1/x of a grid constant (dXI, dET, dZT, Pr): in the contracted FP64 build
+// the host's correctly rounded value (the same bits a device division
+// gives, without one per thread), else the division
+#ifdef CF_FAST_MATH
+#define CF_DINV(T, d, x, ix) (sizeof(T) == 8 ? (T)((d).ix) : T(1) / CF_DC(T, d, x))
+#else
+#define CF_DINV(T, d, x, ix) (T(1) / CF_DC(T, d, x))
+#endif
 
 
 #define CF_BOX_INDEX(b, i, j, k)                                    \

@@ -1,6 +1,7 @@
 // Reduced-division forms of the face states and face fluxes, used by the
 // contracted FP64 build and the FP32 build (CF_FAST_MATH).  Same mathematics
-// as cf_flux.cuh, evaluated with fewer IEEE divisions:
+// as cf_flux.cuh, evaluated with fewer divisions, each reciprocal by frcp
+// (cf_common.cuh: Newton-refined hardware reciprocal in FP64):
 //
 // * limited states: every ratio of the MUSCL-5 limiter is a quotient of two
 //   neighbouring differences D_k = u_{k+1} - u_k, so the ten states of a
@@ -25,7 +26,7 @@ namespace CF_NS {
 template <typename T>
 __device__ __forceinline__ T ginv(T D)
 {
-    return D != T(0) ? T(1) / D : T(0);
+    return D != T(0) ? frcp<T>(D) : T(0);
 }
 
 // u[0..5] = cells c-2 .. c+3 of the face's stencil line; left state of cell
@@ -152,7 +153,7 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A 
     // rows next to a wall (Flux_Y_limiter.cpp:115-477): wall averages on
     // faces 1 and ny, the guarded ratio of variable 1 and 3rd order
     if (j == 1) {
-        T temp = T(1.) / (T(1) / T(a.J[qL]) + T(1) / T(a.J[qL + s]));
+        T temp = frcp<T>(frcp<T>(T(a.J[qL])) + frcp<T>(T(a.J[qL + s])));
 #pragma unroll
         for (int n = 0; n < 5; n++) mL[n] = temp * (T(a.U[n][qL]) + T(a.U[n][qL + s]));
     } else if (wallL) {
@@ -174,7 +175,7 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A 
     }
     if (j == ny) {
         const size_t q = d.ix(i + 1, ny, k + 1);
-        T temp = T(1.) / (T(1) / T(a.J[q]) + T(1) / T(a.J[q + s]));
+        T temp = frcp<T>(frcp<T>(T(a.J[q])) + frcp<T>(T(a.J[q + s])));
 #pragma unroll
         for (int n = 0; n < 5; n++) mR[n] = temp * (T(a.U[n][q]) + T(a.U[n][q + s]));
     } else if (wallR) {
@@ -216,10 +217,10 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
         iJ[3] = T(iJp[qL + 1]);
         iJ[4] = T(iJp[qL + 2]);
         iJ[5] = hi3 ? T(0) : T(iJp[qL + 3]);
-        const T jl = lo3 ? T(1.) / (T(-1) * iJ[1] + T(5) * iJ[2] + T(2) * iJ[3])
-                         : T(1.) / (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]);
-        const T jr = hi3 ? T(1.) / (T(2) * iJ[2] + T(5) * iJ[3] - T(1) * iJ[4])
-                         : T(1.) / (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]);
+        const T jl = frcp<T>(lo3 ? (T(-1) * iJ[1] + T(5) * iJ[2] + T(2) * iJ[3])
+                                 : (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]));
+        const T jr = frcp<T>(hi3 ? (T(2) * iJ[2] + T(5) * iJ[3] - T(1) * iJ[4])
+                                 : (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]));
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T u[6];
@@ -236,9 +237,9 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
 #pragma unroll
         for (int n = 0; n < 5; n++) mL[n] = lin3L<T>(a.U[n], a.J, qL, 1);
     } else {
-        const T jl = lo3 ? T(1.) / (T(-1) * T(iJp[qL - 1]) + T(5) * T(iJp[qL]) + T(2) * T(iJp[qL + 1]))
-                         : T(1.) / (T(2) * T(iJp[qL - 2]) - T(13) * T(iJp[qL - 1]) + T(47) * T(iJp[qL]) +
-                                    T(27) * T(iJp[qL + 1]) - T(3) * T(iJp[qL + 2]));
+        const T jl = frcp<T>(lo3 ? (T(-1) * T(iJp[qL - 1]) + T(5) * T(iJp[qL]) + T(2) * T(iJp[qL + 1]))
+                                 : (T(2) * T(iJp[qL - 2]) - T(13) * T(iJp[qL - 1]) + T(47) * T(iJp[qL]) +
+                                    T(27) * T(iJp[qL + 1]) - T(3) * T(iJp[qL + 2])));
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T u[5];
@@ -254,9 +255,9 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
 #pragma unroll
         for (int n = 0; n < 5; n++) mR[n] = lin3R<T>(a.U[n], a.J, qR, 1);
     } else {
-        const T jr = hi3 ? T(1.) / (T(2) * T(iJp[qR - 1]) + T(5) * T(iJp[qR]) - T(1) * T(iJp[qR + 1]))
-                         : T(1.) / (T(-3) * T(iJp[qR - 2]) + T(27) * T(iJp[qR - 1]) + T(47) * T(iJp[qR]) -
-                                    T(13) * T(iJp[qR + 1]) + T(2) * T(iJp[qR + 2]));
+        const T jr = frcp<T>(hi3 ? (T(2) * T(iJp[qR - 1]) + T(5) * T(iJp[qR]) - T(1) * T(iJp[qR + 1]))
+                                 : (T(-3) * T(iJp[qR - 2]) + T(27) * T(iJp[qR - 1]) + T(47) * T(iJp[qR]) -
+                                    T(13) * T(iJp[qR + 1]) + T(2) * T(iJp[qR + 2])));
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T w[5];
@@ -272,9 +273,9 @@ __device__ __forceinline__ void fast_lin_pair(const A &a, size_t qc, ptrdiff_t s
 {
     T iJ[6];
 #pragma unroll
-    for (int t = 0; t < 6; t++) iJ[t] = T(1) / T(a.J[qc + (t - 2) * s]);
-    const T tl = T(1.) / (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]);
-    const T tr = T(1.) / (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]);
+    for (int t = 0; t < 6; t++) iJ[t] = frcp<T>(T(a.J[qc + (t - 2) * s]));
+    const T tl = frcp<T>(T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]);
+    const T tr = frcp<T>(T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
         const auto *U = a.U[n];
@@ -325,11 +326,11 @@ __device__ __forceinline__ void fast_flux_precond_roe(const T *mL, const T *mR, 
 {
     const T n0 = m[3 * dir], n1 = m[3 * dir + 1], n2 = m[3 * dir + 2];
     const T nn = n0 * n0 + n1 * n1 + n2 * n2;
-    const T inorm = T(1) / sqrt(nn);
+    const T inorm = frcp<T>(sqrt(nn));
     const T NX = n0 * inorm, NY = n1 * inorm, NZ = n2 * inorm;
-    const T Km1 = K - T(1), iKm1 = T(1) / Km1, iK = T(1) / K;
+    const T Km1 = K - T(1), iKm1 = frcp<T>(Km1), iK = frcp<T>(K);
 
-    const T _rho = mL[0], irL = T(1) / _rho;
+    const T _rho = mL[0], irL = frcp<T>(_rho);
     const T _u = mL[1] * irL, _v = mL[2] * irL, _w = mL[3] * irL;
     const T _U = n0 * _u + n1 * _v + n2 * _w;
     const T __U = NX * _u + NY * _v + NZ * _w;
@@ -338,7 +339,7 @@ __device__ __forceinline__ void fast_flux_precond_roe(const T *mL, const T *mR, 
     const T _T = _P * irL;
     const T _H = T(0.5) * _VV + K * _T * iKm1;
 
-    const T rho_ = mR[0], irR = T(1) / rho_;
+    const T rho_ = mR[0], irR = frcp<T>(rho_);
     const T u_ = mR[1] * irR, v_ = mR[2] * irR, w_ = mR[3] * irR;
     const T U_ = n0 * u_ + n1 * v_ + n2 * w_;
     const T U__ = NX * u_ + NY * v_ + NZ * w_;
@@ -355,18 +356,18 @@ __device__ __forceinline__ void fast_flux_precond_roe(const T *mL, const T *mR, 
     const T H = T(0.5) * (_H + H_);
     const T C = (H - T(0.5) * VV) * Km1;
     const T Tm = C * iK;                 // P/rho with P = rho*C/K
-    const T iT = K / C;
+    const T iC = frcp<T>(C), iT = K * iC;
 
     const T dU1 = P_ - _P, dU2 = u_ - _u, dU3 = v_ - _v, dU4 = w_ - _w, dU5 = T_ - _T;
 
-    const T beta = rmax(VV / C, e);
+    const T beta = rmax(VV * iC, e);
     const T bm1 = beta - T(1);
     const T S = sqrt(U * U * bm1 * bm1 + T(4) * beta * C * nn);
     const T _S_ = sqrt(_U_ * _U_ * bm1 * bm1 + T(4) * beta * C * (NX * NX + NY * NY + NZ * NZ));
 
     const T TKb = Tm * K * beta;
     const T temp = T(4) * _S_ * TKb;
-    const T it = T(1) / temp, ih = T(0.5) * it;
+    const T it = frcp<T>(temp), ih = T(0.5) * it;
     const T temp1 = S + U + U * beta;
     const T temp2 = -S + U + U * beta;
     const T temp3 = _S_ - _U_ + _U_ * beta;
@@ -430,7 +431,7 @@ __device__ __forceinline__ void fast_flux_precond_roe(const T *mL, const T *mR, 
     const T Fav4 = d41 * dU1 + d42 * dU2 + d43 * dU3 + d44 * dU4 + d45 * dU5;
     const T Fav5 = d51 * dU1 + d52 * dU2 + d53 * dU3 + d54 * dU4 + d55 * dU5;
 
-    const T hJ = T(0.5) / Jf;
+    const T hJ = T(0.5) * frcp<T>(Jf);
     const T Ps = _P + P_;
     F[0] = ((_rho * _U + rho_ * U_) - Ep * Fav1) * hJ;
     F[1] = ((_rho * _u * _U + rho_ * u_ * U_ + n0 * Ps) - Ep * Fav2) * hJ;
@@ -445,18 +446,18 @@ template <typename T>
 __device__ __forceinline__ void fast_flux_roe(const T *mL, const T *mR, const T *m, int dir, T Jf, T K, T *F)
 {
     const T n0 = m[3 * dir], n1 = m[3 * dir + 1], n2 = m[3 * dir + 2];
-    const T insqr = T(1.0) / sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    const T insqr = frcp<T>(sqrt(n0 * n0 + n1 * n1 + n2 * n2));
     const T NX = n0 * insqr, NY = n1 * insqr, NZ = n2 * insqr;
-    const T Km1 = K - T(1), iKm1 = T(1) / Km1;
+    const T Km1 = K - T(1), iKm1 = frcp<T>(Km1);
 
-    const T _rho = mL[0], irL = T(1) / _rho;
+    const T _rho = mL[0], irL = frcp<T>(_rho);
     const T _u = mL[1] * irL, _v = mL[2] * irL, _w = mL[3] * irL;
     const T _U = n0 * _u + n1 * _v + n2 * _w;
     const T _VV = _u * _u + _v * _v + _w * _w;
     const T _P = (mL[4] - T(0.5) * _rho * _VV) * Km1;
     const T _H = T(0.5) * _VV + K * _P * irL * iKm1;
 
-    const T rho_ = mR[0], irR = T(1) / rho_;
+    const T rho_ = mR[0], irR = frcp<T>(rho_);
     const T u_ = mR[1] * irR, v_ = mR[2] * irR, w_ = mR[3] * irR;
     const T U_ = n0 * u_ + n1 * v_ + n2 * w_;
     const T VV_ = u_ * u_ + v_ * v_ + w_ * w_;
@@ -464,7 +465,7 @@ __device__ __forceinline__ void fast_flux_roe(const T *mL, const T *mR, const T 
     const T H_ = T(0.5) * VV_ + K * P_ * irR * iKm1;
 
     const T temp5 = sqrt(_rho), temp6 = sqrt(rho_);
-    const T it4 = T(1) / (temp5 + temp6);
+    const T it4 = frcp<T>(temp5 + temp6);
     const T rho = temp5 * temp6;
     const T u = (temp5 * _u + temp6 * u_) * it4;
     const T v = (temp5 * _v + temp6 * v_) * it4;
@@ -480,10 +481,10 @@ __device__ __forceinline__ void fast_flux_roe(const T *mL, const T *mR, const T 
     const T dU4 = rho_ * w_ - _rho * _w;
     const T dU5 = (P_ * iKm1 + T(0.5) * rho_ * VV_) - (_P * iKm1 + T(0.5) * _rho * _VV);
 
-    const T S = sqrt(C), iS = T(1) / S;
+    const T S = sqrt(C), iS = frcp<T>(S);
     const T Un = U * insqr, aUn = fabs(Un);
     const T dP = P_ - _P, dUn = (U_ - _U) * insqr;
-    const T deltaU = (S - aUn) * dP / (rho * C) + Un * iS * dUn;
+    const T deltaU = (S - aUn) * dP * frcp<T>(rho * C) + Un * iS * dUn;
     const T deltaP = Un * iS * dP + (S - aUn) * rho * dUn;
 
     const T Fav1 = aUn * dU1 + deltaU * rho;
@@ -492,7 +493,7 @@ __device__ __forceinline__ void fast_flux_roe(const T *mL, const T *mR, const T 
     const T Fav4 = aUn * dU4 + deltaU * rho * w + deltaP * NZ;
     const T Fav5 = dir == 1 ? aUn * dU5 + deltaU * rho * H + deltaP * Un : aUn * dU5 + deltaU * rho * H + deltaP * U;
 
-    const T sq = T(1) / insqr, hJ = T(0.5) / Jf;
+    const T sq = frcp<T>(insqr), hJ = T(0.5) * frcp<T>(Jf);
     const T Ps = _P + P_;
     F[0] = ((_rho * _U + rho_ * U_) - Fav1 * sq) * hJ;
     F[1] = ((_rho * _u * _U + rho_ * u_ * U_ + n0 * Ps) - Fav2 * sq) * hJ;

@@ -42,7 +42,6 @@ constexpr int CF_LU_PACK = 52;   // doubles per cell of the sweep coefficient pa
     cudaError_t lu_jacobi(const cf_dims &d, const cf_lu_args &a, double dt, int prec, cudaStream_t s); \
     cudaError_t lu_copy(const cf_dims &d, const cf_lu_args &a, cudaStream_t s);                        \
     cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, int prec, cudaStream_t s);     \
-    cudaError_t lu_wave_norm(const cf_dims &d, const cf_wave_args &w, double *er_dev, cudaStream_t s);  \
     size_t lu_partial_count(const cf_dims &d);                                                          \
     cudaError_t statistic(const cf_dims &d, const cf_stat_args &a, double *acc, double *partial,         \
                           size_t partial_len, cudaStream_t s);                                          \

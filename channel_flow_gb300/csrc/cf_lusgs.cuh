@@ -32,6 +32,20 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
     Jq = cp ? T(a.J32[q]) : T(a.J[q]);
     const T u1 = u[0];
     s.rho = u1 * Jq;
+#ifdef CF_FAST_MATH
+    // three reciprocals instead of seven divisions
+    const T iu1 = frcp<T>(u1), irho = frcp<T>(s.rho);
+    const T ikm1 = sizeof(T) == 8 ? T(d.ikm1) : T(1) / (K - T(1));
+    s.u = u[1] * iu1;
+    s.v = u[2] * iu1;
+    s.w = u[3] * iu1;
+    s.VV = s.u * s.u + s.v * s.v + s.w * s.w;
+    s.P = (u[4] * Jq - T(0.5) * s.rho * s.VV) * (K - T(1));
+    s.C = K * s.P * irho;
+    s.Tt = s.P * irho;
+    s.H = T(0.5) * s.VV + s.C * ikm1;
+    s.beta = rmax(s.VV * frcp<T>(s.C), CF_DC(T, d, e));
+#else
     s.u = u[1] / u1;
     s.v = u[2] / u1;
     s.w = u[3] / u1;
@@ -41,6 +55,7 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
     s.Tt = s.P / s.rho;
     s.H = T(0.5) * s.VV + s.C / (K - T(1));
     s.beta = rmax(s.VV / s.C, CF_DC(T, d, e));
+#endif
     return s;
 }
 
@@ -108,13 +123,23 @@ __device__ __forceinline__ ldiag<T> lu_diag(const cf_dims &d, const cf_lu_args &
     T lambdaX = ((beta + T(1)) * fabs(U) + Sx) / T(2);
     T lambdaY = ((beta + T(1)) * fabs(V) + Sy) / T(2);
     T lambdaZ = ((beta + T(1)) * fabs(W) + Sz) / T(2);
-    T lambda = lambdaX / CF_DC(T, d, dXI) + lambdaY / CF_DC(T, d, dET) + lambdaZ / CF_DC(T, d, dZT);
     ldiag<T> g;
+#ifdef CF_FAST_MATH
+    T lambda = lambdaX * CF_DINV(T, d, dXI, idXI) + lambdaY * CF_DINV(T, d, dET, idET) +
+               lambdaZ * CF_DINV(T, d, dZT, idZT);
+    g.d11 = T(2) * deltaT * frcp<T>(T(3) * beta + T(2) * lambda * deltaT);
+    g.d22 = T(2) * deltaT * frcp<T>(T(3) + T(2) * lambda * deltaT);
+    T temp1 = T(6) * (K - T(1)) * (beta - T(1)) * deltaT;
+    T temp2 = K * (T(3) + T(2) * lambda * deltaT) * (T(3) * beta + T(2) * lambda * deltaT) * s.rho;
+    g.d51 = -temp1 * frcp<T>(temp2);
+#else
+    T lambda = lambdaX / CF_DC(T, d, dXI) + lambdaY / CF_DC(T, d, dET) + lambdaZ / CF_DC(T, d, dZT);
     g.d11 = T(2) * deltaT / (T(3) * beta + T(2) * lambda * deltaT);
     g.d22 = T(2) * deltaT / (T(3) + T(2) * lambda * deltaT);
     T temp1 = T(6) * (K - T(1)) * (beta - T(1)) * deltaT;
     T temp2 = K * (T(3) + T(2) * lambda * deltaT) * (T(3) * beta + T(2) * lambda * deltaT) * s.rho;
     g.d51 = -temp1 / temp2;
+#endif
     return g;
 }
 
@@ -155,17 +180,27 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
     T d13 = -(K - T(1)) * v * beta;
     T d14 = -(K - T(1)) * w * beta;
     T d15 = (K - T(1)) * beta;
-    T d21 = -u / rho, d22 = T(1) / rho;
-    T d31 = -v / rho;
-    T d41 = -w / rho;
-    T d51 = (K - T(1)) * (VV + K * Tt * beta + (K - T(1)) * VV * beta + H * (T(-1) + beta - K * beta)) / temp;
-    T d52 = -(K - T(1)) * u * (T(1) + (K - T(1)) * beta) / temp;
-    T d53 = -(K - T(1)) * v * (T(1) + (K - T(1)) * beta) / temp;
-    T d54 = -(K - T(1)) * w * (T(1) + (K - T(1)) * beta) / temp;
-    T d55 = (K - T(1)) * (T(1) + (K - T(1)) * beta) / temp;
+#ifdef CF_FAST_MATH
+    // reciprocals of rho, K rho, J and the spacings instead of 26 divisions
+    const T irho = frcp<T>(rho), itemp = frcp<T>(temp);
+#define CF_LDIV(x, y, iy) ((x) * (iy))
+#else
+#define CF_LDIV(x, y, iy) ((x) / (y))
+#endif
+    T d21 = CF_LDIV(-u, rho, irho), d22 = CF_LDIV(T(1), rho, irho);
+    T d31 = CF_LDIV(-v, rho, irho);
+    T d41 = CF_LDIV(-w, rho, irho);
+    T d51 = CF_LDIV((K - T(1)) * (VV + K * Tt * beta + (K - T(1)) * VV * beta + H * (T(-1) + beta - K * beta)), temp, itemp);
+    T d52 = CF_LDIV(-(K - T(1)) * u * (T(1) + (K - T(1)) * beta), temp, itemp);
+    T d53 = CF_LDIV(-(K - T(1)) * v * (T(1) + (K - T(1)) * beta), temp, itemp);
+    T d54 = CF_LDIV(-(K - T(1)) * w * (T(1) + (K - T(1)) * beta), temp, itemp);
+    T d55 = CF_LDIV((K - T(1)) * (T(1) + (K - T(1)) * beta), temp, itemp);
     const size_t fx = d.ix(i, j - 1, k - 1), f0 = d.ix(i - 1, j - 1, k - 1);
     const size_t fy = d.ix(i - 1, j, k - 1), fz = d.ix(i - 1, j - 1, k);
     const T dXI = CF_DC(T, d, dXI), dET = CF_DC(T, d, dET), dZT = CF_DC(T, d, dZT);
+#ifdef CF_FAST_MATH
+    const T iXI = CF_DINV(T, d, dXI, idXI), iET = CF_DINV(T, d, dET, idET), iZT = CF_DINV(T, d, dZT, idZT);
+#endif
     T Rk[5];
 #ifdef CF_FAST_MATH
     const double rdt2 = sizeof(T) == 4 ? 0.0 : 0.5 / dt;   // one FP64 division per cell instead of five
@@ -193,16 +228,20 @@ __device__ __forceinline__ void lu_mr(const cf_dims &d, const cf_lu_args &a, int
         T Rp = T(-(3.0 * a.U_[n][q] - 4.0 * a.U[n][q] + a.Uq[n][q]) / (2.0 * dt));
 #endif
         const int f32 = a.f32_rhs;
-        T Rf = -((rhs_get<T>(a.Fx[n], fx, f32) - rhs_get<T>(a.Fx[n], f0, f32)) / dXI +
-                 (rhs_get<T>(a.Fy[n], fy, f32) - rhs_get<T>(a.Fy[n], f0, f32)) / dET +
-                 (rhs_get<T>(a.Fz[n], fz, f32) - rhs_get<T>(a.Fz[n], f0, f32)) / dZT);
+        T Rf = -(CF_LDIV(rhs_get<T>(a.Fx[n], fx, f32) - rhs_get<T>(a.Fx[n], f0, f32), dXI, iXI) +
+                 CF_LDIV(rhs_get<T>(a.Fy[n], fy, f32) - rhs_get<T>(a.Fy[n], f0, f32), dET, iET) +
+                 CF_LDIV(rhs_get<T>(a.Fz[n], fz, f32) - rhs_get<T>(a.Fz[n], f0, f32), dZT, iZT));
         Rk[n] = Rp + Rf;
     }
     const T f = CF_DC(T, d, f), Jq = (sizeof(T) == 4 && (cf_step_layout || a.J32)) ? T(a.J32[q]) : T(a.J[q]);
-    Rk[1] = Rk[1] + rhs_get<T>(a.vF[0], q, a.f32_rhs) + f / Jq;
+#ifdef CF_FAST_MATH
+    const T iJq = frcp<T>(Jq);
+#endif
+    Rk[1] = Rk[1] + rhs_get<T>(a.vF[0], q, a.f32_rhs) + CF_LDIV(f, Jq, iJq);
     Rk[2] = Rk[2] + rhs_get<T>(a.vF[1], q, a.f32_rhs);
     Rk[3] = Rk[3] + rhs_get<T>(a.vF[2], q, a.f32_rhs);
-    Rk[4] = Rk[4] + rhs_get<T>(a.vF[3], q, a.f32_rhs) + f * u / Jq;
+    Rk[4] = Rk[4] + rhs_get<T>(a.vF[3], q, a.f32_rhs) + CF_LDIV(f * u, Jq, iJq);
+#undef CF_LDIV
     MR[0] = (d11 * Rk[0] + d12 * Rk[1] + d13 * Rk[2] + d14 * Rk[3] + d15 * Rk[4]);
     MR[1] = (d21 * Rk[0] + d22 * Rk[1]);
     MR[2] = (d31 * Rk[0] + d22 * Rk[2]);
@@ -635,9 +674,14 @@ __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_b
     if (k < b.k0 + b.nk && j < b.j0 + b.nj) {
         const size_t q = d.ix(i, j, k);
         if (sizeof(T) == 4) {
+            // FP32: also NL <- NR here (the arrays may hold FP32 values,
+            // which the FP64 copy kernel would pair up wrongly)
             float nr[5];
 #pragma unroll
-            for (int n = 0; n < 5; n++) nr[n] = rhs_get<float>(a.NR[n], q, a.f32_lu);
+            for (int n = 0; n < 5; n++) {
+                nr[n] = rhs_get<float>(a.NR[n], q, a.f32_lu);
+                rhs_put<float>(a.NL[n], q, nr[n], a.f32_lu);
+            }
             lu_update_cell_f32(d, a, q, nr, r2);
         } else {
             double nr[5];

@@ -23,6 +23,7 @@ struct cf_dims {
     // FP64 -> FP32 conversion of a kernel parameter issues to the FP64 pipe)
     float f_dXI, f_dET, f_dZT, f_K, f_R, f_e, f_Cv, f_mu_L, f_Pr_L, f_f, f_high;
     double ikm1;              // 1 / (K - 1), for the contracted build's state update
+    double idXI, idET, idZT, iPr;   // 1/dXI, 1/dET, 1/dZT, 1/Pr_L (correctly rounded, host)
 
     __host__ __device__ __forceinline__ size_t ix(int i, int j, int k) const
     {
@@ -39,6 +40,7 @@ static inline void cf_dims_fill_f32(cf_dims &d)
     d.f_K = (float)d.K; d.f_R = (float)d.R; d.f_e = (float)d.e; d.f_Cv = (float)d.Cv;
     d.f_mu_L = (float)d.mu_L; d.f_Pr_L = (float)d.Pr_L; d.f_f = (float)d.f; d.f_high = (float)d.high;
     d.ikm1 = 1.0 / (d.K - 1.0);
+    d.idXI = 1.0 / d.dXI; d.idET = 1.0 / d.dET; d.idZT = 1.0 / d.dZT; d.iPr = 1.0 / d.Pr_L;
 }
 
 struct cf_ptr5 {
@@ -149,7 +151,6 @@ struct cf_wave_args {
     int *err;                // bit 0: dependency wait ran out, bit 1: pack copy wait ran out
     long long *trace;        // optional: per tile 4 global-timer stamps (claimed, inputs ready,
                              // pack landed, done); NULL when tracing is off
-    double *partial;         // per tile: the 5 residual-norm partial sums of the fused update
 };
 
 struct cf_stat_args {

@@ -276,15 +276,6 @@ cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, int
     return cudaGetLastError();
 }
 
-// er from the per-tile partial sums of the update fused into the backward sweep
-cudaError_t lu_wave_norm(const cf_dims &d, const cf_wave_args &w, double *er_dev, cudaStream_t s)
-{
-    if (!w.partial) return cudaErrorInvalidValue;
-    const double DN = 1. / (d.X_out * d.Y_out * d.Z_out);
-    k_lu_norm<<<1, 256, 0, s>>>(w.partial, (size_t)w.ntiles, DN, er_dev);
-    return cudaGetLastError();
-}
-
 template <int KIND>
 static cudaError_t stat_kind(const cf_dims &d, const cf_stat_args &a, double *partial, size_t partial_len,
                              double *out, int Ym, st_qmap qm, int j0, int nrows, int accumulate,

@@ -35,9 +35,16 @@ __global__ void k_visc_prim(cf_dims d, cf_visc_args a, size_t n)
     if (q >= n) return;
     const T K = CF_DC(T, d, K), R = CF_DC(T, d, R);
     T rho = T(a.U[0][q]);
+#ifdef CF_FAST_MATH
+    const T irho = frcp<T>(rho);
+    T U = T(a.U[1][q]) * irho;
+    T V = T(a.U[2][q]) * irho;
+    T W = T(a.U[3][q]) * irho;
+#else
     T U = T(a.U[1][q]) / rho;
     T V = T(a.U[2][q]) / rho;
     T W = T(a.U[3][q]) / rho;
+#endif
     T VV = U * U + V * V + W * W;
     T Jq = T(a.J[q]);
     T P = (T(a.U[4][q]) - T(0.5) * rho * VV) * (K - T(1)) * Jq;
@@ -144,22 +151,27 @@ __device__ __forceinline__ vcross<T> ccross(T p0, T p1, T p2, T q0, T q1, T q2)
 // register footprint of one face: no spills in FP64, and in FP32 twice the
 // resident warps of a kernel doing all three faces, which measured slower)
 template <typename T, int FACE>
-__global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const T K = CF_DC(T, d, K), Cv = CF_DC(T, d, Cv), mu_E = CF_DC(T, d, mu_L), Pr_E = CF_DC(T, d, Pr_L);
 #ifdef CF_FAST_MATH
     // the contracted and FP32 builds multiply by reciprocals of Pr and J_f
-    const T iPr = T(1) / Pr_E;
+    const T iPr = CF_DINV(T, d, Pr_L, iPr);
 #define CF_VPR(x) ((x) * iPr)
 #define CF_VJF(x) ((x) * iJf)
 #else
 #define CF_VPR(x) ((x) / (Pr_E))
 #define CF_VJF(x) ((x) / Jf)
 #endif
-    const T invXI = T(1.) / CF_DC(T, d, dXI), invET = T(1.) / CF_DC(T, d, dET), invZT = T(1.) / CF_DC(T, d, dZT);
+    const T invXI = CF_DINV(T, d, dXI, idXI), invET = CF_DINV(T, d, dET, idET), invZT = CF_DINV(T, d, dZT, idZT);
+#ifdef CF_FAST_MATH
+    // 1/(4 d) = (1/d)/4 exactly: a power-of-two scaling commutes with rounding
+    const T inv4XI = T(0.25) * invXI, inv4ET = T(0.25) * invET, inv4ZT = T(0.25) * invZT;
+#else
     const T inv4XI = T(1.) / (T(4) * CF_DC(T, d, dXI)), inv4ET = T(1.) / (T(4) * CF_DC(T, d, dET)),
             inv4ZT = T(1.) / (T(4) * CF_DC(T, d, dZT));
+#endif
     const size_t q = d.ix(i, j, k), f = d.ix(i - 1, j - 1, k - 1);
     const vcell<T> c = ld<T>(a, q);
     const vcell<T> im = ld<T>(a, d.ix(i - 1, j, k)), jm = ld<T>(a, d.ix(i, j - 1, k)),
@@ -183,7 +195,7 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         T Ux = T(0.5) * (c.u + im.u), Vx = T(0.5) * (c.v + im.v), Wx = T(0.5) * (c.w + im.w);
         T Jf = met_ld<T>(a.Jf[0], a.Jf32[0], f);
 #ifdef CF_FAST_MATH
-        const T iJf = T(1) / Jf;
+        const T iJf = frcp<T>(Jf);
 #endif
         rhs_put<T>(a.LL[0], q, T(CF_VJF(mu_E * (A.s1 * X.du + A.s5 * X.dv + A.s7 * X.dw + D.x1 * Y.du + D.x7 * Y.dv + D.x9 * Y.dw + E.x1 * Z.du + E.x7 * Z.dv + E.x9 * Z.dw))), a.f32_io);
         rhs_put<T>(a.LL[1], q, T(CF_VJF(mu_E * (A.s5 * X.du + A.s2 * X.dv + A.s6 * X.dw + D.x5 * Y.du + D.x2 * Y.dv + D.x10 * Y.dw + E.x5 * Z.du + E.x2 * Z.dv + E.x10 * Z.dw))), a.f32_io);
@@ -209,7 +221,7 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         T Uy = T(0.5) * (c.u + jm.u), Vy = T(0.5) * (c.v + jm.v), Wy = T(0.5) * (c.w + jm.w);
         T Jf = met_ld<T>(a.Jf[1], a.Jf32[1], f);
 #ifdef CF_FAST_MATH
-        const T iJf = T(1) / Jf;
+        const T iJf = frcp<T>(Jf);
 #endif
         rhs_put<T>(a.ML[0], q, T(CF_VJF(mu_E * (D.x1 * X.du + D.x5 * X.dv + D.x6 * X.dw + B.s1 * Y.du + B.s5 * Y.dv + B.s7 * Y.dw + F.x1 * Z.du + F.x7 * Z.dv + F.x9 * Z.dw))), a.f32_io);
         rhs_put<T>(a.ML[1], q, T(CF_VJF(mu_E * (D.x7 * X.du + D.x2 * X.dv + D.x8 * X.dw + B.s5 * Y.du + B.s2 * Y.dv + B.s6 * Y.dw + F.x5 * Z.du + F.x2 * Z.dv + F.x10 * Z.dw))), a.f32_io);
@@ -235,7 +247,7 @@ __global__ void __launch_bounds__(256) k_visc_faces(cf_dims d, cf_visc_args a, c
         T Uz = T(0.5) * (c.u + km.u), Vz = T(0.5) * (c.v + km.v), Wz = T(0.5) * (c.w + km.w);
         T Jf = met_ld<T>(a.Jf[2], a.Jf32[2], f);
 #ifdef CF_FAST_MATH
-        const T iJf = T(1) / Jf;
+        const T iJf = frcp<T>(Jf);
 #endif
         rhs_put<T>(a.NL[0], q, T(CF_VJF(mu_E * (E.x1 * X.du + E.x5 * X.dv + E.x6 * X.dw + F.x1 * Y.du + F.x5 * Y.dv + F.x6 * Y.dw + Cc.s1 * Z.du + Cc.s5 * Z.dv + Cc.s7 * Z.dw))), a.f32_io);
         rhs_put<T>(a.NL[1], q, T(CF_VJF(mu_E * (E.x7 * X.du + E.x2 * X.dv + E.x8 * X.dw + F.x7 * Y.du + F.x2 * Y.dv + F.x8 * Y.dw + Cc.s5 * Z.du + Cc.s2 * Z.dv + Cc.s6 * Z.dw))), a.f32_io);
@@ -254,7 +266,7 @@ template <typename T>
 __global__ void k_visc_div(cf_dims d, cf_visc_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
-    const T invXI = T(1.) / CF_DC(T, d, dXI), invET = T(1.) / CF_DC(T, d, dET), invZT = T(1.) / CF_DC(T, d, dZT);
+    const T invXI = CF_DINV(T, d, dXI, idXI), invET = CF_DINV(T, d, dET, idET), invZT = CF_DINV(T, d, dZT, idZT);
     const size_t q = d.ix(i, j, k), qi = d.ix(i + 1, j, k), qj = d.ix(i, j + 1, k), qk = q + 1;
 #pragma unroll
     for (int v = 0; v < 4; v++) {

@@ -559,42 +559,6 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
                 else rhs_put<T>(a.NR[n], q, x, a.f32_lu);
             }
         }
-        if (!FWD && w.partial) {
-            // The tile's cells are final: the state update (FP32 change,
-            // FP64 state; lu_update_cell_f32), NL <- NR and the tile's norm
-            // partial sums here, after the done flag,
-            // where they overlap the sweep's dependency waits instead of
-            // taking a pass of their own (no tile of this sweep reads U_)
-            double r2[5] = {0, 0, 0, 0, 0};
-            for (int c = tid; c < WV_CELLS; c += 32 * WV_WARPS) {
-                const int li = c >> 6, lj = (c >> 3) & 7, lk = c & 7;
-                if (li < ti && lj < tj && lk < tk) {
-                    const size_t q = d.ix(i0 + li, j0 + lj, k0 + lk);
-                    float nr[5];
-#pragma unroll
-                    for (int n = 0; n < 5; n++) {
-                        nr[n] = float(sN[n * WV_CELLS + c]);
-                        rhs_put<T>(a.NL[n], q, sN[n * WV_CELLS + c], a.f32_lu);
-                    }
-                    lu_update_cell_f32(d, a, q, nr, r2);
-                }
-            }
-            // fixed-order tree over the block in the incoming-term buffer,
-            // idle until the next tile is staged
-            double *red = reinterpret_cast<double *>(sin);
-#pragma unroll
-            for (int n = 0; n < 5; n++) red[n * 32 * WV_WARPS + tid] = r2[n];
-            __syncthreads();
-            for (int m = 16 * WV_WARPS; m > 0; m >>= 1) {
-                if (tid < m)
-#pragma unroll
-                    for (int n = 0; n < 5; n++) red[n * 32 * WV_WARPS + tid] += red[n * 32 * WV_WARPS + tid + m];
-                __syncthreads();
-            }
-            if (tid == 0)
-#pragma unroll
-                for (int n = 0; n < 5; n++) w.partial[5 * (size_t)tile + n] = red[n * 32 * WV_WARPS];
-        }
         slot = s_slot;
         __syncthreads();
     }
