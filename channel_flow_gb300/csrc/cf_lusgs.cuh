@@ -15,6 +15,7 @@ namespace CF_NS {
 template <typename T>
 struct lstate {
     T rho, u, v, w, VV, P, C, Tt, H, beta;
+    T irho;      // 1/rho (contracted builds)
 };
 
 // Dual_time_stepping.cpp:344-363
@@ -35,6 +36,7 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
 #ifdef CF_FAST_MATH
     // three reciprocals instead of seven divisions
     const T iu1 = frcp<T>(u1), irho = frcp<T>(s.rho);
+    s.irho = irho;
     const T ikm1 = sizeof(T) == 8 ? T(d.ikm1) : T(1) / (K - T(1));
     s.u = u[1] * iu1;
     s.v = u[2] * iu1;
@@ -46,6 +48,7 @@ __device__ __forceinline__ lstate<T> lu_state(const cf_dims &d, const cf_lu_args
     s.H = T(0.5) * s.VV + s.C * ikm1;
     s.beta = rmax(s.VV * frcp<T>(s.C), CF_DC(T, d, e));
 #else
+    s.irho = T(0);
     s.u = u[1] / u1;
     s.v = u[2] / u1;
     s.w = u[3] / u1;
@@ -78,6 +81,15 @@ __device__ __forceinline__ lsplit<T> lu_split(lstate<T> s, T m0, T m1, T m2, boo
     A.p12 = T(0.5) * s.P * K * s.beta * m0;
     A.p13 = T(0.5) * s.P * K * s.beta * m1;
     A.p14 = T(0.5) * s.P * K * s.beta * m2;
+#ifdef CF_FAST_MATH
+    A.p21 = T(0.5) * m0 * s.irho;
+    A.p22 = T(0.5) * (U + dd);
+    A.p31 = T(0.5) * m1 * s.irho;
+    A.p33 = A.p22;
+    A.p41 = T(0.5) * m2 * s.irho;
+    A.p44 = A.p22;
+    A.p51 = T(0.5) * U * (K - T(1)) * (s.beta - T(1)) * s.irho * frcp<T>(K);
+#else
     A.p21 = T(0.5) * m0 / s.rho;
     A.p22 = T(0.5) * (U + dd);
     A.p31 = T(0.5) * m1 / s.rho;
@@ -85,6 +97,7 @@ __device__ __forceinline__ lsplit<T> lu_split(lstate<T> s, T m0, T m1, T m2, boo
     A.p41 = T(0.5) * m2 / s.rho;
     A.p44 = A.p22;
     A.p51 = T(0.5) * U * (K - T(1)) * (s.beta - T(1)) / s.rho / K;
+#endif
     if (xform) {
         A.p52 = T(0.5) * m0 * s.beta * s.Tt * (K - T(1));
         A.p53 = T(0.5) * m1 * s.beta * s.Tt * (K - T(1));
@@ -571,7 +584,7 @@ __device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_arg
 #ifdef CF_FAST_MATH
     // FP64 with three divisions instead of ten (reciprocals of U1 and J,
     // 1/(K-1) from the host, 1/rho_old = (1/U1)(1/J))
-    const double iu1 = 1.0 / a.U_[0][q], iJ = 1.0 / Jq;
+    const double iu1 = frcp<double>(a.U_[0][q]), iJ = frcp<double>(Jq);
     double Uold = a.U_[1][q] * iu1;
     double Vold = a.U_[2][q] * iu1;
     double Wold = a.U_[3][q] * iu1;
@@ -592,8 +605,8 @@ __device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_arg
     double V = Vold + nr[2] * Jq;
     double W = Wold + nr[3] * Jq;
     double Tt = Told + nr[4] * Jq;
-    double rho = P / Tt;
 #ifdef CF_FAST_MATH
+    const double rho = P * frcp<double>(Tt);
     const double rJ = rho * iJ;
     a.U_[0][q] = rJ;
     a.U_[1][q] = rJ * U;
@@ -601,6 +614,7 @@ __device__ __forceinline__ void lu_update_cell(const cf_dims &d, const cf_lu_arg
     a.U_[3][q] = rJ * W;
     a.U_[4][q] = (P * d.ikm1 + 0.5 * rho * (U * U + V * V + W * W)) * iJ;
 #else
+    const double rho = P / Tt;
     a.U_[0][q] = rho / Jq;
     a.U_[1][q] = rho * U / Jq;
     a.U_[2][q] = rho * V / Jq;
