@@ -77,9 +77,9 @@ __global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__
         const double a_ = Yp[q + s] - Yp[q - s];
         const double b_ = Yp[q + s] - Yp[q];
         const double c_ = Yp[q] - Yp[q - s];
-        const double iJ = 1.0 / J[q];
-        cA[q] = ST(b_ / a_ * (J[q - s] * iJ));
-        cC[q] = ST(c_ / a_ * (J[q + s] * iJ));
+        const double iJ = frcp<double>(J[q]), ia = frcp<double>(a_);
+        cA[q] = ST(b_ * ia * (J[q - s] * iJ));
+        cC[q] = ST(c_ * ia * (J[q + s] * iJ));
     }
 }
 
@@ -286,7 +286,7 @@ __global__ void k_filter_energy4(cf_dims d, cf_ptr5 U, filt_ptr4<ST> acc, double
     T u1 = T(U.p[0][q]), f1 = T(acc.p[0][q]);
 #ifdef CF_FAST_MATH
     // two reciprocals instead of six divisions
-    const T iu = T(1) / u1, iff = T(1) / f1;
+    const T iu = frcp<T>(u1), iff = frcp<T>(f1);
     T Ue = T(U.p[1][q]) * iu - T(acc.p[1][q]) * iff;
     T Ve = T(U.p[2][q]) * iu - T(acc.p[2][q]) * iff;
     T We = T(U.p[3][q]) * iu - T(acc.p[3][q]) * iff;

@@ -22,11 +22,35 @@
 
 namespace CF_NS {
 
+// The limiter's comparisons in FP64 on the integer pipe: the contracted
+// FP64 build is bound by the FP64 pipe, which would also issue every FP64
+// compare.  fkey orders doubles as signed integers (the sign-magnitude bit
+// pattern turned two's complement); the order is the floating-point order
+// except that -0 < +0 (the limiter then returns -0 for 0, the same state)
+// and NaN (which these limiters are not given).  FP32 keeps its compares.
+__device__ __forceinline__ long long fkey(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+template <typename T>
+__device__ __forceinline__ T lmin(T a, T b) { return rmin(a, b); }
+template <>
+__device__ __forceinline__ double lmin<double>(double a, double b) { return fkey(a) < fkey(b) ? a : b; }
+template <typename T>
+__device__ __forceinline__ T lmax(T a, T b) { return rmax(a, b); }
+template <>
+__device__ __forceinline__ double lmax<double>(double a, double b) { return fkey(a) > fkey(b) ? a : b; }
+template <typename T>
+__device__ __forceinline__ bool nonzero(T D) { return D != T(0); }
+template <>
+__device__ __forceinline__ bool nonzero<double>(double D) { return (__double_as_longlong(D) << 1) != 0; }
+
 // reciprocal of a neighbour difference, 0 for a tie
 template <typename T>
 __device__ __forceinline__ T ginv(T D)
 {
-    return D != T(0) ? frcp<T>(D) : T(0);
+    return nonzero(D) ? frcp<T>(D) : T(0);
 }
 
 // u[0..5] = cells c-2 .. c+3 of the face's stencil line; left state of cell
@@ -44,7 +68,7 @@ __device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, 
         const T rLi = (u[4] - u[3]) * inv2;
         bL = T(1.) / T(30) * (T(-2) * (u[1] - u[0]) * inv1 + T(11) + T(24) * rL - T(3) * rL * rLi);
     }
-    const T phiL = rmax(T(0), rmin(T(2), rmin(T(2) * rL, bL)));
+    const T phiL = lmax(T(0), lmin(T(2), lmin(T(2) * rL, bL)));
     mL = (S > 0 ? u[2] + T(0.5) * phiL * D1 : u[2] - T(0.5) * phiL * D1) * jL;
     const T rR = D2 * inv3;
     T bR;
@@ -54,7 +78,7 @@ __device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, 
         const T irR = D1 * inv2;
         bR = T(1.) / T(30) * (T(-2) * (u[5] - u[4]) * inv3 + T(11) + T(24) * rR - T(3) * rR * irR);
     }
-    const T phiR = rmax(T(0), rmin(T(2), rmin(T(2) * rR, bR)));
+    const T phiR = lmax(T(0), lmin(T(2), lmin(T(2) * rR, bR)));
     mR = (u[3] - T(0.5) * phiR * D3) * jR;
 }
 
@@ -72,7 +96,7 @@ __device__ __forceinline__ T fast_left(const T *u, bool o3)
         const T rLi = (u[4] - u[3]) * ginv(D2);
         b = T(1.) / T(30) * (T(-2) * (u[1] - u[0]) * inv1 + T(11) + T(24) * rL - T(3) * rL * rLi);
     }
-    const T phi = rmax(T(0), rmin(T(2), rmin(T(2) * rL, b)));
+    const T phi = lmax(T(0), lmin(T(2), lmin(T(2) * rL, b)));
     return S > 0 ? u[2] + T(0.5) * phi * D1 : u[2] - T(0.5) * phi * D1;
 }
 
@@ -91,7 +115,7 @@ __device__ __forceinline__ T fast_right(const T *w, bool o3)
         const T irR = (w[1] - w[0]) * ginv(Dm);
         b = T(1.) / T(30) * (T(-2) * (w[4] - w[3]) * invp + T(11) + T(24) * rR - T(3) * rR * irR);
     }
-    const T phi = rmax(T(0), rmin(T(2), rmin(T(2) * rR, b)));
+    const T phi = lmax(T(0), lmin(T(2), lmin(T(2) * rR, b)));
     return w[2] - T(0.5) * phi * Dp;
 }
 
