@@ -694,15 +694,14 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     const size_t nl = (size_t)w.ntiles * 5 * cells * T8;
     const size_t flags = (((size_t)w.ntiles + 2) * sizeof(int) + 255) / 256 * 256;
     unsigned char *base = static_cast<unsigned char *>(
-        scratch_bytes(c, "lu_wave", 2 * pack + fx + fy + fz + nl + flags));
+        scratch_bytes(c, "lu_wave", pack + fx + fy + fz + nl + flags));
     if (!base) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: wavefront scratch allocation failed");
-    w.packF = base;
-    w.packB = base + pack;
-    w.inx = base + 2 * pack;
-    w.iny = base + 2 * pack + fx;
-    w.inz = base + 2 * pack + fx + fy;
-    w.nl = base + 2 * pack + fx + fy + fz;
-    unsigned char *f = base + 2 * pack + fx + fy + fz + nl;
+    w.pack = base;
+    w.inx = base + pack;
+    w.iny = base + pack + fx;
+    w.inz = base + pack + fx + fy;
+    w.nl = base + pack + fx + fy + fz;
+    unsigned char *f = base + pack + fx + fy + fz + nl;
     w.flags = reinterpret_cast<int *>(f);
     w.counter = w.flags + w.ntiles;
     w.err = w.flags + w.ntiles + 1;
@@ -883,8 +882,8 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     kp += sizeof a;
     std::memcpy(kp, &pack, sizeof pack);
     kp += sizeof pack;
-    std::memcpy(kp, &w.packF, sizeof w.packF);
-    kp += sizeof w.packF;
+    std::memcpy(kp, &w.pack, sizeof w.pack);
+    kp += sizeof w.pack;
     std::memcpy(kp, &deltaT, sizeof deltaT);
     kp += sizeof deltaT;
     std::memcpy(kp, &c->prec, sizeof c->prec);

@@ -138,12 +138,12 @@ struct cf_lu_args {
 };
 
 // tiled wavefront of the hyperplane sweeps (cf_wave.cuh)
-constexpr int CF_WAVE_TI = 4, CF_WAVE_TJ = 8, CF_WAVE_TK = 8, CF_WAVE_PACK = 44;
+constexpr int CF_WAVE_TI = 4, CF_WAVE_TJ = 8, CF_WAVE_TK = 8, CF_WAVE_PACK = 50;
 struct cf_wave_args {
     cf_dims d;
     int nti, ntj, ntk, ntiles;
     const int *order;        // tile ids sorted by ti + tj + tk
-    void *packF, *packB;     // [ntiles][tile cells][CF_WAVE_PACK] of the kernel's type
+    void *pack;              // [ntiles][CF_WAVE_PACK][tile cells] of the kernel's type (cf_wave.cuh)
     void *inx, *iny, *inz;   // terms arriving at a tile's x, y, z face: [ntiles][5][64 | 32 | 32]
     void *nl;                // forward N of every tile, [ntiles][5][tile cells]
     int *flags;              // per tile: 1 when done; [ntiles] = claim counter, [ntiles+1] = error word

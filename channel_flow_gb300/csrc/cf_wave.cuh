@@ -33,14 +33,22 @@
 namespace CF_NS {
 
 constexpr int WV_TI = 4, WV_TJ = 8, WV_TK = 8, WV_CELLS = WV_TI * WV_TJ * WV_TK;
-constexpr int WV_PACK = 44;          // values per cell of a tile pack
+constexpr int WV_PACK = 50;          // values per cell of a tile pack
+constexpr int WV_STAGE = 44;         // values per cell a sweep stages (forward: 6..49, backward: 0..38)
+constexpr int WV_FWD0 = 6;           // first value of the forward window
 constexpr unsigned WV_SPIN_LIMIT = 1u << 22;   // polls before a wait gives up
 
-// per-tile packs (tile-major; inside a tile value-major, value m of cell
-// c = (li*8 + lj)*8 + lk at [m][c]):
-// forward:  x, y, z split {p11 p22 p12 p13 p14 p21 p31 p41 p51 p52 p53 p54},
-//           d11 d22 d51, MR1..MR5
-// backward: x, y, z split {m11 m22 p12 ... p54}, d11 d22 d51, NL1..NL5
+// One pack per tile (tile-major; inside a tile value-major, value m of cell
+// c = (li*8 + lj)*8 + lk at [m][c]), ordered so that each sweep stages one
+// contiguous window of it:
+//   0..5    m11 m22 of the x, y, z splits            (backward only)
+//   6..35   p12 p13 p14 p21 p31 p41 p51 p52 p53 p54 of x, y, z   (both)
+//   36..38  d11 d22 d51                               (both)
+//   39..44  p11 p22 of the x, y, z splits             (forward only)
+//   45..49  MR1..MR5                                  (forward only)
+// The forward sweep stages values 6..49, the backward sweep values 0..38
+// (and the forward N of the tile, from cf_wave_args::nl), so the pack is
+// written once for both sweeps.
 // (cf_wave_args in cf_types.h holds the tiling and the scratch.)
 using wave_args = cf_wave_args;
 static_assert(WV_TI == CF_WAVE_TI && WV_TJ == CF_WAVE_TJ && WV_TK == CF_WAVE_TK && WV_PACK == CF_WAVE_PACK,
@@ -225,7 +233,7 @@ template <typename T, bool ASM>
 __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w, T dt)
 {
     extern __shared__ __align__(128) unsigned char pack_smem[];
-    T *sp = reinterpret_cast<T *>(pack_smem);     // [WV_CELLS][WV_PACK]
+    T *sp = reinterpret_cast<T *>(pack_smem);     // [WV_PACK][WV_CELLS]
     const cf_dims &d = w.d;
     const int tile = blockIdx.x;
     int ta, tb, tc;
@@ -246,42 +254,32 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
 #pragma unroll
         for (int dir = 0; dir < 3; dir++) A[dir] = wave_split<T>(d, a, q, s, dir);
         g = lu_diag<T>(d, a, q, s, dt);
-        // forward pack
 #pragma unroll
         for (int dir = 0; dir < 3; dir++) {
             wave_split12<T, false>(A[dir], v);
             wave_scale<T>(v, den[dir]);
+            P[(39 + 2 * dir) * WV_CELLS] = v[0];       // p11
+            P[(40 + 2 * dir) * WV_CELLS] = v[1];       // p22
 #pragma unroll
-            for (int m = 0; m < 12; m++) P[(12 * dir + m) * WV_CELLS] = v[m];
+            for (int m = 2; m < 12; m++) P[(6 + 10 * dir + m - 2) * WV_CELLS] = v[m];
+            wave_split12<T, true>(A[dir], v);
+            wave_scale<T>(v, den[dir]);
+            P[(2 * dir) * WV_CELLS] = v[0];            // m11
+            P[(2 * dir + 1) * WV_CELLS] = v[1];        // m22
         }
         P[36 * WV_CELLS] = g.d11; P[37 * WV_CELLS] = g.d22; P[38 * WV_CELLS] = g.d51;
-#pragma unroll
         T MR[5];
         if (ASM) lu_mr<T>(d, a, i, j, k, q, dt, s, MR);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             if (ASM) rhs_put<T>(a.MR[n], q, MR[n], a.f32_lu);
             else MR[n] = rhs_get<T>(a.MR[n], q, a.f32_lu);
-            P[(39 + n) * WV_CELLS] = MR[n];
+            P[(45 + n) * WV_CELLS] = MR[n];
         }
     }
     const unsigned bytes = (unsigned)(WV_CELLS * WV_PACK * sizeof(T));
     __syncthreads();
-    if (c == 0) wave_bulk_store(static_cast<T *>(w.packF) + (size_t)tile * WV_CELLS * WV_PACK, sp, bytes);
-    __syncthreads();
-    if (in) {
-        // backward pack
-#pragma unroll
-        for (int dir = 0; dir < 3; dir++) {
-            wave_split12<T, true>(A[dir], v);
-            wave_scale<T>(v, den[dir]);
-#pragma unroll
-            for (int m = 0; m < 12; m++) P[(12 * dir + m) * WV_CELLS] = v[m];
-        }
-        P[36 * WV_CELLS] = g.d11; P[37 * WV_CELLS] = g.d22; P[38 * WV_CELLS] = g.d51;
-    }
-    __syncthreads();
-    if (c == 0) wave_bulk_store(static_cast<T *>(w.packB) + (size_t)tile * WV_CELLS * WV_PACK, sp, bytes);
+    if (c == 0) wave_bulk_store(static_cast<T *>(w.pack) + (size_t)tile * WV_CELLS * WV_PACK, sp, bytes);
     if (in) {
         if (i == 3) wave_ghost_term<T, false>(d, a, q - d.plane(), 0, den[0], wave_face<T>(w, 0, tile), WV_FX,
                                               lj * WV_TK + lk);
@@ -315,7 +313,7 @@ constexpr int WV_WARPS = 4;                  // x terms, y terms, z terms, N
 constexpr int WV_STEPS = WV_TI + WV_TJ + WV_TK - 2;
 
 // shared memory of k_lu_wave, in elements of T
-constexpr int WV_SM_PACK = WV_CELLS * WV_PACK;
+constexpr int WV_SM_PACK = WV_CELLS * WV_STAGE;
 constexpr int WV_SM_IN = 15 * WV_CELLS;             // [3][5][cells] incoming terms
 constexpr int WV_SM_N = 5 * WV_CELLS;               // [5][cells] this sweep's N
 constexpr int WV_SM_NL = 5 * WV_CELLS;              // [5][cells] forward N (backward sweep input)
@@ -342,14 +340,16 @@ __device__ __forceinline__ void wave_steps(int L, bool full, int ti, int tj, int
             for (int n = 0; n < 5; n++)
                 S[n] = (sin[(0 * 5 + n) * WV_CELLS + c] + sin[(1 * 5 + n) * WV_CELLS + c]) +
                        sin[(2 * 5 + n) * WV_CELLS + c];
-            const T d11 = P[36 * WV_CELLS], d22 = P[37 * WV_CELLS], d51 = P[38 * WV_CELLS];
+            // staged window: forward values 6..49 at 0..43, backward 0..38
+            constexpr int wo = FWD ? WV_FWD0 : 0;
+            const T d11 = P[(36 - wo) * WV_CELLS], d22 = P[(37 - wo) * WV_CELLS], d51 = P[(38 - wo) * WV_CELLS];
             if (FWD) {
-                const T r0 = P[39 * WV_CELLS] - S[0];
+                const T r0 = P[(45 - wo) * WV_CELLS] - S[0];
                 N[0] = d11 * r0;
-                N[1] = d22 * (P[40 * WV_CELLS] - S[1]);
-                N[2] = d22 * (P[41 * WV_CELLS] - S[2]);
-                N[3] = d22 * (P[42 * WV_CELLS] - S[3]);
-                N[4] = d51 * r0 + d22 * (P[43 * WV_CELLS] - S[4]);
+                N[1] = d22 * (P[(46 - wo) * WV_CELLS] - S[1]);
+                N[2] = d22 * (P[(47 - wo) * WV_CELLS] - S[2]);
+                N[3] = d22 * (P[(48 - wo) * WV_CELLS] - S[3]);
+                N[4] = d51 * r0 + d22 * (P[(49 - wo) * WV_CELLS] - S[4]);
             } else {
                 N[0] = snl[0 * WV_CELLS + c] - d11 * S[0];
                 N[1] = snl[1 * WV_CELLS + c] - d22 * S[1];
@@ -362,9 +362,13 @@ __device__ __forceinline__ void wave_steps(int L, bool full, int ti, int tj, int
                 for (int n = 0; n < 5; n++) sN[n * WV_CELLS + c] = N[n];
             } else {
                 // the terms owed to the next cell along direction W
+                // this direction's split: p11 p22 (forward) or m11 m22
+                // (backward), then p12 .. p54
                 T o[5], cw[12];
+                cw[0] = P[((FWD ? 39 : 0) + 2 * W - wo) * WV_CELLS];
+                cw[1] = P[((FWD ? 40 : 1) + 2 * W - wo) * WV_CELLS];
 #pragma unroll
-                for (int m = 0; m < 12; m++) cw[m] = P[(12 * W + m) * WV_CELLS];
+                for (int m = 2; m < 12; m++) cw[m] = P[(6 + 10 * W + m - 2 - wo) * WV_CELLS];
                 if (FWD) wave_lower_terms<T>(cw, N, dw, o);
                 else wave_upper_terms<T>(cw, N, dw, o);
                 constexpr int cstep = W == 0 ? WV_TJ * WV_TK : W == 1 ? WV_TK : 1;
@@ -425,9 +429,10 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
     __syncthreads();
     unsigned phase = 0;
     const lu_den<T> dw(T(warp == 0 ? d.dXI : warp == 1 ? d.dET : d.dZT));   // this warp's direction
-    const unsigned pbytes = (unsigned)(WV_SM_PACK * sizeof(T));
+    // the sweep's window of each tile pack: forward values 6..49, backward 0..38
+    const unsigned pbytes = (unsigned)((FWD ? WV_STAGE : 39) * WV_CELLS * sizeof(T));
     const unsigned nbytes = (unsigned)(WV_SM_NL * sizeof(T));
-    const void *packsrc = FWD ? w.packF : w.packB;
+    const T *packsrc = static_cast<const T *>(w.pack) + (FWD ? WV_FWD0 * WV_CELLS : 0);
     while (slot < w.ntiles) {
         const int tile = w.order[FWD ? slot : w.ntiles - 1 - slot];
         int ta, tb, tc;
@@ -441,7 +446,7 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
         // these buffers before the async-proxy writes
         if (tid == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const T *src = static_cast<const T *>(packsrc) + (size_t)tile * WV_SM_PACK;
+            const T *src = packsrc + (size_t)tile * WV_CELLS * WV_PACK;
             const unsigned total = FWD ? pbytes : pbytes + nbytes;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(total) : "memory");
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
