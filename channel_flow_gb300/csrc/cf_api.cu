@@ -38,6 +38,8 @@ struct cf_ctx {
     double *er_dev = nullptr;         // 5 doubles + device counter space
     double *er_host = nullptr;        // pinned
     cudaStream_t cap = nullptr;       // private stream for graph capture
+    cudaStream_t side = nullptr;      // cf_step: Flux_Y/Z beside the viscous terms
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int lu_schedule = CF_LU_WAVEFRONT;                // hyperplane sweep schedule
     int *tile_order = nullptr;        // wavefront tiles sorted by plane (device)
     long long *trace = nullptr;       // wavefront trace: [2 sweeps][tiles][4] stamps, when enabled
@@ -227,6 +229,9 @@ void cf_destroy(cf_ctx *c)
     if (c->tile_order) cudaFree(c->tile_order);
     if (c->trace) cudaFree(c->trace);
     if (c->cap) cudaStreamDestroy(c->cap);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     for (auto &m : c->met32) cudaFree(m.second);
     delete c;
 }
@@ -1230,6 +1235,14 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
     // fixed metric arrays: their FP32 copies are made once and kept
     const bool static_m = f32_rhs && pp->static_metrics != 0;
     c->er_hist.clear();
+    if (!c->side) {
+        if (int rc = cuda_check(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "cf_step stream"))
+            return rc;
+        if (int rc = cuda_check(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cf_step event"))
+            return rc;
+        if (int rc = cuda_check(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "cf_step event"))
+            return rc;
+    }
     if (f32_rhs) {
         // U - Uq is fixed over the step: its FP32 value once, for the BDF2 term
         float *dq = reinterpret_cast<float *>(scratch(c, "step_duq", 3));
@@ -1249,6 +1262,11 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         if (pp->filter)
             if (int rc = cf_Filter(c, 0, pp->roe_criterion, pp->e_high, pp->e_low, U_[0], U_[1], U_[2], U_[3],
                                    U_[4], f->Y_point, f->Ep[0], f->Ep[1], f->Ep[2], f->J)) return rc;
+        // Flux_X on the stream (in FP32 it makes the copies of U and J the
+        // others read), then Flux_Y and Flux_Z on a side stream while the
+        // viscous terms run: independent kernels that are each bound by
+        // latency fill the GPU together
+        const cudaStream_t main = c->stream;
         for (int dir = 0; dir < 3; dir++) {
             double *p32[32] = {nullptr};
             for (int n = 0; n < 5; n++) {
@@ -1261,11 +1279,22 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
             p32[31] = f->Ep[dir];
             static const char *names[2][3] = {{"Flux_X", "Flux_Y", "Flux_Z"},
                                               {"Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter"}};
-            if (int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32, dir > 0,
-                                     f32_rhs, static_m))
+            if (dir == 1) {
+                if (int rc = cuda_check(c, cudaEventRecord(c->ev_fork, main), "cf_step")) return rc;
+                if (int rc = cuda_check(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0), "cf_step")) return rc;
+                c->stream = c->side;
+            }
+            const int rc = flux_common(c, names[pp->limiter ? 1 : 0][dir], dir, pp->limiter != 0, p32, dir > 0,
+                                       f32_rhs, static_m);
+            if (rc) {
+                c->stream = main;
                 return rc;
+            }
         }
+        c->stream = main;
+        if (int rc = cuda_check(c, cudaEventRecord(c->ev_join, c->side), "cf_step")) return rc;
         if (int rc = viscous_common(c, visc, f32_rhs, static_m)) return rc;
+        if (int rc = cuda_check(c, cudaStreamWaitEvent(main, c->ev_join, 0), "cf_step")) return rc;
         if (int rc = dts_common(c, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr, nullptr, dts,
                                 f32_rhs, static_m, f32_rhs)) return rc;
         for (int n = 0; n < 5; n++) {
