@@ -676,50 +676,56 @@ __device__ __forceinline__ void lu_update_cell_f32(const cf_dims &d, const cf_lu
     }
 }
 
-// the update over the interior box; each block also writes its partial
-// sums of Residual^2
+// the update over the interior box (blocks of 32 x 8 cells of a plane,
+// grid-stride over the planes: gridDim.z may be smaller than the box); each
+// block also writes its partial sums of Residual^2
 template <typename T>
 __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_box b)
 {
     const int k = b.k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = b.j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    const int i = b.i0 + (int)blockIdx.z;
     double r2[5] = {0, 0, 0, 0, 0};
-    if (k < b.k0 + b.nk && j < b.j0 + b.nj) {
-        const size_t q = d.ix(i, j, k);
-        if (sizeof(T) == 4) {
-            // FP32: also NL <- NR here (the arrays may hold FP32 values,
-            // which the FP64 copy kernel would pair up wrongly)
-            float nr[5];
+    if (k < b.k0 + b.nk && j < b.j0 + b.nj)
+        for (int i = b.i0 + (int)blockIdx.z; i < b.i0 + b.ni; i += (int)gridDim.z) {
+            const size_t q = d.ix(i, j, k);
+            if (sizeof(T) == 4) {
+                // FP32: also NL <- NR here (the arrays may hold FP32 values,
+                // which the FP64 copy kernel would pair up wrongly)
+                float nr[5];
 #pragma unroll
-            for (int n = 0; n < 5; n++) {
-                nr[n] = rhs_get<float>(a.NR[n], q, a.f32_lu);
-                rhs_put<float>(a.NL[n], q, nr[n], a.f32_lu);
+                for (int n = 0; n < 5; n++) {
+                    nr[n] = rhs_get<float>(a.NR[n], q, a.f32_lu);
+                    rhs_put<float>(a.NL[n], q, nr[n], a.f32_lu);
+                }
+                lu_update_cell_f32(d, a, q, nr, r2);
+            } else {
+                double nr[5];
+#pragma unroll
+                for (int n = 0; n < 5; n++) nr[n] = a.NR[n][q];
+                lu_update_cell(d, a, q, nr, r2);
             }
-            lu_update_cell_f32(d, a, q, nr, r2);
-        } else {
-            double nr[5];
-#pragma unroll
-            for (int n = 0; n < 5; n++) nr[n] = a.NR[n][q];
-            lu_update_cell(d, a, q, nr, r2);
         }
-    }
-    // block reduction in a fixed order (deterministic)
-    __shared__ double sh[5][256];
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    // block reduction in a fixed order (deterministic): each warp by
+    // shuffles, then the eight warp sums by the first warp
+    __shared__ double sh[5][8];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
-    for (int n = 0; n < 5; n++) sh[n][tid] = r2[n];
+    for (int n = 0; n < 5; n++) {
+        double v = r2[n];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) sh[n][warp] = v;
+    }
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (tid < w)
-#pragma unroll
-            for (int n = 0; n < 5; n++) sh[n][tid] += sh[n][tid + w];
-        __syncthreads();
-    }
-    if (tid == 0) {
+    if (warp == 0) {
         const size_t blk = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
 #pragma unroll
-        for (int n = 0; n < 5; n++) a.partial[5 * blk + n] = sh[n][0];
+        for (int n = 0; n < 5; n++) {
+            double v = lane < 8 ? sh[n][lane] : 0.0;
+#pragma unroll
+            for (int off = 4; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0) a.partial[5 * blk + n] = v;
+        }
     }
 }
 

@@ -267,12 +267,15 @@ cudaError_t lu_finish(const cf_dims &d, const cf_lu_args &a, double *er_dev, int
     cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
     dim3 g = box_grid(b);
 #ifdef CF_WITH_FLOAT
-    if (prec == 1) k_lu_update<float><<<g, box_block(), 0, s>>>(d, a, b);
-    else
+    if (prec == 1) {
+        // FP32: four planes per thread (fewer partial sums to reduce)
+        g.z = (unsigned)((b.ni + 3) / 4);
+        k_lu_update<float><<<g, box_block(), 0, s>>>(d, a, b);
+    } else
 #endif
         k_lu_update<double><<<g, box_block(), 0, s>>>(d, a, b);
     const double DN = 1. / (d.X_out * d.Y_out * d.Z_out);
-    k_lu_norm<<<1, 256, 0, s>>>(a.partial, lu_partial_count(d), DN, er_dev);
+    k_lu_norm<<<1, 256, 0, s>>>(a.partial, (size_t)g.x * g.y * g.z, DN, er_dev);
     return cudaGetLastError();
 }
 
