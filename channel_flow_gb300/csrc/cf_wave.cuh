@@ -332,7 +332,7 @@ __device__ __forceinline__ void wave_steps(int L, bool full, int ti, int tj, int
     for (int s = 0; s < L; s++) {
         const int l = FWD ? s : L - 1 - s;
         const int c = s_cell[l][lane];
-        const int li = c >> 6, lj = (c >> 3) & 7, lk = c & 7;
+        const int li = c / (WV_TJ * WV_TK), lj = (c / WV_TK) % WV_TJ, lk = c % WV_TK;
         if (c >= 0 && (full || (li < ti && lj < tj && lk < tk))) {
             const T *P = spack + c;                    // value m at P[m * WV_CELLS]
             T S[5], N[5];
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
         // N of the tile to HBM (read only by later launches)
         for (int v = tid; v < 5 * WV_CELLS; v += 32 * WV_WARPS) {
             const int n = v / WV_CELLS, c = v % WV_CELLS;
-            const int li = c >> 6, lj = (c >> 3) & 7, lk = c & 7;
+            const int li = c / (WV_TJ * WV_TK), lj = (c / WV_TK) % WV_TJ, lk = c % WV_TK;
             const T x = sN[v];
             if (FWD) static_cast<T *>(w.nl)[(size_t)tile * WV_SM_NL + v] = x;
             if (li < ti && lj < tj && lk < tk) {
