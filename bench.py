@@ -789,8 +789,9 @@ def secondary(ctx, g, w, calls, stream, torch, args):
             out["physical_step_to_tolerance"] = {"error": repr(exc)}
     out["note"] = ("per grid: physical step = 10 LU-SGS sub-iterations x (RHS + Dual_time_stepping), the "
                    "reference's limited scheme with the filter; FP32 = flux/viscous/filter/LU-SGS sweeps in FP32, "
-                   "state update, BDF2 time term and norms FP64.  physical_step_to_tolerance: steps run to the "
-                   "pseudo-time tolerance instead, with and without the learned initial guess")
+                   "FP64 state accumulating the FP32 changes, BDF2 differences and norms FP64.  "
+                   "physical_step_to_tolerance: steps run to the pseudo-time tolerance instead, with and without "
+                   "the learned initial guess")
     return out
 
 

@@ -42,7 +42,7 @@ extern "C" {
 /* arithmetic modes of the flux, viscous, filter and LU-SGS kernels */
 #define CF_PREC_FP64_EXACT 0 /* FP64, no fused multiply-add: equals the reference bit for bit */
 #define CF_PREC_FP64 1       /* FP64 with fused multiply-add (within 1e-12 of the reference) */
-#define CF_PREC_FP32 2       /* FP32 kernels, FP64 state update and norms */
+#define CF_PREC_FP32 2       /* FP32 kernels; the FP64 state accumulates their changes; FP64 norms */
 
 typedef struct cf_ctx cf_ctx;
 

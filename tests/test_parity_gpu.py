@@ -91,7 +91,7 @@ def test_gpu_fp64_fma_within_1e12(dims, name, port, ctx_factory):
 @pytest.mark.parametrize("name", ["Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter", "Flux_X", "Flux_Y",
                                   "Flux_Z", "Viscous_terms", "RK3NODT", "DPLUSGS", "Dual_time_stepping"])
 def test_gpu_fp32_error_bounded(name, port, ctx_factory):
-    """FP32 kernels (FP64 state update): normwise error against the FP64
+    """FP32 kernels (FP64 state, FP32 changes): normwise error against the FP64
     oracle stays at single-precision level."""
     r = routines.BY_NAME[name]
     dims = cases.GRIDS[0]
