@@ -88,6 +88,20 @@ __device__ __forceinline__ double frcp<double>(double d)
     return fma(x, e, x);
 }
 
+// float -> double on the integer pipe (the conversion instruction issues
+// to GB300's slow FP64 pipe): exact for normal values and signed zeros,
+// infinities and NaNs stay infinities and NaNs, FP32 subnormals (below
+// 1.2e-38) become signed zeros
+__device__ __forceinline__ double f2d(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u, ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
+    const unsigned exd = ex == 0xffu ? 0x7ffu : ex + 896u;      // 1023 - 127
+    const unsigned hi = ex == 0u ? sign : (sign | (exd << 20) | (man >> 3));
+    const unsigned lo = ex == 0u ? 0u : (man << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // a grid constant of cf_dims in the compute type T (its FP32 copy for float)
 #define CF_DC(T, d, x) (sizeof(T) == 4 ? (T)((d).f_##x) : (T)((d).x))
 // 1/x of a grid constant (dXI, dET, dZT, Pr): in the contracted FP64 build

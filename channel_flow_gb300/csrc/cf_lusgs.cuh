@@ -667,10 +667,12 @@ __device__ __forceinline__ void lu_update_cell_f32(const cf_dims &d, const cf_lu
     const float dE = e[0] / Km1 + 0.5f * (drho * VV + rn * (e[1] * (2.0f * uo + e[1]) + e[2] * (2.0f * vo + e[2]) +
                                                           e[3] * (2.0f * wo + e[3])));
     const float dc[5] = {drho, drho * uo + rn * e[1], drho * vo + rn * e[2], drho * wo + rn * e[3], dE};
+    // FP32 -> FP64 on the integer pipe (f2d): the FP64 pipe keeps the
+    // additions and the norm terms only
 #pragma unroll
     for (int n = 0; n < 5; n++) {
-        a.U_[n][q] = u[n] + double(dc[n] * iJ);
-        const double x = double(e[n]), r = x * x;
+        a.U_[n][q] = u[n] + f2d(dc[n] * iJ);
+        const double x = f2d(e[n]), r = x * x;
         a.Res[n][q] = r;
         acc[n] = fma(r, r, acc[n]);
     }
