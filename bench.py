@@ -551,7 +551,7 @@ def physical_steps(torch, g, precision, steps, warmup):
 
 
 def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=24, evals=3, tolerance=1e-6,
-                               max_iterations=200, epochs=80, batch=131072, online=0):
+                               max_iterations=200, epochs=200, batch=131072, online=0):
     """Wall time per physical step at equal pseudo-time tolerance: plain FP64
     (the reference's start from U^n, every kernel FP64) against the mixed
     FP32 path with the plain start, with the quadratic extrapolation and
