@@ -550,7 +550,7 @@ def physical_steps(torch, g, precision, steps, warmup):
             "subiterations": its, "ms_per_step": ms, "ms_per_subiteration": sum(ms) / max(1, sum(its))}
 
 
-def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=24, evals=3, tolerance=1e-6,
+def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=3, tolerance=1e-6,
                                max_iterations=200, epochs=200, batch=131072, online=0):
     """Wall time per physical step at equal pseudo-time tolerance: plain FP64
     (the reference's start from U^n, every kernel FP64) against the mixed
