@@ -52,6 +52,11 @@ ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_
 NCU_TRAFFIC_PER_CELL = {"Flux_X_limiter": (76.687360e6 + 11.400192e6) / (96 * 96 * 96),
                         "Flux_Y_limiter": (76.323328e6 + 11.568640e6) / (96 * 96 * 96)}
 NCU_FP64_PIPE_PCT = {"Flux_X_limiter": 87.6, "Flux_Y_limiter": 87.3}
+# floating-point operations per interior cell of the routine's algorithm:
+# the exact count of the oracle's restatement on the seeded 64x48x32 case
+# (tests/golden/flop_counts.json, made by tests/golden/make_flop_counts.py)
+ALG_FLOPS_PER_CELL = {"Flux_X_limiter": 1001.5, "Flux_Y_limiter": 998.3}
+FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (non-tensor), nominal
 LU_SUBITERATIONS = 10   # LU-SGS sub-iterations of one physical step of the fixed-count schedule
 L2_BYTES = 129 * 2 ** 20
 
@@ -389,6 +394,11 @@ def main():
             "traffic": traffic * g.cells if traffic else None,
             "traffic_source": "ncu dram bytes of one launch at 96^3 scaled by cells" if traffic else None,
             "fp64_pipe_active_pct": NCU_FP64_PIPE_PCT.get(dom),
+            "fp64": {"alg_flops_per_cell": ALG_FLOPS_PER_CELL[dom],
+                     "achieved_tflops": ALG_FLOPS_PER_CELL[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e12,
+                     "peak_tflops": FP64_NOMINAL_TFLOPS, "peak_kind": "nominal",
+                     "frac": ALG_FLOPS_PER_CELL[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e12
+                     / FP64_NOMINAL_TFLOPS},
             "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
             "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 84-88% pipe busy, "
                     "DRAM 1%); the HBM fraction is the byte-model figure"}
