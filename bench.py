@@ -401,7 +401,9 @@ def main():
                      / FP64_NOMINAL_TFLOPS},
             "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
             "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 84-88% pipe busy, "
-                    "DRAM 1%); the HBM fraction is the byte-model figure"}
+                    "DRAM 1%): fp64.frac (the oracle's exact flop count per cell over the launch time, "
+                    "against the nominal FP64 peak) is the binding roofline; the HBM fraction is the "
+                    "byte-model figure"}
 
     # secondary measurements on the same workload: FP32 kernels, and one
     # dual-time pseudo-iteration (RHS + hyperplane LU-SGS) per precision
