@@ -38,7 +38,8 @@ def _ptr(x):
 class Context:
     """One device context for one grid (the reference's one MPI rank)."""
 
-    def __init__(self, grid: Grid, precision: str = "fp64", stream=None, gamma: float = 1.5):
+    def __init__(self, grid: Grid, precision: str = "fp64", stream=None, gamma: float = 1.5,
+                 scheme: str = "reference"):
         self.lib = _lib.load()
         self.grid = grid
         g = _lib.grid_struct(grid)
@@ -53,6 +54,9 @@ class Context:
         self.set_stream(stream)
         if gamma != 1.5:
             self._ok(self.lib.cf_set_stretching(self.h, gamma))
+        self.scheme = "reference"
+        if scheme != "reference":
+            self.set_scheme(scheme)
 
     def close(self):
         if getattr(self, "h", None):
@@ -77,6 +81,14 @@ class Context:
         Dual_time_stepping are launched; both give the same results."""
         self._ok(self.lib.cf_set_lu_schedule(self.h, {"wavefront": _lib.CF_LU_WAVEFRONT,
                                                       "planes": _lib.CF_LU_PLANES}[schedule]))
+
+    def set_scheme(self, scheme: str):
+        """'reference' (default: the reference's face-state scaling of the
+        limited fluxes, bit for bit) or 'consistent' (Flux_Y_limiter's
+        near-wall rows reconstruct the conserved variables, Flux_Z_limiter's
+        weights are normalised and its left state upwind)."""
+        self._ok(self.lib.cf_set_scheme(self.h, _lib.SCHEME[scheme]))
+        self.scheme = scheme
 
     def lu_trace(self, enable: bool = True):
         """Record per-tile timer stamps of the wavefront sweeps."""
@@ -135,7 +147,9 @@ class Context:
         member names to device tensors (lists for the multi-array members,
         a list of three lists for face_metric and inF).  Returns
         (iterations, er[5], Q).  ``static_metrics``: the metric arrays stay
-        unchanged between calls (the FP32 path then converts them once)."""
+        unchanged between calls (the FP32 path then converts them once).
+        ``filter``: True (every sub-iteration), False, or "per_step" (the
+        sensor at the first sub-iteration only)."""
         f = _lib.cf_fields()
         for name, val in fields.items():
             slot = getattr(f, name)
@@ -148,7 +162,8 @@ class Context:
                         slot[i] = _ptr(v)
             else:
                 setattr(f, name, _ptr(val))
-        prm = _lib.cf_step_params(deltaT, max_iterations, tolerance, int(limiter), int(filter), roe_criterion,
+        filt = 2 if filter == "per_step" else int(bool(filter))
+        prm = _lib.cf_step_params(deltaT, max_iterations, tolerance, int(limiter), filt, roe_criterion,
                                   e_high, e_low, statistic_step, int(static_metrics))
         it = C.c_int(0)
         er = np.zeros(5)
@@ -281,9 +296,10 @@ class Context:
 
 def dplusgs_noalloc(grid: Grid, deltaT, *arrays, stream=None):
     """DPLUSGS through the allocation-free entry point (no context, scratch in
-    a fixed file-scope device array): for callers that cannot allocate
-    device memory, e.g. inside a CUDA stream capture.  Returns the residual
-    norms er1..er5."""
+    a fixed file-scope device array): for callers that may not allocate
+    device memory (a host memory manager owns the device, or the loop cannot
+    absorb an allocation's device-wide synchronisation).  The call
+    synchronises the stream.  Returns the residual norms er1..er5."""
     lib = _lib.load()
     if len(arrays) != 64:
         raise ValueError("DPLUSGS takes 64 arrays")

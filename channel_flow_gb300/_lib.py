@@ -14,6 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libcfgb300.so"
 CF_OK, CF_ERR_ARG, CF_ERR_CUDA, CF_ERR_NONFINITE, CF_ERR_NOMEM, CF_ERR_STATE, CF_ERR_TIMEOUT = range(7)
 CF_LU_WAVEFRONT, CF_LU_PLANES = 0, 1
 PREC = {"fp64_exact": 0, "fp64": 1, "fp32": 2}
+SCHEME = {"reference": 0, "consistent": 1}
 
 
 class cf_grid(C.Structure):
@@ -72,6 +73,7 @@ _SIGS = {
     "cf_set_stream": ([P, P], C.c_int),
     "cf_set_stretching": ([P, C.c_double], C.c_int),
     "cf_set_lu_schedule": ([P, C.c_int], C.c_int),
+    "cf_set_scheme": ([P, C.c_int], C.c_int),
     "cf_lu_trace": ([P, C.c_int], C.c_int),
     "cf_lu_trace_read": ([P, P, C.c_size_t], C.c_int),
     "cf_synchronize": ([P], C.c_int),

@@ -200,6 +200,7 @@ int cf_create(const cf_grid *g, int precision, cf_ctx **out)
     d.dXI = g->d_xi; d.dET = g->d_eta; d.dZT = g->d_zeta;
     d.K = g->gamma_gas; d.R = g->r_gas; d.e = g->beta_min; d.Cv = g->cv; d.mu_L = g->mu; d.Pr_L = g->prandtl;
     d.f = g->body_force; d.high = g->height;
+    d.scheme = CF_SCHEME_REFERENCE;
     cf_dims_fill_f32(d);
     c->q0 = g->bulk_flux;
     c->prec = precision;
@@ -247,6 +248,13 @@ int cf_set_stream(cf_ctx *c, void *stream)
 {
     if (!c) return CF_ERR_ARG;
     c->stream = (cudaStream_t)stream;
+    return CF_OK;
+}
+
+int cf_set_scheme(cf_ctx *c, int scheme)
+{
+    if (!c || (scheme != CF_SCHEME_REFERENCE && scheme != CF_SCHEME_CONSISTENT)) return CF_ERR_ARG;
+    c->d.scheme = scheme;
     return CF_OK;
 }
 
@@ -1243,6 +1251,23 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         if (int rc = cuda_check(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "cf_step event"))
             return rc;
     }
+    if (static_m) {
+        // every FP32 metric copy the loop reads, made here on the main
+        // stream: Flux_Y and Flux_Z run on the side stream and the viscous
+        // terms on the main one, and both read the y- and z-face copies, so
+        // a copy made by whichever comes first would be read unordered by
+        // the other
+        for (int s = 0; s < 3; s++) {
+            if (!met32_get(c, R(c, f->face_J[s])))
+                return fail(c, CF_ERR_NOMEM, "cf_step: FP32 metric copy allocation failed");
+            for (int n = 0; n < 9; n++)
+                if (!met32_get(c, R(c, f->face_metric[s][n])))
+                    return fail(c, CF_ERR_NOMEM, "cf_step: FP32 metric copy allocation failed");
+        }
+        for (int n = 0; n < 9; n++)
+            if (!met32_get(c, R(c, f->cell_metric[n])))
+                return fail(c, CF_ERR_NOMEM, "cf_step: FP32 metric copy allocation failed");
+    }
     if (f32_rhs) {
         // U - Uq is fixed over the step: its FP32 value once, for the BDF2 term
         float *dq = reinterpret_cast<float *>(scratch(c, "step_duq", 3));
@@ -1259,7 +1284,7 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         if (int rc = cf_X_periodic(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4])) return rc;
         if (int rc = cf_Y_boundary_condition(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4], f->J)) return rc;
         if (int rc = cf_Z_boundary_condition(c, 0, U_[0], U_[1], U_[2], U_[3], U_[4], f->J)) return rc;
-        if (pp->filter)
+        if (pp->filter == 1 || (pp->filter == 2 && it == 1))
             if (int rc = cf_Filter(c, 0, pp->roe_criterion, pp->e_high, pp->e_low, U_[0], U_[1], U_[2], U_[3],
                                    U_[4], f->Y_point, f->Ep[0], f->Ep[1], f->Ep[2], f->J)) return rc;
         // Flux_X on the stream (in FP32 it makes the copies of U and J the

@@ -165,6 +165,27 @@ __device__ __forceinline__ T ywall_var1_right(const SP *U, const SP *J, size_t q
     return (u * T(J[q]) - T(0.5) * rmax(T(0), m) * (ui - u));
 }
 
+// CF_SCHEME_CONSISTENT, near-wall rows: the limited 3rd-order states of the
+// conserved variables q = U_*J of cells q-s, q, q+s themselves (the
+// reference's variable-1 line with every cell value scaled by its own J),
+// variable 1 with the reference's 1e-7 ratio guard
+template <typename T, typename SP>
+__device__ __forceinline__ T ywall_q_left(const SP *U, const SP *J, size_t q, ptrdiff_t s, bool guard)
+{
+    T iu = T(U[q - s]) * T(J[q - s]), u = T(U[q]) * T(J[q]), ui = T(U[q + s]) * T(J[q + s]);
+    T rL = guard ? (ui - u) / ((u - iu) + T(0.0000001)) : (ui - u) / (u - iu);
+    T m = lim3(rL);
+    return u + T(0.5) * rmax(T(0), m) * (u - iu);
+}
+template <typename T, typename SP>
+__device__ __forceinline__ T ywall_q_right(const SP *U, const SP *J, size_t q, ptrdiff_t s, bool guard)
+{
+    T iu = T(U[q - s]) * T(J[q - s]), u = T(U[q]) * T(J[q]), ui = T(U[q + s]) * T(J[q + s]);
+    T rR = guard ? (u - iu) / ((ui - u) + T(0.0000001)) : (u - iu) / (ui - u);
+    T m = lim3(rR);
+    return u - T(0.5) * rmax(T(0), m) * (ui - u);
+}
+
 template <typename T, typename A>
 __device__ __forceinline__ void states_y_limited(const cf_dims &d, const A &a, int i, int j,
                                                  int k, T *mL, T *mR)
@@ -178,6 +199,9 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const A &a, i
         T temp = T(1.) / (T(1) / T(a.J[qL]) + T(1) / T(a.J[qL + s]));
 #pragma unroll
         for (int n = 0; n < 5; n++) mL[n] = temp * (T(a.U[n][qL]) + T(a.U[n][qL + s]));
+    } else if ((j <= 2 || j >= ny - 1) && d.scheme) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mL[n] = ywall_q_left<T>(a.U[n], a.J, qL, s, n == 0);
     } else if (j <= 2 || j >= ny - 1) {
         mL[0] = ywall_var1_left<T>(a.U[0], a.J, qL, s);
 #pragma unroll
@@ -197,6 +221,9 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const A &a, i
         T temp = T(1.) / (T(1) / T(a.J[q]) + T(1) / T(a.J[q + s]));
 #pragma unroll
         for (int n = 0; n < 5; n++) mR[n] = temp * (T(a.U[n][q]) + T(a.U[n][q + s]));
+    } else if ((jc <= 2 || jc >= ny - 1) && d.scheme) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mR[n] = ywall_q_right<T>(a.U[n], a.J, qR, s, n == 0);
     } else if (jc <= 2 || jc >= ny - 1) {
         mR[0] = ywall_var1_right<T>(a.U[0], a.J, qR, s);
 #pragma unroll
@@ -215,25 +242,27 @@ __device__ __forceinline__ void states_y_limited(const cf_dims &d, const A &a, i
 // (average, linear 3rd order); interior cells k = 3..nz-1 the limited states
 // scaled by 1/sum(w/J) with the reference's unnormalised weights, and the
 // 3rd-order branch where k >= ny (the reference compares with the y extent).
+// CF_SCHEME_CONSISTENT: numerators 60 and 6 (the weights' sums) and the
+// upwind left slope.
 template <typename T, typename SP>
-__device__ __forceinline__ T zjL5(const SP *J, size_t q)
+__device__ __forceinline__ T zjL5(const SP *J, size_t q, int scheme = 0)
 {
-    return T(1.) / (T(2) / T(J[q - 2]) - T(13) / T(J[q - 1]) + T(47) / T(J[q]) + T(27) / T(J[q + 1]) - T(3) / T(J[q + 2]));
+    return T(scheme ? 60. : 1.) / (T(2) / T(J[q - 2]) - T(13) / T(J[q - 1]) + T(47) / T(J[q]) + T(27) / T(J[q + 1]) - T(3) / T(J[q + 2]));
 }
 template <typename T, typename SP>
-__device__ __forceinline__ T zjR5(const SP *J, size_t q)
+__device__ __forceinline__ T zjR5(const SP *J, size_t q, int scheme = 0)
 {
-    return T(1.) / (T(-3) / T(J[q - 2]) + T(27) / T(J[q - 1]) + T(47) / T(J[q]) - T(13) / T(J[q + 1]) + T(2) / T(J[q + 2]));
+    return T(scheme ? 60. : 1.) / (T(-3) / T(J[q - 2]) + T(27) / T(J[q - 1]) + T(47) / T(J[q]) - T(13) / T(J[q + 1]) + T(2) / T(J[q + 2]));
 }
 template <typename T, typename SP>
-__device__ __forceinline__ T zjL3(const SP *J, size_t q)
+__device__ __forceinline__ T zjL3(const SP *J, size_t q, int scheme = 0)
 {
-    return T(1.) / (T(-1) / T(J[q - 1]) + T(5) / T(J[q]) + T(2) / T(J[q + 1]));
+    return T(scheme ? 6. : 1.) / (T(-1) / T(J[q - 1]) + T(5) / T(J[q]) + T(2) / T(J[q + 1]));
 }
 template <typename T, typename SP>
-__device__ __forceinline__ T zjR3(const SP *J, size_t q)
+__device__ __forceinline__ T zjR3(const SP *J, size_t q, int scheme = 0)
 {
-    return T(1.) / (T(2) / T(J[q - 1]) + T(5) / T(J[q]) - T(1) / T(J[q + 1]));
+    return T(scheme ? 6. : 1.) / (T(2) / T(J[q - 1]) + T(5) / T(J[q]) - T(1) / T(J[q + 1]));
 }
 
 template <typename T, typename A>
@@ -253,13 +282,15 @@ __device__ __forceinline__ void states_z_limited(const cf_dims &d, const A &a, i
         T jl = T(a.wz[0][qL]);
 #pragma unroll
         for (int n = 0; n < 5; n++)
-            mL[n] = left3<T, -1>(T(a.U[n][qL - 1]), T(a.U[n][qL]), T(a.U[n][qL + 1])) * jl;
+            mL[n] = (d.scheme ? left3<T, 1>(T(a.U[n][qL - 1]), T(a.U[n][qL]), T(a.U[n][qL + 1]))
+                              : left3<T, -1>(T(a.U[n][qL - 1]), T(a.U[n][qL]), T(a.U[n][qL + 1]))) * jl;
     } else {
         T jl = T(a.wz[0][qL]);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             const auto *U = a.U[n];
-            mL[n] = left5<T, -1>(T(U[qL - 2]), T(U[qL - 1]), T(U[qL]), T(U[qL + 1]), T(U[qL + 2])) * jl;
+            mL[n] = (d.scheme ? left5<T, 1>(T(U[qL - 2]), T(U[qL - 1]), T(U[qL]), T(U[qL + 1]), T(U[qL + 2]))
+                              : left5<T, -1>(T(U[qL - 2]), T(U[qL - 1]), T(U[qL]), T(U[qL + 1]), T(U[qL + 2]))) * jl;
         }
     }
     // right state of face k from cell k+1
@@ -646,8 +677,8 @@ __global__ void __launch_bounds__(256) k_flux_zweights(cf_dims d, const double *
     wl[q] = 1.0 / J[q];
 #else
     const bool o3 = k >= d.ny;
-    wl[q] = o3 ? zjL3<double>(J, q) : zjL5<double>(J, q);
-    wr[q] = o3 ? zjR3<double>(J, q) : zjR5<double>(J, q);
+    wl[q] = o3 ? zjL3<double>(J, q, d.scheme) : zjL5<double>(J, q, d.scheme);
+    wr[q] = o3 ? zjR3<double>(J, q, d.scheme) : zjR5<double>(J, q, d.scheme);
 #endif
 }
 

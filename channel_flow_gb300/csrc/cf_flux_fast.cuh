@@ -55,8 +55,11 @@ __device__ __forceinline__ T ginv(T D)
 
 // u[0..5] = cells c-2 .. c+3 of the face's stencil line; left state of cell
 // c (3rd or 5th order, slope sign S) and right state of cell c+1
+// (S = 0: the sign of the left slope term is that of hs = +-0.5, chosen at
+// run time)
 template <typename T, int S>
-__device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, T jR, T &mL, T &mR)
+__device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, T jR, T &mL, T &mR,
+                                          T hs = T(0.5))
 {
     const T D1 = u[2] - u[1], D2 = u[3] - u[2], D3 = u[4] - u[3];
     const T inv1 = ginv(D1), inv2 = ginv(D2), inv3 = ginv(D3);
@@ -69,7 +72,7 @@ __device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, 
         bL = T(1.) / T(30) * (T(-2) * (u[1] - u[0]) * inv1 + T(11) + T(24) * rL - T(3) * rL * rLi);
     }
     const T phiL = lmax(T(0), lmin(T(2), lmin(T(2) * rL, bL)));
-    mL = (S > 0 ? u[2] + T(0.5) * phiL * D1 : u[2] - T(0.5) * phiL * D1) * jL;
+    mL = (S > 0 ? u[2] + T(0.5) * phiL * D1 : S < 0 ? u[2] - T(0.5) * phiL * D1 : u[2] + hs * phiL * D1) * jL;
     const T rR = D2 * inv3;
     T bR;
     if (hi3) {
@@ -84,7 +87,7 @@ __device__ __forceinline__ void fast_pair(const T *u, bool lo3, bool hi3, T jL, 
 
 // left state alone: u[0..4] = cells c-2 .. c+2 (u[0] unused at 3rd order)
 template <typename T, int S>
-__device__ __forceinline__ T fast_left(const T *u, bool o3)
+__device__ __forceinline__ T fast_left(const T *u, bool o3, T hs = T(0.5))
 {
     const T D1 = u[2] - u[1], D2 = u[3] - u[2];
     const T inv1 = ginv(D1);
@@ -97,7 +100,7 @@ __device__ __forceinline__ T fast_left(const T *u, bool o3)
         b = T(1.) / T(30) * (T(-2) * (u[1] - u[0]) * inv1 + T(11) + T(24) * rL - T(3) * rL * rLi);
     }
     const T phi = lmax(T(0), lmin(T(2), lmin(T(2) * rL, b)));
-    return S > 0 ? u[2] + T(0.5) * phi * D1 : u[2] - T(0.5) * phi * D1;
+    return S > 0 ? u[2] + T(0.5) * phi * D1 : S < 0 ? u[2] - T(0.5) * phi * D1 : u[2] + hs * phi * D1;
 }
 
 // right state alone: w[0..4] = cells c-2 .. c+2 of the right cell c
@@ -180,6 +183,9 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A 
         T temp = frcp<T>(frcp<T>(T(a.J[qL])) + frcp<T>(T(a.J[qL + s])));
 #pragma unroll
         for (int n = 0; n < 5; n++) mL[n] = temp * (T(a.U[n][qL]) + T(a.U[n][qL + s]));
+    } else if (wallL && d.scheme) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mL[n] = ywall_q_left<T>(a.U[n], a.J, qL, s, n == 0);
     } else if (wallL) {
         mL[0] = ywall_var1_left<T>(a.U[0], a.J, qL, s);
 #pragma unroll
@@ -202,6 +208,9 @@ __device__ __forceinline__ void fast_states_y_limited(const cf_dims &d, const A 
         T temp = frcp<T>(frcp<T>(T(a.J[q])) + frcp<T>(T(a.J[q + s])));
 #pragma unroll
         for (int n = 0; n < 5; n++) mR[n] = temp * (T(a.U[n][q]) + T(a.U[n][q + s]));
+    } else if (wallR && d.scheme) {
+#pragma unroll
+        for (int n = 0; n < 5; n++) mR[n] = ywall_q_right<T>(a.U[n], a.J, qR, s, n == 0);
     } else if (wallR) {
         mR[0] = ywall_var1_right<T>(a.U[0], a.J, qR, s);
 #pragma unroll
@@ -233,6 +242,9 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
     const bool limR = INTERIOR || (k + 1 >= 3 && k + 1 <= nz - 1);  // cell k+1 takes a limited state
     const bool lo3 = k >= ny, hi3 = k + 1 >= ny;      // the reference compares with the y extent
     const auto *iJp = a.wz[0];      // 1/J per cell
+    // CF_SCHEME_CONSISTENT: normalised weights (the sums 60 and 6) and the
+    // upwind left slope; the reference's: unnormalised, downwind
+    const T w5 = T(d.scheme ? 60 : 1), w3 = T(d.scheme ? 6 : 1), hs = T(d.scheme ? 0.5 : -0.5);
     if (limL && limR) {
         T iJ[6];
         iJ[0] = lo3 ? T(0) : T(iJp[qL - 2]);
@@ -242,14 +254,16 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
         iJ[4] = T(iJp[qL + 2]);
         iJ[5] = hi3 ? T(0) : T(iJp[qL + 3]);
         const T jl = frcp<T>(lo3 ? (T(-1) * iJ[1] + T(5) * iJ[2] + T(2) * iJ[3])
-                                 : (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4]));
+                                 : (T(2) * iJ[0] - T(13) * iJ[1] + T(47) * iJ[2] + T(27) * iJ[3] - T(3) * iJ[4])) *
+                     (lo3 ? w3 : w5);
         const T jr = frcp<T>(hi3 ? (T(2) * iJ[2] + T(5) * iJ[3] - T(1) * iJ[4])
-                                 : (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5]));
+                                 : (T(-3) * iJ[1] + T(27) * iJ[2] + T(47) * iJ[3] - T(13) * iJ[4] + T(2) * iJ[5])) *
+                     (hi3 ? w3 : w5);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T u[6];
             load6<T>(a.U[n], qL, 1, lo3, hi3, u);
-            fast_pair<T, -1>(u, lo3, hi3, jl, jr, mL[n], mR[n]);
+            fast_pair<T, 0>(u, lo3, hi3, jl, jr, mL[n], mR[n], hs);
         }
         return;
     }
@@ -263,12 +277,12 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
     } else {
         const T jl = frcp<T>(lo3 ? (T(-1) * T(iJp[qL - 1]) + T(5) * T(iJp[qL]) + T(2) * T(iJp[qL + 1]))
                                  : (T(2) * T(iJp[qL - 2]) - T(13) * T(iJp[qL - 1]) + T(47) * T(iJp[qL]) +
-                                    T(27) * T(iJp[qL + 1]) - T(3) * T(iJp[qL + 2])));
+                                    T(27) * T(iJp[qL + 1]) - T(3) * T(iJp[qL + 2]))) * (lo3 ? w3 : w5);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T u[5];
             load5<T>(a.U[n], qL, 1, u);
-            mL[n] = fast_left<T, -1>(u, lo3) * jl;
+            mL[n] = fast_left<T, 0>(u, lo3, hs) * jl;
         }
     }
     // right state of face k from cell k+1
@@ -281,7 +295,7 @@ __device__ __forceinline__ void fast_states_z_limited(const cf_dims &d, const A 
     } else {
         const T jr = frcp<T>(hi3 ? (T(2) * T(iJp[qR - 1]) + T(5) * T(iJp[qR]) - T(1) * T(iJp[qR + 1]))
                                  : (T(-3) * T(iJp[qR - 2]) + T(27) * T(iJp[qR - 1]) + T(47) * T(iJp[qR]) -
-                                    T(13) * T(iJp[qR + 1]) + T(2) * T(iJp[qR + 2])));
+                                    T(13) * T(iJp[qR + 1]) + T(2) * T(iJp[qR + 2]))) * (hi3 ? w3 : w5);
 #pragma unroll
         for (int n = 0; n < 5; n++) {
             T w[5];

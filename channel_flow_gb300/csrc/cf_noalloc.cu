@@ -1,21 +1,21 @@
 // Allocation-free entry point: the data-parallel LU-SGS (DPLUSGS) without a
 // context.
 //
-// Who needs it: a host solver that drives the pseudo-time iterations from a
-// place where device allocation is not allowed or not affordable - inside a
-// CUDA stream capture (cudaMalloc is illegal under global capture mode), in
-// a latency-bound loop where cudaMalloc/cudaFree would synchronise the whole
-// device, or under a memory manager that owns every device byte and forbids
-// a library from taking more.  Such a caller passes all inputs and outputs;
-// this file keeps the only scratch the routine needs (per-block partial sums
-// of the residual norms and the five norms themselves) in file-scope device
+// Who needs it: a host solver that drives the pseudo-time iterations but may
+// not allocate device memory itself - because a memory manager of the host
+// application owns every device byte (it reserves the HBM for the large
+// grids up front and forbids a library from taking more), or because its
+// loop cannot absorb the device-wide synchronisation that cudaMalloc and
+// cudaFree imply.  Such a caller passes all inputs and outputs; this file
+// keeps the only scratch the routine needs (per-block partial sums of the
+// residual norms and the five norms themselves) in file-scope device
 // arrays of fixed size, which every GPU that loads the library holds until
 // the process exits.
 //
 // Limits and rules:
 // * at most CF_NOALLOC_MAX_BLOCKS reduction blocks, i.e. ceil(Z_out/32) *
 //   ceil(Y_out/8) * X_out <= 262144 (a 512 x 256 x 384 grid needs 196608);
-//   larger grids are rejected with CF_ERR_ARG;
+//   larger grids are rejected with CF_ERR_ARG before anything is launched;
 // * the scratch is shared by every call on a device and keeps the last
 //   call's contents; every value the routine reads from it is written
 //   earlier in the same call, so nothing needs clearing, but calls that
@@ -23,7 +23,9 @@
 //   race on it and must not be issued;
 // * the device address of the scratch is looked up once per device, on the
 //   first call made with that device current; make that first call before
-//   any stream capture begins.
+//   any stream capture begins;
+// * the call ends by copying the five norms to the caller's host doubles and
+//   synchronising the stream.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -75,13 +77,15 @@ extern "C" int cf_DPLUSGS_noalloc(const cf_grid *g, void *stream, double deltaT,
     if (g->cells_x < 6 || g->cells_y < 6 || g->cells_z < 6) return CF_ERR_ARG;
     for (int i = 0; i < 64; i++)
         if (!p[i]) return CF_ERR_ARG;
-    cf_dims d;
+    cf_dims d{};
     d.X_out = g->cells_x; d.Y_out = g->cells_y; d.Z_out = g->cells_z;
     d.Ym = g->cells_y + 4; d.Zm = g->cells_z + 4;
     d.gend = g->cells_x + 2; d.ny = g->cells_y + 1; d.nz = g->cells_z + 1;
     d.dXI = g->d_xi; d.dET = g->d_eta; d.dZT = g->d_zeta;
     d.K = g->gamma_gas; d.R = g->r_gas; d.e = g->beta_min; d.Cv = g->cv; d.mu_L = g->mu; d.Pr_L = g->prandtl;
     d.f = g->body_force; d.high = g->height;
+    d.scheme = CF_SCHEME_REFERENCE;
+    cf_dims_fill_f32(d);
 
     const cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
     const dim3 grid = box_grid(b), block = box_block();

@@ -24,6 +24,12 @@ struct cf_dims {
     float f_dXI, f_dET, f_dZT, f_K, f_R, f_e, f_Cv, f_mu_L, f_Pr_L, f_f, f_high;
     double ikm1;              // 1 / (K - 1), for the contracted build's state update
     double idXI, idET, idZT, iPr;   // 1/dXI, 1/dET, 1/dZT, 1/Pr_L (correctly rounded, host)
+    // face-state scaling of the limited fluxes: 0 = the reference's
+    // (CF_SCHEME_REFERENCE), 1 = consistently scaled (CF_SCHEME_CONSISTENT:
+    // Flux_Y_limiter's near-wall rows reconstruct the conserved variables
+    // themselves, Flux_Z_limiter's weights are normalised and its left
+    // state takes the upwind slope as in x and y)
+    int scheme;
 
     __host__ __device__ __forceinline__ size_t ix(int i, int j, int k) const
     {

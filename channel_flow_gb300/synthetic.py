@@ -155,12 +155,16 @@ def y_points(g: Grid, gamma: float = 2.8):
 
 
 def channel_state(g: Grid, J, seed: int = 0, mach: float = 0.5, noise: float = 0.05,
-                  jitter: float = 0.01, rho_b: float = RHO_REF, gamma: float = 1.5):
+                  jitter: float = 0.01, rho_b: float = RHO_REF, gamma: float = 1.5,
+                  wall_damped: bool = False):
     """Seeded channel state U/J = (rho, rho u, rho v, rho w, E)/J on every
     cell of the array: laminar parabola u = 1.5 U_b (1 - eta^2) plus uniform
     +-noise*U_b on u, v, w, and +-jitter relative noise on rho and T (the
     unguarded limiter ratios need distinct neighbours, so exact ties are
-    avoided).  U_b = mach * sqrt(K R T_wall)."""
+    avoided).  U_b = mach * sqrt(K R T_wall).  ``wall_damped``: the
+    velocity noise is scaled by the parabola's shape 1 - eta^2, so it
+    vanishes at the no-slip walls (the noise keeps its +-noise*U_b
+    amplitude on the centre line)."""
     rng = np.random.default_rng(seed)
     X, Y, Z = g.shape
     ub = mach * math.sqrt(g.K * g.R * T_WALL)
@@ -169,11 +173,12 @@ def channel_state(g: Grid, J, seed: int = 0, mach: float = 0.5, noise: float = 0
     # position in the stretched coordinate mapped back to [-1, 1]
     yy = 1 - 1.0 / math.tanh(gamma) * np.tanh(gamma * eta)            # 0 .. 2
     prof = 1.5 * ub * (1 - (yy - 1) ** 2)
+    amp = noise * ub * ((1 - (yy - 1) ** 2)[None, :, None] if wall_damped else 1.0)
     rho = rho_b * (1 + jitter * rng.uniform(-1, 1, g.shape))
     T = T_WALL * (1 + jitter * rng.uniform(-1, 1, g.shape))
-    u = prof[None, :, None] + noise * ub * rng.uniform(-1, 1, g.shape)
-    v = noise * ub * rng.uniform(-1, 1, g.shape)
-    w = noise * ub * rng.uniform(-1, 1, g.shape)
+    u = prof[None, :, None] + amp * rng.uniform(-1, 1, g.shape)
+    v = amp * rng.uniform(-1, 1, g.shape)
+    w = amp * rng.uniform(-1, 1, g.shape)
     p = rho * g.R * T
     E = p / (g.K - 1) + 0.5 * rho * (u * u + v * v + w * w)
     return [np.ascontiguousarray(x / J) for x in (rho, rho * u, rho * v, rho * w, E)]
@@ -181,3 +186,23 @@ def channel_state(g: Grid, J, seed: int = 0, mach: float = 0.5, noise: float = 0
 
 def bulk_velocity(g: Grid, mach: float = 0.5):
     return mach * math.sqrt(g.K * g.R * T_WALL)
+
+
+def channel_physics(g: Grid, mach: float, re_bulk: float, rho_b: float = RHO_REF) -> Grid:
+    """The grid with the viscosity and body force of a channel at bulk Mach
+    number ``mach`` and bulk Reynolds number ``re_bulk`` = rho_b U_b (2h) / mu
+    (length: the full channel height 2h = ``high``), U_b = mach *
+    sqrt(K R T_wall): mu = rho_b U_b 2h / Re_b; the body force f = 3 mu U_b /
+    h^2 holds the laminar parabola in balance with the wall shear (the
+    reference keeps f constant, prm.h:14); Q0 = rho_b U_b is Driven_force's
+    target bulk flux.  The other constants (K, R, Cv, Pr_L, e) stay the
+    reference's."""
+    ub = bulk_velocity(g, mach)
+    h = 0.5 * g.high
+    mu = rho_b * ub * g.high / re_bulk
+    return g.with_(mu_L=mu, f=3.0 * mu * ub / (h * h), Q0=rho_b * ub)
+
+
+def time_step(g: Grid, mach: float, h_over_ub: float = 0.005) -> float:
+    """Physical time step h_over_ub * h / U_b (the configurations' 0.005 h/U_b)."""
+    return h_over_ub * 0.5 * g.high / bulk_velocity(g, mach)

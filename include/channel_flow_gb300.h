@@ -83,6 +83,25 @@ int cf_set_stretching(cf_ctx *ctx, double gamma);
 #define CF_LU_WAVEFRONT 0
 #define CF_LU_PLANES 1
 int cf_set_lu_schedule(cf_ctx *ctx, int schedule);
+/* Face-state scaling of the limited fluxes.  CF_SCHEME_REFERENCE (default)
+ * is the reference's, bit for bit in CF_PREC_FP64_EXACT.  Two of its
+ * scalings are inconsistent, and the assembled limited loop diverges on
+ * channel states at the configuration time step:
+ *   - Flux_Y_limiter's rows next to a wall (cells j <= 2, j >= ny-1) scale
+ *     the density by the cell J and leave its slope unscaled, and scale the
+ *     other four variables by jL/jR, which that branch never sets
+ *     (Flux_Y_limiter.cpp:115-232; here the face J_v);
+ *   - Flux_Z_limiter scales its limited states by 1/sum(w/J) with weights
+ *     summing to 60 (5-point) and 6 (3-point), so interior z faces carry
+ *     1/60 of the state, and its left state takes the downwind slope
+ *     (Flux_Z_limiter.cpp:131-272).
+ * CF_SCHEME_CONSISTENT reconstructs the conserved variables U_*J of the
+ * three cells with the same limiter in Flux_Y_limiter's near-wall rows,
+ * normalises the z weights (60/sum(w/J), 6/sum(w/J)) and takes the upwind
+ * left slope in z.  Every other face and routine is unchanged. */
+#define CF_SCHEME_REFERENCE 0
+#define CF_SCHEME_CONSISTENT 1
+int cf_set_scheme(cf_ctx *ctx, int scheme);
 /* Wavefront trace (profiling): when enabled, each Dual_time_stepping call
  * records per tile four device global-timer stamps in ns (claimed, inputs
  * ready, coefficients staged, done), forward sweep then backward sweep.
@@ -194,9 +213,10 @@ int cf_DPLUSGS(cf_ctx *ctx, int myid, double deltaT, double *er1, double *er2, d
 /* Allocation-free DPLUSGS: no counterpart in the reference.  Same arrays,
  * arithmetic and results as cf_DPLUSGS in CF_PREC_FP64_EXACT mode, but it
  * needs no context and calls no cudaMalloc/cudaFree, for callers that may
- * not allocate device memory (inside a CUDA stream capture, in loops where
- * an allocation's device-wide synchronisation is unaffordable, under a
- * memory manager that owns all device memory).  Its only scratch, the
+ * not allocate device memory: a host application whose memory manager owns
+ * all device memory (the HBM reserved up front for its grids), or a loop
+ * that cannot absorb the device-wide synchronisation an allocation
+ * implies.  Its only scratch, the
  * residual-norm partial sums, is a fixed 10 MB file-scope device array per
  * GPU, so grids needing more than 262144 reduction blocks
  * (ceil(cells_z/32) * ceil(cells_y/8) * cells_x) are rejected with CF_ERR_ARG.
@@ -308,7 +328,10 @@ typedef struct {
     int max_iterations;        /* pseudo-time iterations at most (iteration_end_step, main.cpp:48) */
     double tolerance;          /* er_n / max(er_n) of fields 1-4 below this ends the step (main.cpp:406) */
     int limiter;               /* 1: Flux_X/Y/Z_limiter, 0: Flux_X/Y/Z */
-    int filter;                /* 1: Filter (its Ep switches the limited fluxes' dissipation) */
+    int filter;                /* 1: Filter every sub-iteration (its Ep switches the limited fluxes'
+                                  dissipation), 2: Filter at the first sub-iteration of the step only
+                                  (the sensor then stays fixed while the sub-iterations converge),
+                                  0: no Filter (Ep as given) */
     double roe_criterion, e_high, e_low;
     int statistic_step;        /* > 0: Statistic after the step */
     int static_metrics;        /* 1: the metric arrays (J, cell and face metrics) stay unchanged between

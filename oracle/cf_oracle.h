@@ -33,6 +33,8 @@ typedef struct {
     double K, R, e;                   /* gamma, gas constant, preconditioning floor (prm.h:7-11) */
     double Cv, mu_L, Pr_L;            /* Viscous_terms.h:3-5 */
     double f, high;                   /* body force, channel height 2h (prm.h:14,19) */
+    int scheme;                       /* limited-flux face-state scaling: 0 the reference's,
+                                       * 1 consistent (cfo_Flux_Y_limiter, cfo_Flux_Z_limiter) */
 } cfo_grid;
 
 /* boundary conditions */

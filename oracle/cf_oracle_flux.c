@@ -393,7 +393,22 @@ void cfo_Flux_X_limiter(const cfo_grid *g, double **a)
  * (private, uninitialised OpenMP variables at Flux_Y_limiter.cpp:120).  Here
  * they are the face Jacobians J_v of the same face, exactly as the interior
  * branch sets them (Flux_Y_limiter.cpp:231-232).  Faces j = 1, 2, ny-2,
- * ny-1 and ny depend on this choice. */
+ * ny-1 and ny depend on this choice.
+ *
+ * g->scheme == 1 (the consistent variant, not the reference): in the
+ * near-wall branch every variable is reconstructed from the conserved values
+ * q = U_*J of cells j-1, j, j+1 (each scaled by its own J) with the same
+ * 3rd-order limiter - the reference's variable-1 line with its slope scaled
+ * like its cell value - variable 1 keeping the 1e-7 ratio guard. */
+static inline void ywall_q(double iq, double q, double qi, int guard, double *mL, double *mR)
+{
+    double rL = guard ? (qi - q) / ((q - iq) + 0.0000001) : (qi - q) / (q - iq);
+    double rR = guard ? (q - iq) / ((qi - q) + 0.0000001) : (q - iq) / (qi - q);
+    double minL3 = lim3(rL), minR3 = lim3(rR);
+    *mL = q + 0.5 * RMAX(0, minL3) * (q - iq);
+    *mR = q - 0.5 * RMAX(0, minR3) * (qi - q);
+}
+
 void cfo_Flux_Y_limiter(const cfo_grid *g, double **a)
 {
     GRID_LOCALS(g);
@@ -405,7 +420,14 @@ void cfo_Flux_Y_limiter(const cfo_grid *g, double **a)
                 const double jL = J_v[IX(i - 1, j, k - 1)];
                 const double jR = J_v[IX(i - 1, j - 1, k - 1)];
                 const size_t qL = IX(i - 1, j, k - 1), qR = IX(i - 1, j - 1, k - 1);
-                if (j <= 2 || j >= ny - 1) {
+                if ((j <= 2 || j >= ny - 1) && g->scheme) {
+                    const double Jm = J[IX(i, j - 1, k)], J0 = J[IX(i, j, k)], Jp = J[IX(i, j + 1, k)];
+                    for (int n = 0; n < 5; n++) {
+                        const double *Un = a[A_U + n];
+                        ywall_q(Un[IX(i, j - 1, k)] * Jm, Un[IX(i, j, k)] * J0, Un[IX(i, j + 1, k)] * Jp, n == 0,
+                                &a[A_ML + n][qL], &a[A_MR + n][qR]);
+                    }
+                } else if (j <= 2 || j >= ny - 1) {
                     /* variable 1: ratios guarded by +1e-7 and the cell value
                      * scaled by the cell Jacobian (Flux_Y_limiter.cpp:153-168) */
                     const double *U = a[A_U];
@@ -445,31 +467,37 @@ void cfo_Flux_Y_limiter(const cfo_grid *g, double **a)
  * the y extent kept as written), 354-520 (rows k = 1, 2, nz) and 548-712
  * (faces i = 2..gend-1, j = 1..ny-1, k = 1..nz).  The reconstructed states
  * are scaled by 1/sum(w/J) with the unnormalised 5-point (sum 60) and
- * 3-point (sum 6) weights, as the reference does. */
+ * 3-point (sum 6) weights, as the reference does.
+ *
+ * g->scheme == 1 (the consistent variant, not the reference): the weights
+ * are normalised (60/sum(w/J), 6/sum(w/J)) and the left state takes the
+ * upwind slope u + 0.5*phi*(u-iu), as in x and y. */
 void cfo_Flux_Z_limiter(const cfo_grid *g, double **a)
 {
     GRID_LOCALS(g);
     const double *J = a[A_J];
+    const double w5 = g->scheme ? 60. : 1., w3 = g->scheme ? 6. : 1.;
+    const int sL = g->scheme ? +1 : -1;
     #pragma omp parallel for collapse(2)
     for (int i = 2; i <= gend; i++)
         for (int j = 2; j <= ny; j++)
             for (int k = 3; k <= nz - 1; k++) {
                 const size_t qL = IX(i - 1, j - 1, k), qR = IX(i - 1, j - 1, k - 1);
                 if (k <= 2 || k >= ny) {
-                    double jL = 1. / (-1 / J[IX(i, j, k - 1)] + 5 / J[IX(i, j, k)] + 2 / J[IX(i, j, k + 1)]);
-                    double jR = 1. / (2 / J[IX(i, j, k - 1)] + 5 / J[IX(i, j, k)] - 1 / J[IX(i, j, k + 1)]);
+                    double jL = w3 / (-1 / J[IX(i, j, k - 1)] + 5 / J[IX(i, j, k)] + 2 / J[IX(i, j, k + 1)]);
+                    double jR = w3 / (2 / J[IX(i, j, k - 1)] + 5 / J[IX(i, j, k)] - 1 / J[IX(i, j, k + 1)]);
                     for (int n = 0; n < 5; n++) {
                         const double *U = a[A_U + n];
-                        muscl3(U[IX(i, j, k - 1)], U[IX(i, j, k)], U[IX(i, j, k + 1)], -1, jL, jR,
+                        muscl3(U[IX(i, j, k - 1)], U[IX(i, j, k)], U[IX(i, j, k + 1)], sL, jL, jR,
                                &a[A_ML + n][qL], &a[A_MR + n][qR]);
                     }
                 } else {
-                    double jL = 1. / (2 / J[IX(i, j, k - 2)] - 13 / J[IX(i, j, k - 1)] + 47 / J[IX(i, j, k)] + 27 / J[IX(i, j, k + 1)] - 3 / J[IX(i, j, k + 2)]);
-                    double jR = 1. / (-3 / J[IX(i, j, k - 2)] + 27 / J[IX(i, j, k - 1)] + 47 / J[IX(i, j, k)] - 13 / J[IX(i, j, k + 1)] + 2 / J[IX(i, j, k + 2)]);
+                    double jL = w5 / (2 / J[IX(i, j, k - 2)] - 13 / J[IX(i, j, k - 1)] + 47 / J[IX(i, j, k)] + 27 / J[IX(i, j, k + 1)] - 3 / J[IX(i, j, k + 2)]);
+                    double jR = w5 / (-3 / J[IX(i, j, k - 2)] + 27 / J[IX(i, j, k - 1)] + 47 / J[IX(i, j, k)] - 13 / J[IX(i, j, k + 1)] + 2 / J[IX(i, j, k + 2)]);
                     for (int n = 0; n < 5; n++) {
                         const double *U = a[A_U + n];
                         muscl5(U[IX(i, j, k - 2)], U[IX(i, j, k - 1)], U[IX(i, j, k)], U[IX(i, j, k + 1)],
-                               U[IX(i, j, k + 2)], -1, jL, jR, &a[A_ML + n][qL], &a[A_MR + n][qR]);
+                               U[IX(i, j, k + 2)], sL, jL, jR, &a[A_ML + n][qL], &a[A_MR + n][qR]);
                     }
                 }
             }

@@ -35,12 +35,15 @@ class cfo_grid(C.Structure):
                 ("deltaXI", C.c_double), ("deltaET", C.c_double), ("deltaZT", C.c_double),
                 ("K", C.c_double), ("R", C.c_double), ("e", C.c_double),
                 ("Cv", C.c_double), ("mu_L", C.c_double), ("Pr_L", C.c_double),
-                ("f", C.c_double), ("high", C.c_double)]
+                ("f", C.c_double), ("high", C.c_double), ("scheme", C.c_int)]
+
+# limited-flux face-state scaling (cfo_grid.scheme)
+SCHEMES = {"reference": 0, "consistent": 1}
 
 
-def grid_struct(g) -> cfo_grid:
+def grid_struct(g, scheme: str = "reference") -> cfo_grid:
     return cfo_grid(g.X_out, g.Y_out, g.Z_out, g.deltaXI, g.deltaET, g.deltaZT,
-                    g.K, g.R, g.e, g.Cv, g.mu_L, g.Pr_L, g.f, g.high)
+                    g.K, g.R, g.e, g.Cv, g.mu_L, g.Pr_L, g.f, g.high, SCHEMES[scheme])
 
 
 def build_port(force: bool = False) -> Path:
@@ -74,9 +77,9 @@ class Port:
     def __init__(self):
         self.lib = C.CDLL(str(build_port()))
 
-    def _call(self, name, g, arrays, *scalars):
+    def _call(self, name, g, arrays, *scalars, scheme="reference"):
         fn = getattr(self.lib, "cfo_" + name)
-        gs = grid_struct(g)
+        gs = grid_struct(g, scheme)
         fn(C.byref(gs), *scalars, _ptrs(arrays))
 
     def x_periodic(self, g, U):
@@ -88,8 +91,8 @@ class Port:
     def Z_boundary_condition(self, g, arrays):
         self._call("Z_boundary_condition", g, arrays)
 
-    def flux(self, name, g, arrays):
-        self._call(name, g, arrays)
+    def flux(self, name, g, arrays, scheme="reference"):
+        self._call(name, g, arrays, scheme=scheme)
 
     def Viscous_terms(self, g, arrays):
         self._call("Viscous_terms", g, arrays)

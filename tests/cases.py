@@ -239,10 +239,10 @@ def step_case(g, seed=0):
             "Residual": [z() for _ in range(5)]}
 
 
-def port_step(port, g, f, deltaT, max_iterations, tolerance, E, crit=(0.007, 1.0, 0.0)):
+def port_step(port, g, f, deltaT, max_iterations, tolerance, E, crit=(0.007, 1.0, 0.0), scheme="reference"):
     """The same physical step on the C oracle: the loop of main.cpp:143-480
-    with Filter and the limited fluxes; f is modified in place, E (running
-    maxima) too.  Returns (iterations, er, Q)."""
+    with Filter and the limited fluxes (face-state scaling ``scheme``); f is
+    modified in place, E (running maxima) too.  Returns (iterations, er, Q)."""
     from oracle.cforacle import hyperplane_buffers
     U_, J = f["U_"], f["J"]
     s10 = [np.zeros(g.shape) for _ in range(10)]
@@ -256,7 +256,8 @@ def port_step(port, g, f, deltaT, max_iterations, tolerance, E, crit=(0.007, 1.0
         port.Z_boundary_condition(g, U_ + [J])
         port.Filter(g, *crit, U_ + [f["Y_point"]] + f["Ep"] + [J])
         for d, name in enumerate(("Flux_X_limiter", "Flux_Y_limiter", "Flux_Z_limiter")):
-            port.flux(name, g, U_ + s10 + [J, f["face_J"][d]] + f["face_metric"][d] + f["inF"][d] + [f["Ep"][d]])
+            port.flux(name, g, U_ + s10 + [J, f["face_J"][d]] + f["face_metric"][d] + f["inF"][d] + [f["Ep"][d]],
+                      scheme=scheme)
         visc = U_ + f["vF"] + [J] + f["cell_metric"]
         for d in range(3):
             visc += [f["face_J"][d]] + f["face_metric"][d]
@@ -281,3 +282,30 @@ def port_step(port, g, f, deltaT, max_iterations, tolerance, E, crit=(0.007, 1.0
         f["Uq"][n][ix] = f["U"][n][ix]
         f["U"][n][ix] = f["U_"][n][ix]
     return it, np.asarray(er), Q
+
+
+def channel_step_case(g, gamma=2.0, seed=0, mach=0.5, port=None):
+    """The fields of a physical step on the benchmark channel (synthetic.py:
+    tanh-stretched flat walls, laminar parabola with wall-damped +-5 % velocity
+    noise, +-1 % rho and T jitter), as numpy arrays, U = U_ = Uq; face
+    metrics from the oracle's Jacobian_u/v/w."""
+    cm = syn.flat_metrics(g, gamma, "cell")
+    J = cm["J"]
+    U = syn.channel_state(g, J, seed=seed, mach=mach, noise=0.05, jitter=0.01, gamma=gamma, wall_damped=True)
+    if port is None:
+        from oracle.cforacle import Port
+        port = Port()
+    faces = []
+    for w in ("u", "v", "w"):
+        arrs = [np.zeros(g.shape) for _ in range(10)]
+        extra = [J] + [cm[n] for n in syn.METRIC_NAMES] if w == "v" else []
+        port.Jacobian_face(w, g, gamma, arrs + extra)
+        faces.append(arrs)
+    z = lambda: np.zeros(g.shape)
+    return {"U_": [u.copy() for u in U], "U": [u.copy() for u in U], "Uq": [u.copy() for u in U], "J": J,
+            "Y_point": syn.y_points(g, gamma=gamma), "cell_metric": [cm[n] for n in syn.METRIC_NAMES],
+            "face_J": [f[0] for f in faces], "face_metric": [f[1:] for f in faces],
+            "Ep": [z() for _ in range(3)], "inF": [[z() for _ in range(5)] for _ in range(3)],
+            "vF": [z() for _ in range(4)], "LL": [z() for _ in range(4)], "ML": [z() for _ in range(4)],
+            "MR": [z() for _ in range(5)], "NR": [z() for _ in range(5)], "NL": [z() for _ in range(5)],
+            "Residual": [z() for _ in range(5)]}

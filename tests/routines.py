@@ -51,14 +51,19 @@ BY_NAME = {r.name: r for r in ROUTINES}
 RK_STAGE = 2
 
 
-def run_cpu(impl, r: Routine, g, arrays):
+def run_cpu(impl, r: Routine, g, arrays, scheme="reference"):
     """Run routine r on the compiled reference or the C oracle (in place);
-    returns the residual norms for the dual-time routines, else None."""
+    returns the residual norms for the dual-time routines, else None.
+    ``scheme``: the oracle's face-state scaling of the limited fluxes (the
+    reference itself has only its own)."""
     n = r.name
     if n in ("Y_boundary_condition", "Z_boundary_condition", "Viscous_terms"):
         getattr(impl, n)(g, arrays)
     elif n.startswith("Flux"):
-        impl.flux(n, g, arrays)
+        if scheme == "reference":
+            impl.flux(n, g, arrays)
+        else:
+            impl.flux(n, g, arrays, scheme=scheme)
     elif n == "Filter":
         impl.Filter(g, *cases.FILTER_ARGS, arrays)
     elif n == "RK3NODT":
@@ -110,13 +115,16 @@ def run_gpu(ctx, r: Routine, arrays):
     return er
 
 
-def compare(r: Routine, g, got, want, rtol=0.0):
+def compare(r: Routine, g, got, want, rtol=0.0, masked=False):
     """Largest normwise relative difference per written array (0 = equal
-    bit for bit where rtol == 0); masked entries are skipped."""
+    bit for bit where rtol == 0).  ``masked``: skip the entries that depend
+    on the reference's undefined values (only for comparisons with the
+    reference itself; the GPU and the oracle define them alike and are
+    compared everywhere)."""
     worst = {}
     for i in r.outputs:
         a, b = got[i], want[i]
-        m = r.mask(g, i)
+        m = r.mask(g, i) if masked else None
         if m is not None:
             a = np.where(m, 0.0, a)
             b = np.where(m, 0.0, b)

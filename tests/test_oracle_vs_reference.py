@@ -23,7 +23,7 @@ def test_port_equals_reference(dims, name, port):
     want, got = cases.copy_case(a), cases.copy_case(a)
     e_ref = routines.run_cpu(ref, r, g, want)
     e_port = routines.run_cpu(port, r, g, got)
-    diff = routines.compare(r, g, got, want)
+    diff = routines.compare(r, g, got, want, masked=True)
     assert all(v == 0 for v in diff.values()), f"{name} mismatching entries per slot: {diff}"
     # everything the routine does not write stays as it was
     for i in range(len(a)):

@@ -130,3 +130,43 @@ def test_gpu_fp32_step_equals_routine_loop(static_metrics, cuda_lib):
     finally:
         ctx_a.close()
         ctx_b.close()
+
+
+def test_gpu_fp32_static_metrics_first_step_after_poisoned_memory(cuda_lib):
+    """The first FP32 step with static metrics makes the FP32 metric copies;
+    Flux_Y/Flux_Z (side stream) and the viscous terms (main stream) both
+    read the y- and z-face copies, so they must exist before the loop forks.
+    Device memory is first filled with NaN and released, so a read of a copy
+    before it is written shows as NaN.  On the 256 x 192 x 192 channel one
+    sub-iteration with the copies equals one without them to FP32 rounding,
+    and every value of the state is finite."""
+    import torch
+    import channel_flow_gb300 as cf
+    from channel_flow_gb300 import stepper, synthetic as syn
+    import bench
+
+    g = syn.channel_physics(syn.channel_grid(256, 192, 192), 0.5, 5600)
+    cm = syn.flat_metrics(g, 2.0, "cell")
+    host = {"U": syn.channel_state(g, cm["J"], seed=2800, gamma=2.0, wall_damped=True), "J": cm["J"],
+            "cm": [cm[n] for n in syn.METRIC_NAMES], "Yp": syn.y_points(g, gamma=2.0)}
+    dt = syn.time_step(g, 0.5) / 4
+    ers = {}
+    for static in (True, False):
+        x = torch.full((2 ** 30,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        del x
+        torch.cuda.empty_cache()
+        ctx = cf.Context(g, precision="fp32", gamma=2.0, scheme="consistent")
+        try:
+            w = bench.DeviceWorkload(ctx, g, host, torch)
+            f = stepper.fields_from_workload(w, torch, g)
+            ctx.step_reset()
+            ctx.step(f, step=1, deltaT=dt, max_iterations=2, tolerance=1e-9, limiter=True, filter="per_step",
+                     static_metrics=static)
+            assert all(bool(torch.isfinite(u).all()) for u in f["U_"]), static
+            ers[static] = ctx.step_residuals()
+        finally:
+            ctx.close()
+        del w, f
+        torch.cuda.empty_cache()
+    np.testing.assert_allclose(ers[True], ers[False], rtol=1e-3, atol=0)
