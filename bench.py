@@ -602,9 +602,10 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=4,
     The sub-iterations of every mode run until er_n / max er_n < 1e-6 for
     n = 1..4 (main.cpp:387-406; er_n are sums of squared primitive updates,
     Dual_time_stepping.cpp:1318-1361) or 200 iterations.  `harvest` steps of
-    the mixed path from the seeded state (the first two from U^n, the rest
-    from the extrapolation) give the training windows and the common start
-    (the last three levels and the residual maxima).  Every mode then runs
+    the mixed path from the seeded state (each from U^n: on this oscillating
+    transient the quadratic extrapolation overshoots, and a start that far
+    off can make the sub-iterations diverge) give the training windows and
+    the common start (the last three levels and the residual maxima).  Every mode then runs
     `evals` timed steps from that start with Statistic accumulating; its
     mean velocity and Reynolds-stress profiles and its final state are
     compared with those of the FP64 run.  The learned mode also runs capped
@@ -622,7 +623,7 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=4,
     harvest_its = []
     t0 = time.perf_counter()
     for n in range(harvest):
-        harvest_its.append(st.step("extrapolate" if n >= 2 else None)[0])
+        harvest_its.append(st.step(None)[0])
         hist.append([u.clone() for u in st.f["U"]])
     torch.cuda.synchronize()
     harvest_s = time.perf_counter() - t0
@@ -646,6 +647,7 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=4,
            "training": {"s": train_s, "adam_steps": len(losses), "batch_cells": batch,
                         "loss_first_last": [losses[0], losses[-1]], "held_out": net.validation},
            "online_adam_steps": online}
+    out["guess_breakdown_ms"] = guess_breakdown(torch, net, g, start, st.f["U_"])
     ref = None
     modes = (("fp64", "fp64", None, None), ("fp32", "fp32", None, None),
              ("fp32+extrapolate", "fp32", "extrapolate", None), ("fp32+learned", "fp32", net, None),
@@ -695,6 +697,43 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=4,
     ctx.close()
     tmp.cleanup()
     return out
+
+
+def guess_breakdown(torch, net, g, levels, out, reps=5):
+    """CUDA-event time of each part of one learned guess on all cells:
+    the device-side feature scales, the feature rows, the three forward
+    GEMMs and the guess itself (mean of `reps` after one untimed call),
+    and of the whole guess; with the fitted predictor coefficients."""
+    from channel_flow_gb300 import mlp
+    un, u1, u2 = levels[2], levels[1], levels[0]
+    Mpad = (g.cells + 255) // 256 * 256
+    b1, b2, b3 = net.view("b1"), net.view("b2"), net.view("b3")
+    a15 = (mlp.C.c_void_p * 15)(*[t.data_ptr() for t in list(un) + list(u1) + list(u2)])
+    o5 = (mlp.C.c_void_p * 5)(*[t.data_ptr() for t in out])
+    parts = [
+        ("scales", lambda: net.set_scale_device(g, un, u1, u2)),
+        ("features", lambda: net.load_features(g, un, u1, u2)),
+        ("gemm_L1", lambda: net.gemm(net.X, net.W1b, Mpad, mlp.H, mlp.K1, mlp.EPI_SILU, b1, net.H1, None, mlp.H)),
+        ("gemm_L2", lambda: net.gemm(net.H1, net.W2b, Mpad, mlp.H, mlp.H, mlp.EPI_SILU, b2, net.H2, None, mlp.H)),
+        ("gemm_L3", lambda: net.gemm(net.H2, net.W3b, Mpad, mlp.N3, mlp.H, mlp.EPI_BIAS, b3, net.Y, None, mlp.N3)),
+        ("apply", lambda: net._ok(net.lib.cf_mlp_apply(net._s(), g.X_out, g.Y_out, g.Z_out, a15, net.coef.ctypes.data,
+                                                       net.scale.data_ptr(), net.ogain.data_ptr(), net.Y.data_ptr(),
+                                                       o5), "cf_mlp_apply")),
+        ("guess_total", lambda: net.guess(g, un, u1, u2, out)),
+    ]
+    res = {}
+    for name, fn in parts:
+        fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = e0.elapsed_time(e1) / reps
+    res["predictor_coef_a_b"] = [round(float(x), 4) for x in net.coef]
+    return res
 
 
 def mlp_gemms(torch, rows, steps=5, warmup=2):

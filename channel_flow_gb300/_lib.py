@@ -112,8 +112,11 @@ _SIGS = {
     "cf_step_residuals": ([P, P, C.c_int, P], C.c_int),
     "cf_gemm_bf16": ([P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P], C.c_int),
     "cf_mlp_features": ([P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
-    "cf_mlp_targets": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
-    "cf_mlp_apply": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P], C.c_int),
+    "cf_mlp_targets": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
+    "cf_mlp_apply": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P], C.c_int),
+    "cf_mlp_features_grid": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_longlong, P, P], C.c_int),
+    "cf_mlp_base_sums": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),
+    "cf_mlp_scale": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),
     "cf_mlp_dot": ([P, P, P, C.c_longlong, P, C.c_int, P], C.c_int),
     "cf_mlp_rms": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),
     "cf_mlp_rms3": ([P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, P], C.c_int),

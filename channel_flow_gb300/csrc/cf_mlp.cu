@@ -340,12 +340,79 @@ __global__ void k_mlp_features(mlp_grid g, mlp_levels L, const float *scale, con
     *reinterpret_cast<uint4 *>(X + (size_t)r * MLP_K1 + ch * 8) = *reinterpret_cast<const uint4 *>(h);
 }
 
-// targets of row r: the error of the quadratic extrapolation
-// U^n + 2 dU^n - dU^(n-1), i.e. U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2), over
-// scale[5 + v] * oscale[v]; columns 5..15 zero.  L.u[0..2] = U^n, U^(n-1), U^(n-2),
-// next = U^(n+1)
-__global__ void k_mlp_targets(mlp_grid g, mlp_levels L, mlp_levels next, const float *scale, const float *oscale,
-                              const int *rows, long long M, long long Mpad, float *T)
+// Feature rows of every interior cell in two passes (the guess on the
+// whole grid).  k_mlp_diffs forms the ten time differences of every array
+// index once, rounded to FP32 as k_mlp_features rounds them: D[y * N + q],
+// y < 5 the first difference of variable y, y >= 5 the second difference
+// of variable y - 5.  k_mlp_features_grid then gathers the 270 stencil
+// values of 32 consecutive rows per block into shared memory (one lane per
+// row, so each gather is coalesced along z) and writes the block's 32 rows
+// (20 KB, contiguous in X) with coalesced stores.  The values equal
+// k_mlp_features' bit for bit: the same FP64 differences, the same FP32
+// rounding and scaling.
+__global__ void __launch_bounds__(256) k_mlp_diffs(size_t N, mlp_levels L, float *D)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= N) return;
+#pragma unroll
+    for (int v = 0; v < 5; v++) {
+        const double a0 = L.u[0][v][q], a1 = L.u[1][v][q], a2 = L.u[2][v][q];
+        D[(size_t)v * N + q] = (float)(a0 - a1);
+        D[(size_t)(5 + v) * N + q] = (float)((a0 - 2.0 * a1) + a2);
+    }
+}
+
+constexpr int MLP_FROWS = 32;                 // rows per block
+constexpr int MLP_FPAIRS = MLP_K1 / 2;        // 160 column pairs (32-bit words) per row
+constexpr int MLP_FSTRIDE = MLP_FPAIRS + 1;   // padded row stride in words: lanes hit distinct banks
+
+__global__ void __launch_bounds__(256) k_mlp_features_grid(mlp_grid g, size_t N, const float *__restrict__ D,
+                                                           const float *scale, long long M, long long Mpad,
+                                                           uint32_t *Xw)
+{
+    __shared__ uint32_t tile[MLP_FROWS * MLP_FSTRIDE];
+    __shared__ float inv[10];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 10) inv[threadIdx.x] = 1.0f / scale[threadIdx.x];
+    __syncthreads();
+    const long long r0 = (long long)blockIdx.x * MLP_FROWS;
+    const long long r = r0 + lane;
+    const bool live = r < M;
+    const size_t q = live ? g.cell(r) : 0;
+    const ptrdiff_t sx = (ptrdiff_t)g.Ym() * g.Zm(), sy = g.Zm();
+    for (int pr = warp; pr < MLP_FPAIRS; pr += 8) {
+        float f[2] = {0.f, 0.f};
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            const int c = 2 * pr + e;
+            if (live && c < MLP_IN) {
+                const int l = c / 135, rem = c % 135, v = rem / 27, st = rem % 27;
+                const ptrdiff_t p = (ptrdiff_t)q + (st / 9 - 1) * sx + ((st / 3) % 3 - 1) * sy + (st % 3 - 1);
+                f[e] = D[(size_t)(5 * l + v) * N + (size_t)p] * inv[5 * l + v];
+            }
+        }
+        __nv_bfloat162 h = __floats2bfloat162_rn(f[0], f[1]);
+        tile[lane * MLP_FSTRIDE + pr] = *reinterpret_cast<uint32_t *>(&h);
+    }
+    __syncthreads();
+    const long long rows = Mpad - r0 < MLP_FROWS ? Mpad - r0 : MLP_FROWS;
+    for (int w = threadIdx.x; w < rows * MLP_FPAIRS; w += blockDim.x) {
+        const int rr = w / MLP_FPAIRS, pr = w % MLP_FPAIRS;
+        Xw[(size_t)r0 * MLP_FPAIRS + w] = tile[rr * MLP_FSTRIDE + pr];
+    }
+}
+
+// coefficients of the linear predictor P = U^n + a_v dU^n + b_v d2U of
+// U^(n+1) that the network corrects (a = b = 1: the quadratic extrapolation)
+struct mlp_coef {
+    double a[5], b[5];
+};
+
+// targets of row r: the error U^(n+1) - P of the predictor, over
+// scale[5 + v] * oscale[v]; columns 5..15 zero.  L.u[0..2] = U^n, U^(n-1),
+// U^(n-2), next = U^(n+1)
+__global__ void k_mlp_targets(mlp_grid g, mlp_levels L, mlp_levels next, mlp_coef cf, const float *scale,
+                              const float *oscale, const int *rows, long long M, long long Mpad, float *T)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= Mpad) return;
@@ -354,16 +421,17 @@ __global__ void k_mlp_targets(mlp_grid g, mlp_levels L, mlp_levels next, const f
     if (r >= M) return;
     const size_t q = g.cell(rows ? rows[r] : r);
     for (int v = 0; v < 5; v++) {
-        const double d3 = next.u[0][v][q] - 3.0 * L.u[0][v][q] + 3.0 * L.u[1][v][q] - L.u[2][v][q];
-        t[v] = (float)(d3 / ((double)scale[5 + v] * (double)oscale[v]));
+        const double un = L.u[0][v][q], u1 = L.u[1][v][q];
+        const double d1 = un - u1, d2 = (un - 2.0 * u1) + L.u[2][v][q];
+        const double e = ((next.u[0][v][q] - un) - cf.a[v] * d1) - cf.b[v] * d2;
+        t[v] = (float)(e / ((double)scale[5 + v] * (double)oscale[v]));
     }
 }
 
 // the learned initial guess on every interior cell:
-// U_ = U^n + 2 dU^n - dU^(n-1) + scale[5 + v] * oscale[v] * Y (Y null: the
-// plain quadratic extrapolation)
-__global__ void k_mlp_apply(mlp_grid g, mlp_levels L, const float *scale, const float *oscale, const float *Y,
-                            long long M, double *o0, double *o1, double *o2, double *o3, double *o4)
+// U_ = P + scale[5 + v] * oscale[v] * Y (Y null: the predictor alone)
+__global__ void k_mlp_apply(mlp_grid g, mlp_levels L, mlp_coef cf, const float *scale, const float *oscale,
+                            const float *Y, long long M, double *o0, double *o1, double *o2, double *o3, double *o4)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= M) return;
@@ -371,9 +439,10 @@ __global__ void k_mlp_apply(mlp_grid g, mlp_levels L, const float *scale, const 
     double *o[5] = {o0, o1, o2, o3, o4};
 #pragma unroll
     for (int v = 0; v < 5; v++) {
-        const double un = L.u[0][v][q], u1 = L.u[1][v][q], u2 = L.u[2][v][q];
+        const double un = L.u[0][v][q], u1 = L.u[1][v][q];
+        const double d1 = un - u1, d2 = (un - 2.0 * u1) + L.u[2][v][q];
         const double c = Y ? (double)scale[5 + v] * (double)oscale[v] * (double)Y[(size_t)r * MLP_N3 + v] : 0.0;
-        o[v][q] = un + 2.0 * (un - u1) - (u1 - u2) + c;
+        o[v][q] = ((un + cf.a[v] * d1) + cf.b[v] * d2) + c;
     }
 }
 
@@ -408,6 +477,54 @@ __global__ void k_mlp_sq_partial(mlp_grid g, mlp_levels4 L, long long M, double 
         __syncthreads();
     }
     if (threadIdx.x == 0) partial[(size_t)y * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// partial sums (block b, variable v) of the least-squares fit of the
+// predictor: d1 d1, d1 d2, d2 d2, t d1, t d2, t t with d1 = U^n - U^(n-1),
+// d2 = U^n - 2 U^(n-1) + U^(n-2), t = U^(n+1) - U^n (L.u[0..3] = U^(n+1),
+// U^n, U^(n-1), U^(n-2)); partial[(b * 5 + v) * 6 + s]
+struct mlp_levels20 {
+    const double *u[4][5];
+};
+
+__global__ void k_mlp_base_sums(mlp_grid g, mlp_levels20 L, long long M, double *partial)
+{
+    const int v = blockIdx.y;
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x) {
+        const size_t q = g.cell(r);
+        const double un = L.u[1][v][q], u1 = L.u[2][v][q];
+        const double d1 = un - u1, d2 = (un - 2.0 * u1) + L.u[3][v][q], t = L.u[0][v][q] - un;
+        s[0] += d1 * d1;
+        s[1] += d1 * d2;
+        s[2] += d2 * d2;
+        s[3] += t * d1;
+        s[4] += t * d2;
+        s[5] += t * t;
+    }
+    __shared__ double sh[6][256];
+#pragma unroll
+    for (int c = 0; c < 6; c++) sh[c][threadIdx.x] = s[c];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+#pragma unroll
+            for (int c = 0; c < 6; c++) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) partial[((size_t)blockIdx.x * 5 + v) * 6 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// the feature scales on the device (no host round trip): scale[y] =
+// sqrt(sum over the nb partial sums of row y / M), 1 where that is 0
+__global__ void k_mlp_scale_finish(const double *partial, int nb, long long M, float *scale)
+{
+    const int y = threadIdx.x;
+    if (y >= 10) return;
+    double t = 0;
+    for (int b = 0; b < nb; b++) t += partial[(size_t)y * nb + b];
+    const double r = sqrt(t / (double)M);
+    scale[y] = r > 0 ? (float)r : 1.0f;
 }
 
 // per-block sums over rows of T.Y, Y.Y and T.T for each of the 5 outputs
@@ -617,9 +734,36 @@ int cf_mlp_features(void *stream, int X, int Y, int Z, const double *const *leve
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
+int cf_mlp_features_grid(void *stream, int X, int Y, int Z, const double *const *levels15, const float *scale,
+                         long long Mpad, float *diff_scratch, void *Xout)
+{
+    const long long M = (long long)X * Y * Z;
+    if (!levels15 || !scale || !Xout || !diff_scratch || X <= 0 || Y <= 0 || Z <= 0 || Mpad < M || Mpad % 128)
+        return CF_ERR_ARG;
+    for (int i = 0; i < 15; i++)
+        if (!levels15[i]) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    const size_t N = (size_t)(X + 6) * g.Ym() * g.Zm();
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    k_mlp_diffs<<<nblk((long long)N, 256), 256, 0, s>>>(N, levels(levels15), diff_scratch);
+    k_mlp_features_grid<<<nblk(Mpad, MLP_FROWS), 256, 0, s>>>(g, N, diff_scratch, scale, M, Mpad,
+                                                               static_cast<uint32_t *>(Xout));
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
 // targets [Mpad x 16] fp32: levels20 = U^(n+1), U^n, U^(n-1), U^(n-2)
-int cf_mlp_targets(void *stream, int X, int Y, int Z, const double *const *levels20, const float *scale,
-                   const float *oscale, const int *rows, long long M, long long Mpad, float *T)
+static mlp_coef coef_of(const double *c10)
+{
+    mlp_coef c;
+    for (int v = 0; v < 5; v++) {
+        c.a[v] = c10 ? c10[v] : 1.0;
+        c.b[v] = c10 ? c10[5 + v] : 1.0;
+    }
+    return c;
+}
+
+int cf_mlp_targets(void *stream, int X, int Y, int Z, const double *const *levels20, const double *coef10,
+                   const float *scale, const float *oscale, const int *rows, long long M, long long Mpad, float *T)
 {
     if (!levels20 || !scale || !oscale || !T || M <= 0 || Mpad < M || Mpad % 128) return CF_ERR_ARG;
     mlp_grid g{X, Y, Z};
@@ -627,22 +771,48 @@ int cf_mlp_targets(void *stream, int X, int Y, int Z, const double *const *level
     for (int v = 0; v < 5; v++) next.u[0][v] = levels20[v];
     for (int l = 0; l < 3; l++)
         for (int v = 0; v < 5; v++) L.u[l][v] = levels20[5 * (l + 1) + v];
-    k_mlp_targets<<<nblk(Mpad, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(g, L, next, scale, oscale, rows,
-                                                                                   M, Mpad, T);
+    k_mlp_targets<<<nblk(Mpad, 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(g, L, next, coef_of(coef10), scale,
+                                                                                   oscale, rows, M, Mpad, T);
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
-// U_ (out5) = U^n + 2 dU^n - dU^(n-1) + scale * oscale * Y on all interior
-// cells; levels15 = U^n, U^(n-1), U^(n-2)
-int cf_mlp_apply(void *stream, int X, int Y, int Z, const double *const *levels15, const float *scale,
-                 const float *oscale, const float *Yp, double *const *out5)
+// U_ (out5) = P + scale * oscale * Y on all interior cells; levels15 = U^n,
+// U^(n-1), U^(n-2)
+int cf_mlp_apply(void *stream, int X, int Y, int Z, const double *const *levels15, const double *coef10,
+                 const float *scale, const float *oscale, const float *Yp, double *const *out5)
 {
     if (!levels15 || !out5 || (Yp && (!scale || !oscale))) return CF_ERR_ARG;
     mlp_grid g{X, Y, Z};
     const long long M = (long long)X * Y * Z;
     k_mlp_apply<<<nblk(M, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        g, levels(levels15), scale, oscale, Yp, M, out5[0], out5[1], out5[2], out5[3], out5[4]);
+        g, levels(levels15), coef_of(coef10), scale, oscale, Yp, M, out5[0], out5[1], out5[2], out5[3], out5[4]);
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_mlp_base_sums(void *stream, int X, int Y, int Z, const double *const *levels20, double *partial_dev,
+                     int nblocks, double *sums30)
+{
+    if (!levels20 || !partial_dev || !sums30 || nblocks <= 0 || X <= 0 || Y <= 0 || Z <= 0) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    mlp_levels20 L{};
+    for (int l = 0; l < 4; l++)
+        for (int v = 0; v < 5; v++) {
+            if (!levels20[5 * l + v]) return CF_ERR_ARG;
+            L.u[l][v] = levels20[5 * l + v];
+        }
+    const long long M = (long long)X * Y * Z;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    k_mlp_base_sums<<<dim3((unsigned)nblocks, 5), 256, 0, s>>>(g, L, M, partial_dev);
+    std::vector<double> h((size_t)30 * nblocks);
+    if (cudaMemcpyAsync(h.data(), partial_dev, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return CF_ERR_CUDA;
+    for (int n = 0; n < 30; n++) {
+        double t = 0;
+        for (int b = 0; b < nblocks; b++) t += h[(size_t)b * 30 + n];
+        sums30[n] = t;
+    }
+    return CF_OK;
 }
 
 static int mlp_rms(int D, void *stream, int X, int Y, int Z, const double *const *lv, double *partial_dev,
@@ -679,6 +849,26 @@ int cf_mlp_rms(void *stream, int X, int Y, int Z, const double *const *levels15,
                int nblocks, double *rms10)
 {
     return mlp_rms(1, stream, X, Y, Z, levels15, partial_dev, nblocks, rms10);
+}
+
+// the ten feature scales of cf_mlp_rms written to scale10_dev on the
+// device, stream-ordered (no synchronisation)
+int cf_mlp_scale(void *stream, int X, int Y, int Z, const double *const *lv, double *partial_dev, int nblocks,
+                 float *scale10_dev)
+{
+    if (!lv || !partial_dev || !scale10_dev || nblocks <= 0 || X <= 0 || Y <= 0 || Z <= 0) return CF_ERR_ARG;
+    mlp_grid g{X, Y, Z};
+    mlp_levels4 L{};
+    for (int l = 0; l < 3; l++)
+        for (int v = 0; v < 5; v++) {
+            if (!lv[5 * l + v]) return CF_ERR_ARG;
+            L.u[l][v] = lv[5 * l + v];
+        }
+    const long long M = (long long)X * Y * Z;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    k_mlp_sq_partial<1><<<dim3((unsigned)nblocks, 10), 256, 0, s>>>(g, L, M, partial_dev);
+    k_mlp_scale_finish<<<1, 32, 0, s>>>(partial_dev, nblocks, M, scale10_dev);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
 // RMS of U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2) per variable (levels20 in that order)

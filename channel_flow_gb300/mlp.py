@@ -2,16 +2,20 @@
 
 A per-cell MLP maps the 3x3x3 neighbourhood of the last two time
 increments dU^n = U^n - U^(n-1) and dU^(n-1) = U^(n-1) - U^(n-2) of the
-five conserved variables, presented as dU^n and dU^n - dU^(n-1) (2 x 27 x 5
-= 270 features, each kind scaled per variable by its interior RMS; the
-second difference is formed in FP64, because in BF16 the two increments
-agree to about the digits that their difference needs), through two hidden
-layers of 128 SiLU units to the five components of the error of the
-quadratic extrapolation U^n + 2 dU^n - dU^(n-1) of U^(n+1) (in units of the
+five conserved variables, presented as dU^n and d2U = dU^n - dU^(n-1)
+(2 x 27 x 5 = 270 features, each kind scaled per variable by its interior
+RMS; the second difference is formed in FP64, because in BF16 the two
+increments agree to about the digits that their difference needs), through
+two hidden layers of 128 SiLU units to the five components of the error of
+a linear predictor P = U^n + a_v dU^n + b_v d2U of U^(n+1) (in units of the
 RMS second difference times a per-variable factor fitted on the training
-windows).  The network corrects the extrapolation rather than predicting the
-increment itself, so its BF16 precision limits only the small correction,
-and a least-squares gain per variable, fitted on a held-out window, scales a
+windows).  a_v and b_v are least-squares fits over the training windows:
+a smooth transient gives about the quadratic extrapolation (a = b = 1), an
+oscillating one (acoustic waves of the initial state) about the plain
+start U^n (a = b = 0), which the quadratic extrapolation then overshoots.
+The network corrects the predictor rather than predicting the increment
+itself, so its BF16 precision limits only the small correction, and a
+least-squares gain per variable, fitted on a held-out window, scales a
 correction that does not help there towards zero.  Before the
 sub-iterations of a physical step the state starts from that guess instead
 of U^n; the sub-iterations still run to the same residual tolerance, so the
@@ -120,9 +124,11 @@ class LearnedGuess:
         self.H2T = torch.zeros(H, M, dtype=bf, device=dev)
         self.XT = torch.zeros(K1, M, dtype=bf, device=dev)
         self.partial = torch.zeros(M // 256 * 6, dtype=f32, device=dev)
-        self.rms_partial = torch.zeros(10 * 512, dtype=torch.float64, device=dev)
+        self.rms_partial = torch.zeros(30 * 512, dtype=torch.float64, device=dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
         self.scale = torch.ones(10, dtype=f32, device=dev)
+        self.coef = np.ones(10)                             # predictor a[0..4], b[5..9] (quadratic extrapolation)
+        self.D = None                                       # FP32 time differences of the whole-grid feature rows
         self.oscale = torch.ones(5, dtype=f32, device=dev)   # output unit of the network (targets)
         self.ogain = torch.ones(5, dtype=f32, device=dev)    # oscale times the fitted gain (the guess)
         self.gen = torch.Generator(device=dev)
@@ -229,6 +235,15 @@ class LearnedGuess:
         if Mpad > self.cap:
             raise ValueError(f"{M} rows exceed the capacity {self.cap}")
         arr = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
+        if rows is None:
+            # every cell: the time differences once per array index, then the rows
+            n = 10 * (grid.X_out + 6) * (grid.Y_out + 4) * (grid.Z_out + 4)
+            if self.D is None or self.D.numel() < n:
+                self.D = self.torch.empty(n, dtype=self.torch.float32, device="cuda")
+            self._ok(self.lib.cf_mlp_features_grid(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
+                                                   self.scale.data_ptr(), Mpad, self.D.data_ptr(), self.X.data_ptr()),
+                     "cf_mlp_features_grid")
+            return M, Mpad
         self._ok(self.lib.cf_mlp_features(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
                                           self.scale.data_ptr(), None if rows is None else rows.data_ptr(),
                                           M, Mpad, self.X.data_ptr()), "cf_mlp_features")
@@ -240,24 +255,46 @@ class LearnedGuess:
         if Mpad > self.tcap:
             raise ValueError(f"{M} rows exceed the training batch {self.tcap}")
         arr = (C.c_void_p * 20)(*[t.data_ptr() for t in list(Unp1) + list(Un) + list(Unm1) + list(Unm2)])
-        self._ok(self.lib.cf_mlp_targets(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr, self.scale.data_ptr(),
+        self._ok(self.lib.cf_mlp_targets(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr, self.coef.ctypes.data,
+                                         self.scale.data_ptr(),
                                          self.oscale.data_ptr(), None if rows is None else rows.data_ptr(), M, Mpad,
                                          self.T.data_ptr()), "cf_mlp_targets")
         return M, Mpad
 
-    def fit_output_scale(self, grid, history, windows=None):
-        """Per-variable output factor: RMS of the extrapolation error over
-        the RMS of the second time difference, averaged over the windows n
-        (default all) of a history [U^0, U^1, ...] of FP64 states."""
+    def _base_sums(self, grid, history, n):
+        """sums30 of cf_mlp_base_sums for window n of a history, as (5, 6)."""
+        sums = np.zeros(30)
+        lv = [history[n + 1], history[n], history[n - 1], history[n - 2]]
+        arr = (C.c_void_p * 20)(*[t.data_ptr() for level in lv for t in level])
+        self._ok(self.lib.cf_mlp_base_sums(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
+                                           self.rms_partial.data_ptr(), 512, sums.ctypes.data), "cf_mlp_base_sums")
+        return sums.reshape(5, 6)
+
+    def fit_output_scale(self, grid, history, windows=None, fit_predictor: bool = True):
+        """Least-squares coefficients a_v, b_v of the predictor over the
+        windows n (default all) of a history [U^0, U^1, ...] of FP64 states
+        (``fit_predictor``; else the coefficients are kept), and the
+        per-variable output factor: RMS of the predictor's error over the
+        RMS of the second time difference, averaged over the windows."""
+        wins = list(range(2, len(history) - 1)) if windows is None else list(windows)
+        S = [self._base_sums(grid, history, n) for n in wins]
+        if fit_predictor and S:
+            tot = np.sum(S, axis=0)
+            for v in range(5):
+                s11, s12, s22, r1, r2, _ = tot[v]
+                det = s11 * s22 - s12 * s12
+                if det > 1e-12 * max(s11 * s22, 1e-300):
+                    self.coef[v] = (r1 * s22 - r2 * s12) / det
+                    self.coef[5 + v] = (s11 * r2 - s12 * r1) / det
+                else:
+                    self.coef[v] = r1 / s11 if s11 > 0 else 0.0
+                    self.coef[5 + v] = 0.0
+        a, b = self.coef[:5], self.coef[5:]
         r = []
-        for n in (range(2, len(history) - 1) if windows is None else windows):
-            s = self.set_scale(grid, history[n], history[n - 1], history[n - 2])[5:]
-            e = np.zeros(5)
-            lv = [history[n + 1], history[n], history[n - 1], history[n - 2]]
-            arr = (C.c_void_p * 20)(*[t.data_ptr() for level in lv for t in level])
-            self._ok(self.lib.cf_mlp_rms3(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
-                                          self.rms_partial.data_ptr(), 512, e.ctypes.data), "cf_mlp_rms3")
-            r.append(e / s)
+        for s in S:
+            s11, s12, s22, r1, r2, tt = s.T
+            err = tt - 2 * a * r1 - 2 * b * r2 + a * a * s11 + 2 * a * b * s12 + b * b * s22
+            r.append(np.sqrt(np.maximum(err, 0) / np.where(s22 > 0, s22, 1.0)))
         f = np.mean(r, axis=0) if r else np.ones(5)
         f = np.where(f > 0, f, 1.0)
         self.oscale.copy_(self.torch.from_numpy(f.astype(np.float32)))
@@ -307,9 +344,10 @@ class LearnedGuess:
         network has not been trained on, alpha_v = <t, y> / <y, y> clipped
         to [0, 2]; the guess then uses oscale * alpha, so that a correction
         that does not reduce the extrapolation error there is scaled down.
-        Returns alpha and the window's RMS error of extrapolation +
-        correction relative to the extrapolation alone, per variable,
-        before and after the gain."""
+        Returns alpha and the window's RMS error of predictor +
+        correction relative to the predictor alone, per variable, before
+        and after the gain (keys ``err_over_extrapolation*``: the predictor
+        is the fitted one)."""
         torch = self.torch
         gen = self.gen
         if seed is not None:
@@ -354,17 +392,25 @@ class LearnedGuess:
         s = torch.cuda.current_stream().cuda_stream if stream is None else stream
         a = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
         o = (C.c_void_p * 5)(*[t.data_ptr() for t in out])
-        rc = lib.cf_mlp_apply(s, grid.X_out, grid.Y_out, grid.Z_out, a, None, None, None, o)
+        rc = lib.cf_mlp_apply(s, grid.X_out, grid.Y_out, grid.Z_out, a, None, None, None, None, o)
         if rc != _lib.CF_OK:
             raise RuntimeError(f"cf_mlp_apply failed with status {rc}")
 
+    def set_scale_device(self, grid, Un, Unm1, Unm2):
+        """The scales of ``set_scale`` computed and stored on the device,
+        stream-ordered (no host round trip)."""
+        arr = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
+        self._ok(self.lib.cf_mlp_scale(self._s(), grid.X_out, grid.Y_out, grid.Z_out, arr,
+                                       self.rms_partial.data_ptr(), 512, self.scale.data_ptr()), "cf_mlp_scale")
+
     def guess(self, grid, Un, Unm1, Unm2, out):
-        """out (U_) = U^n + 2 dU^n - dU^(n-1) + the network's correction on
+        """out (U_) = U^n + a dU^n + b d2U + the network's correction on
         every interior cell; the grid's cells must fit the capacity."""
-        self.set_scale(grid, Un, Unm1, Unm2)
+        self.set_scale_device(grid, Un, Unm1, Unm2)
         M, Mpad = self.load_features(grid, Un, Unm1, Unm2)
         self.forward(Mpad, keep=False)
         a = (C.c_void_p * 15)(*[t.data_ptr() for t in list(Un) + list(Unm1) + list(Unm2)])
         o = (C.c_void_p * 5)(*[t.data_ptr() for t in out])
-        self._ok(self.lib.cf_mlp_apply(self._s(), grid.X_out, grid.Y_out, grid.Z_out, a, self.scale.data_ptr(),
+        self._ok(self.lib.cf_mlp_apply(self._s(), grid.X_out, grid.Y_out, grid.Z_out, a, self.coef.ctypes.data,
+                                       self.scale.data_ptr(),
                                        self.ogain.data_ptr(), self.Y.data_ptr(), o), "cf_mlp_apply")

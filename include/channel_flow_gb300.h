@@ -388,21 +388,40 @@ int cf_gemm_bf16(void *cuda_stream, const void *A, const void *B, int M, int N, 
  * 3 (dj+1) + (dk+1) of the 3x3x3 stencil, over its scale. */
 int cf_mlp_features(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale10,
                     const int *rows, long long M, long long Mpad, void *X_bf16_Mpad_x_320);
-/* targets: the error of the quadratic extrapolation, U^(n+1) - 3 U^n +
- * 3 U^(n-1) - U^(n-2), over scale10[5 + v] * oscale5[v] (levels20 = U^(n+1),
- * U^n, U^(n-1), U^(n-2)) */
-int cf_mlp_targets(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, const float *scale10,
-                   const float *oscale5, const int *rows, long long M, long long Mpad, float *T_Mpad_x_16);
-/* the guess on every interior cell: out = U^n + 2 dU^n - dU^(n-1) +
- * scale10[5 + v] * oscale5[v] * Y (levels15 = U^n, U^(n-1), U^(n-2));
- * Y = NULL gives the plain quadratic extrapolation (scale10, oscale5 may then be NULL) */
-int cf_mlp_apply(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const float *scale10,
-                 const float *oscale5, const float *Y_M_x_16, double *const *out5);
+/* the same rows for every interior cell (M = X*Y*Z, rows M..Mpad-1 zero),
+ * equal bit for bit, through diff_scratch: 10 * (X+6)*(Y+4)*(Z+4) floats
+ * that receive the FP32 time differences of every array index first */
+int cf_mlp_features_grid(void *cuda_stream, int X, int Y, int Z, const double *const *levels15,
+                         const float *scale10, long long Mpad, float *diff_scratch, void *X_bf16_Mpad_x_320);
+/* The network corrects the linear predictor P = U^n + a_v dU^n + b_v d2U of
+ * U^(n+1), with dU^n = U^n - U^(n-1), d2U = U^n - 2 U^(n-1) + U^(n-2) and
+ * coef10_host = a[0..4], b[5..9] (NULL: a = b = 1, the quadratic
+ * extrapolation U^n + 2 dU^n - dU^(n-1)).
+ * targets: (U^(n+1) - P) over scale10[5 + v] * oscale5[v] (levels20 =
+ * U^(n+1), U^n, U^(n-1), U^(n-2)) */
+int cf_mlp_targets(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, const double *coef10_host,
+                   const float *scale10, const float *oscale5, const int *rows, long long M, long long Mpad,
+                   float *T_Mpad_x_16);
+/* the guess on every interior cell: out = P + scale10[5 + v] * oscale5[v] *
+ * Y (levels15 = U^n, U^(n-1), U^(n-2)); Y = NULL gives P alone (scale10,
+ * oscale5 may then be NULL) */
+int cf_mlp_apply(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, const double *coef10_host,
+                 const float *scale10, const float *oscale5, const float *Y_M_x_16, double *const *out5);
+/* interior sums per variable v for the least-squares fit of P: with
+ * d1 = dU^n, d2 = d2U, t = U^(n+1) - U^n, sums30_host[6 v + 0..5] =
+ * sum d1 d1, d1 d2, d2 d2, t d1, t d2, t t (levels20 = U^(n+1), U^n, U^(n-1),
+ * U^(n-2)); partial_dev holds 30 * nblocks doubles */
+int cf_mlp_base_sums(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, double *partial_dev,
+                     int nblocks, double *sums30_host);
 /* interior RMS per variable of the first and second time differences
  * (rms10_host[0..4], [5..9]); levels15 = U^n, U^(n-1), U^(n-2); partial_dev
  * holds 10 * nblocks doubles */
 int cf_mlp_rms(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, double *partial_dev,
                int nblocks, double *rms10_host);
+/* the same ten RMS values as FP32 feature scales written to scale10_dev on
+ * the device (0 becomes 1), stream-ordered, without a host round trip */
+int cf_mlp_scale(void *cuda_stream, int X, int Y, int Z, const double *const *levels15, double *partial_dev,
+                 int nblocks, float *scale10_dev);
 /* interior RMS per variable of U^(n+1) - 3 U^n + 3 U^(n-1) - U^(n-2) (levels20 in that order) */
 int cf_mlp_rms3(void *cuda_stream, int X, int Y, int Z, const double *const *levels20, double *partial_dev,
                 int nblocks, double *rms5_host);

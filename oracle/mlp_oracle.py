@@ -106,22 +106,33 @@ def features(levels, scale10, X, Y, Z, rows=None):
     return F
 
 
-def targets(next_level, levels, scale10, oscale5, X, Y, Z, rows=None):
-    """cf_mlp_targets: the third time difference over scale10[5+v] * oscale5[v]."""
+def _coef(coef10):
+    c = np.ones(10) if coef10 is None else np.asarray(coef10, np.float64)
+    return c[:5], c[5:]
+
+
+def targets(next_level, levels, scale10, oscale5, X, Y, Z, rows=None, coef10=None):
+    """cf_mlp_targets: the error of the predictor U^n + a dU^n + b d2U
+    (coef10 = a[0..4], b[5..9]; None: a = b = 1) over
+    scale10[5+v] * oscale5[v]."""
     n = X * Y * Z
     rows = np.arange(n) if rows is None else np.asarray(rows)
+    a, b = _coef(coef10)
     T = np.zeros((len(rows), N3))
     for v in range(5):
-        u = [_interior(a[v], X, Y, Z)[rows] for a in (next_level, levels[0], levels[1], levels[2])]
-        d3 = u[0] - 3.0 * u[1] + 3.0 * u[2] - u[3]
-        T[:, v] = d3 / (np.float64(np.float32(scale10[5 + v])) * np.float64(np.float32(oscale5[v])))
+        u = [_interior(x[v], X, Y, Z)[rows] for x in (next_level, levels[0], levels[1], levels[2])]
+        d1 = u[1] - u[2]
+        d2 = (u[1] - 2.0 * u[2]) + u[3]
+        e = ((u[0] - u[1]) - a[v] * d1) - b[v] * d2
+        T[:, v] = e / (np.float64(np.float32(scale10[5 + v])) * np.float64(np.float32(oscale5[v])))
     return T
 
 
-def apply(levels, scale10, oscale5, Y_out16, X, Y, Z):
-    """cf_mlp_apply on the interior: U^n + 2 dU^n - dU^(n-1) + the scaled
-    correction (Y_out16 None: the extrapolation alone); returns five
-    interior arrays [X*Y*Z]."""
+def apply(levels, scale10, oscale5, Y_out16, X, Y, Z, coef10=None):
+    """cf_mlp_apply on the interior: U^n + a dU^n + b d2U + the scaled
+    correction (Y_out16 None: the predictor alone); returns five interior
+    arrays [X*Y*Z]."""
+    a, b = _coef(coef10)
     out = []
     for v in range(5):
         un, u1, u2 = (_interior(levels[l][v], X, Y, Z) for l in range(3))
@@ -129,5 +140,20 @@ def apply(levels, scale10, oscale5, Y_out16, X, Y, Z):
         if Y_out16 is not None:
             c = np.float64(np.float32(scale10[5 + v])) * np.float64(np.float32(oscale5[v])) * \
                 np.asarray(Y_out16[:, v], np.float64)
-        out.append(un + 2.0 * (un - u1) - (u1 - u2) + c)
+        d1 = un - u1
+        d2 = (un - 2.0 * u1) + u2
+        out.append(((un + a[v] * d1) + b[v] * d2) + c)
+    return out
+
+
+def base_sums(levels4, X, Y, Z):
+    """cf_mlp_base_sums: per variable the sums d1 d1, d1 d2, d2 d2, t d1,
+    t d2, t t (levels4 = U^(n+1), U^n, U^(n-1), U^(n-2)); shape (5, 6)."""
+    out = np.zeros((5, 6))
+    for v in range(5):
+        u = [_interior(x[v], X, Y, Z) for x in levels4]
+        d1 = u[1] - u[2]
+        d2 = (u[1] - 2.0 * u[2]) + u[3]
+        t = u[0] - u[1]
+        out[v] = [d1 @ d1, d1 @ d2, d2 @ d2, t @ d1, t @ d2, t @ t]
     return out

@@ -113,14 +113,17 @@ def test_learned_guess_cuts_subiterations(cuda_lib):
     """What the trained network gains, in the mixed-precision loop on a
     64^3 channel at the tolerance 1e-6: against the method without it (the
     plain start from U^n) at most half the sub-iterations, against the
-    quadratic extrapolation that it corrects at least 15% fewer, with the
-    same answer (state difference small against the change over the steps);
-    out of sample (the held-out window) its correction shrinks the
-    extrapolation error of density and energy, the fields whose updates
-    converge last."""
+    quadratic extrapolation at least 15% fewer, with the same answer (state
+    difference small against the change over the steps); out of sample (the
+    held-out window) its correction shrinks the error of the fitted linear
+    predictor it corrects for density and energy, the fields whose updates
+    converge last.  (The loss falls by half at least: the fitted predictor
+    already removes most of what a correction of the plain extrapolation
+    would learn.)"""
     its, final, start, net, losses = _guess_study((64, 64, 64), harvest=12, evals=4, precision="fp32",
                                                   epochs=40, batch=65536)
-    assert losses[-1] < 0.1 * losses[0]
+    print(its, net.coef, net.validation)
+    assert losses[-1] < 0.5 * losses[0]
     plain, extra, learned = (np.mean(its[k]) for k in ("plain", "extrapolate", "learned"))
     assert learned <= 0.5 * plain, its
     assert learned <= 0.85 * extra, its
@@ -144,11 +147,19 @@ def test_mlp_data_kernels_match_oracle(cuda_lib):
     g = type("G", (), {"X_out": X, "Y_out": Y, "Z_out": Z, "cells": X * Y * Z})()
     net = mlp.LearnedGuess(capacity=256, seed=0)
     Dn, D1, D2, Dx = dev(un), dev(u1), dev(u2), dev(nxt)
+    net.set_scale_device(g, Dn, D1, D2)
+    sc_dev = net.scale.cpu().numpy()
     sc = net.set_scale(g, Dn, D1, D2)
     want = mlp_oracle.rms([un, u1, u2], X, Y, Z)
     assert np.allclose(sc, want, rtol=1e-12), (sc, want)
+    assert np.allclose(sc_dev, want.astype(np.float32), rtol=1e-6), (sc_dev, want)
     net.oscale.copy_(torch.tensor([0.5, 1.5, 2.0, 0.25, 1.0]))
     osc = net.oscale.cpu().numpy()
+    # the sums of the predictor fit, and a predictor with mixed coefficients
+    sums = net._base_sums(g, [D2, D1, Dn, Dx], 2).copy()
+    assert np.allclose(sums, mlp_oracle.base_sums([nxt, un, u1, u2], X, Y, Z), rtol=1e-12, atol=0)
+    net.coef[:] = [0.3, 1.0, -0.2, 0.0, 1.7, 0.9, 0.0, 0.4, 1.0, -0.5]
+    coef = net.coef.copy()
     M, Mpad = net.load_features(g, Dn, D1, D2)
     F = net.X[:Mpad].float().cpu().numpy()
     Fw = mlp_oracle.features([un, u1, u2], sc.astype(np.float32), X, Y, Z)
@@ -158,16 +169,16 @@ def test_mlp_data_kernels_match_oracle(cuda_lib):
     assert np.array_equal(net.X[:M].float().cpu().numpy(), Fw[rows])
     M, Mpad = net.load_targets(g, Dx, Dn, D1, D2)
     T = net.T[:M].cpu().numpy()
-    Tw = mlp_oracle.targets(nxt, [un, u1, u2], sc, osc, X, Y, Z)
+    Tw = mlp_oracle.targets(nxt, [un, u1, u2], sc, osc, X, Y, Z, coef10=coef)
     assert np.allclose(T, Tw, rtol=1e-6, atol=1e-6 * np.abs(Tw).max())
     Yc = rng.normal(size=(M, 16)).astype(np.float32)
     net.Y[:M].copy_(torch.from_numpy(Yc))
     out = dev([np.zeros(shape)] * 5)
     net._ok(net.lib.cf_mlp_apply(net._s(), X, Y, Z, (mlp.C.c_void_p * 15)(*[t.data_ptr() for t in Dn + D1 + D2]),
-                                 net.scale.data_ptr(), net.oscale.data_ptr(), net.Y.data_ptr(),
+                                 coef.ctypes.data, net.scale.data_ptr(), net.oscale.data_ptr(), net.Y.data_ptr(),
                                  (mlp.C.c_void_p * 5)(*[t.data_ptr() for t in out])), "cf_mlp_apply")
     got = [o.cpu().numpy()[3:3 + X, 2:2 + Y, 2:2 + Z].reshape(-1) for o in out]
-    want = mlp_oracle.apply([un, u1, u2], sc, osc, Yc, X, Y, Z)
+    want = mlp_oracle.apply([un, u1, u2], sc, osc, Yc, X, Y, Z, coef10=coef)
     for v in range(5):
         assert np.allclose(got[v], want[v], rtol=1e-14, atol=0), v
     mlp.LearnedGuess.extrapolate(g, Dn, D1, D2, out)
