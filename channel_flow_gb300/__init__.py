@@ -90,6 +90,11 @@ class Context:
         self._ok(self.lib.cf_set_scheme(self.h, _lib.SCHEME[scheme]))
         self.scheme = scheme
 
+    def set_wait_limit(self, polls: int = 0):
+        """Polls of a wavefront dependency wait before it gives up and the
+        call returns CF_ERR_TIMEOUT (0: the default); a test hook."""
+        self._ok(self.lib.cf_set_wait_limit(self.h, polls))
+
     def lu_trace(self, enable: bool = True):
         """Record per-tile timer stamps of the wavefront sweeps."""
         self._ok(self.lib.cf_lu_trace(self.h, 1 if enable else 0))

@@ -41,6 +41,7 @@ struct cf_ctx {
     cudaStream_t side = nullptr;      // cf_step: Flux_Y/Z beside the viscous terms
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int lu_schedule = CF_LU_WAVEFRONT;                // hyperplane sweep schedule
+    unsigned wait_limit = CF_WAVE_SPIN_LIMIT;         // polls of a wavefront dependency wait
     int *tile_order = nullptr;        // wavefront tiles sorted by plane (device)
     long long *trace = nullptr;       // wavefront trace: [2 sweeps][tiles][4] stamps, when enabled
     size_t trace_tiles = 0;
@@ -255,6 +256,13 @@ int cf_set_scheme(cf_ctx *c, int scheme)
 {
     if (!c || (scheme != CF_SCHEME_REFERENCE && scheme != CF_SCHEME_CONSISTENT)) return CF_ERR_ARG;
     c->d.scheme = scheme;
+    return CF_OK;
+}
+
+int cf_set_wait_limit(cf_ctx *c, unsigned polls)
+{
+    if (!c) return CF_ERR_ARG;
+    c->wait_limit = polls ? polls : CF_WAVE_SPIN_LIMIT;
     return CF_OK;
 }
 
@@ -718,6 +726,7 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     w.flags = reinterpret_cast<int *>(f);
     w.counter = w.flags + w.ntiles;
     w.err = w.flags + w.ntiles + 1;
+    w.dep_limit = c->wait_limit;
     w.trace = nullptr;
     if (c->trace_tiles) {
         if (c->trace_tiles != (size_t)w.ntiles) {
@@ -904,6 +913,8 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     std::memcpy(kp, &c->lu_schedule, sizeof c->lu_schedule);
     key.insert(key.end(), reinterpret_cast<const unsigned char *>(&w.trace),
                reinterpret_cast<const unsigned char *>(&w.trace) + sizeof w.trace);
+    key.insert(key.end(), reinterpret_cast<const unsigned char *>(&w.dep_limit),
+               reinterpret_cast<const unsigned char *>(&w.dep_limit) + sizeof w.dep_limit);
     if (!c->dts_exec || key != c->dts_key) {
         if (int rc = capture_dts(c, a, pack, w, deltaT)) return rc;
         c->dts_key = key;
@@ -1322,6 +1333,10 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         if (int rc = cuda_check(c, cudaStreamWaitEvent(main, c->ev_join, 0), "cf_step")) return rc;
         if (int rc = dts_common(c, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr, nullptr, dts,
                                 f32_rhs, static_m, f32_rhs)) return rc;
+        for (int n = 0; n < 5; n++)
+            if (!std::isfinite(er[n]))
+                return fail(c, CF_ERR_NONFINITE, "cf_step: residual norm er%d is not finite at iteration %d", n + 1,
+                            it);
         for (int n = 0; n < 5; n++) {
             c->E[n] = std::max(c->E[n], er[n]);
             er[n] = er[n] / c->E[n];

@@ -145,6 +145,7 @@ struct cf_lu_args {
 
 // tiled wavefront of the hyperplane sweeps (cf_wave.cuh)
 constexpr int CF_WAVE_TI = 4, CF_WAVE_TJ = 8, CF_WAVE_TK = 8, CF_WAVE_PACK = 50;
+constexpr unsigned CF_WAVE_SPIN_LIMIT = 1u << 22;   // default polls before a wavefront wait gives up
 struct cf_wave_args {
     cf_dims d;
     int nti, ntj, ntk, ntiles;
@@ -155,6 +156,8 @@ struct cf_wave_args {
     int *flags;              // per tile: 1 when done; [ntiles] = claim counter, [ntiles+1] = error word
     int *counter;
     int *err;                // bit 0: dependency wait ran out, bit 1: pack copy wait ran out
+    unsigned dep_limit;      // polls of a dependency-flag wait before it gives up (the tile's own
+                             // copy waits keep CF_WAVE_SPIN_LIMIT)
     long long *trace;        // optional: per tile 4 global-timer stamps (claimed, inputs ready,
                              // pack landed, done); NULL when tracing is off
 };

@@ -36,7 +36,7 @@ constexpr int WV_TI = 4, WV_TJ = 8, WV_TK = 8, WV_CELLS = WV_TI * WV_TJ * WV_TK;
 constexpr int WV_PACK = 50;          // values per cell of a tile pack
 constexpr int WV_STAGE = 44;         // values per cell a sweep stages (forward: 6..49, backward: 0..38)
 constexpr int WV_FWD0 = 6;           // first value of the forward window
-constexpr unsigned WV_SPIN_LIMIT = 1u << 22;   // polls before a wait gives up
+constexpr unsigned WV_SPIN_LIMIT = CF_WAVE_SPIN_LIMIT;   // polls before a copy wait gives up
 
 // One pack per tile (tile-major; inside a tile value-major, value m of cell
 // c = (li*8 + lj)*8 + lk at [m][c]), ordered so that each sweep stages one
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
                 const int *f = w.flags + (na * w.ntj + nb) * w.ntk + nc;
                 unsigned it = 0;
                 while (ld_acquire(f) == 0) {
-                    if (++it > WV_SPIN_LIMIT) {
+                    if (++it > w.dep_limit) {
                         atomicOr(w.err, 1);
                         break;
                     }

@@ -83,6 +83,13 @@ int cf_set_stretching(cf_ctx *ctx, double gamma);
 #define CF_LU_WAVEFRONT 0
 #define CF_LU_PLANES 1
 int cf_set_lu_schedule(cf_ctx *ctx, int schedule);
+/* Polls of a wavefront dependency wait (a tile waiting for the done flags
+ * of its upstream tiles) before it gives up, sets the error word and the
+ * call returns CF_ERR_TIMEOUT; 0 restores the default (2^22 polls of
+ * about 20 ns).  A test hook: a short limit makes a wait run out on
+ * purpose, without a fault or a hang (the tile's own copy waits keep the
+ * default limit, so no copy is left in flight). */
+int cf_set_wait_limit(cf_ctx *ctx, unsigned polls);
 /* Face-state scaling of the limited fluxes.  CF_SCHEME_REFERENCE (default)
  * is the reference's, bit for bit in CF_PREC_FP64_EXACT.  Two of its
  * scalings are inconsistent, and the assembled limited loop diverges on
@@ -347,7 +354,9 @@ typedef struct {
  * statistic_step > 0, and Uq <- U, U <- U_.  Returns the iteration count,
  * the last normalised er1..er5 and Q (pointers may be NULL).  In
  * CF_PREC_FP32 the loop's intermediate arrays (inF, vF, LL, ML, MR, NR, NL)
- * are its scratch and hold FP32 values in their FP64 allocation afterwards. */
+ * are its scratch and hold FP32 values in their FP64 allocation afterwards.
+ * A residual norm that is not finite (a NaN or Inf in the state) ends the
+ * step with CF_ERR_NONFINITE. */
 int cf_step(cf_ctx *ctx, const cf_step_params *params, int step, const cf_fields *fields, int *iterations,
             double *er, double *Q);
 /* forget the running residual maxima and the FP32 metric copies */

@@ -205,3 +205,64 @@ def test_gpu_dts_schedules_agree(precision, cuda_lib):
         scale = max(float(np.max(np.abs(a1[i]))), 1e-300)
         assert float(np.max(np.abs(a0[i] - a1[i]))) / scale <= tol, i
     np.testing.assert_allclose(np.asarray(e0), np.asarray(e1), rtol=tol * 10, atol=0)
+
+
+CONFIG0_GRID = (64, 64, 64)
+
+
+@pytest.mark.parametrize("name", [r.name for r in routines.ROUTINES])
+def test_gpu_exact_equals_oracle_config0_grid(name, port, cuda_lib):
+    """Every routine at the 64^3 grid of the CPU-runnable configuration
+    (many wavefront tiles, grids of several waves, the filter's full
+    level sizes), no-FMA build against the oracle: bit for bit on every
+    written array and every face, norms to 1e-12, tanh/cosh metrics to
+    1e-13."""
+    import channel_flow_gb300 as cf
+    r = routines.BY_NAME[name]
+    g = cases.grid(CONFIG0_GRID)
+    ctx = cf.Context(g, precision="fp64_exact")
+    try:
+        want, got, e_want, e_got = _run_both(port, ctx, r, g, seed=17)
+    finally:
+        ctx.close()
+    if r.libm:
+        diff = routines.compare(r, g, got, want, rtol=1)
+        assert max(diff.values()) <= 1e-13, diff
+    else:
+        diff = routines.compare(r, g, got, want)
+        assert all(v == 0 for v in diff.values()), f"{name}: differing entries per slot {diff}"
+    if r.scalars:
+        np.testing.assert_allclose(e_got, e_want, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("name", ["Flux_Y_limiter", "Flux_Z_limiter"])
+def test_gpu_consistent_exact_equals_oracle_config0_grid(name, port, cuda_lib):
+    """The consistent face-state scaling at 64^3, no-FMA build, bit for bit."""
+    import channel_flow_gb300 as cf
+    r = routines.BY_NAME[name]
+    g = cases.grid(CONFIG0_GRID)
+    a = r.build(g, 19)
+    want, got = cases.copy_case(a), cases.copy_case(a)
+    routines.run_cpu(port, r, g, want, scheme="consistent")
+    ctx = cf.Context(g, precision="fp64_exact", scheme="consistent")
+    try:
+        routines.run_gpu(ctx, r, got)
+    finally:
+        ctx.close()
+    diff = routines.compare(r, g, got, want)
+    assert all(v == 0 for v in diff.values()), diff
+
+
+@pytest.mark.parametrize("dims", cases.GRIDS + [(13, 9, 17), CONFIG0_GRID])
+def test_gpu_hyperplane_tables_equal_oracle(dims, port, cuda_lib):
+    """cf_Hyperplane's plane tables Nijk and ijk (Hyperplane.cpp:50-78)
+    equal the oracle's, whose tables equal the reference's."""
+    import channel_flow_gb300 as cf
+    g = cases.grid(dims)
+    ctx = cf.Context(g, precision="fp64_exact")
+    try:
+        n_gpu, i_gpu = ctx.Hyperplane()
+    finally:
+        ctx.close()
+    n_cpu, i_cpu = port.Hyperplane(g)
+    assert np.array_equal(n_gpu, n_cpu) and np.array_equal(i_gpu, i_cpu)
