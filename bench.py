@@ -48,7 +48,6 @@ ALG_BYTES = {"Filter": 80, "Flux_X_limiter": 168, "Flux_Y_limiter": 176, "Flux_Z
 ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>"}
 # DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
 # launch on the 96^3 case divided by its cells) and FP64-pipe activity
-# (profiles/k_flux_x_limiter_96.md, profiles/k_flux_y_limiter_96.md)
 NCU_TRAFFIC_PER_CELL = {"Flux_X_limiter": (76.687360e6 + 11.400192e6) / (96 * 96 * 96),
                         "Flux_Y_limiter": (76.323328e6 + 11.568640e6) / (96 * 96 * 96)}
 NCU_FP64_PIPE_PCT = {"Flux_X_limiter": 87.6, "Flux_Y_limiter": 87.3}

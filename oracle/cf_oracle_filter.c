@@ -29,11 +29,19 @@ static void free5(fields5 f)
 }
 static void copy5(fields5 d, double **src, size_t n)
 {
-    for (int q = 0; q < 5; q++) memcpy(d.v[q], src[q], n * sizeof(double));
+    for (int q = 0; q < 5; q++) {
+        double *dst = d.v[q];
+        const double *s = src[q];
+        #pragma omp parallel for
+        for (size_t x = 0; x < n; x++) dst[x] = s[x];
+    }
 }
 
 /* one x, y and z pass: dst = Z(Y(X(src))), using gx, gy as the
- * intermediate arrays (their out-of-box values are U copies) */
+ * intermediate arrays (their out-of-box values are U copies).  Loops run
+ * variable by variable with k innermost (contiguous, vectorisable); every
+ * value is the reference's expression, so the order of the loops does not
+ * change a bit. */
 static void level(const cfo_grid *g, double *const *src, fields5 gx, fields5 gy, fields5 dst,
                   const double *J, const double *Yp, int wide)
 {
@@ -43,26 +51,35 @@ static void level(const cfo_grid *g, double *const *src, fields5 gx, fields5 gy,
     #pragma omp parallel for collapse(2)
     for (int i = 3; i <= gend; i++)
         for (int j = 2; j <= ny; j++)
-            for (int k = 2; k <= nz; k++) {
-                const size_t q = IX(i, j, k);
-                for (int n = 0; n < 5; n++) {
-                    const double *s = src[n];
-                    gx.v[n][q] = wide ? 0.25 * (s[q - sx] + 2 * s[q] + s[q + sx])
-                                      : 0.125 * (s[q - sx] + 6 * s[q] + s[q + sx]);
-                }
+            for (int n = 0; n < 5; n++) {
+                const double *s = src[n];
+                double *d = gx.v[n];
+                const size_t q0 = IX(i, j, 0);
+                if (wide)
+                    for (int k = 2; k <= nz; k++) {
+                        const size_t q = q0 + k;
+                        d[q] = 0.25 * (s[q - sx] + 2 * s[q] + s[q + sx]);
+                    }
+                else
+                    for (int k = 2; k <= nz; k++) {
+                        const size_t q = q0 + k;
+                        d[q] = 0.125 * (s[q - sx] + 6 * s[q] + s[q + sx]);
+                    }
             }
     /* stretched y pass (Filter.cpp:186-208 / 863-883) */
     #pragma omp parallel for collapse(2)
     for (int i = 3; i <= gend; i++)
         for (int j = 2; j <= ny; j++)
-            for (int k = 2; k <= nz; k++) {
-                const size_t q = IX(i, j, k);
-                double a = Yp[q + sy] - Yp[q - sy];
-                double b = Yp[q + sy] - Yp[q];
-                double c = Yp[q] - Yp[q - sy];
-                for (int n = 0; n < 5; n++) {
-                    const double *G = gx.v[n];
-                    gy.v[n][q] = wide
+            for (int n = 0; n < 5; n++) {
+                const double *G = gx.v[n];
+                double *d = gy.v[n];
+                const size_t q0 = IX(i, j, 0);
+                for (int k = 2; k <= nz; k++) {
+                    const size_t q = q0 + k;
+                    double a = Yp[q + sy] - Yp[q - sy];
+                    double b = Yp[q + sy] - Yp[q];
+                    double c = Yp[q] - Yp[q - sy];
+                    d[q] = wide
                         ? 0.5 * (b / a * G[q - sy] * J[q - sy] + G[q] * J[q] + c / a * G[q + sy] * J[q + sy]) / J[q]
                         : 0.125 * (2 * b / a * G[q - sy] * J[q - sy] + 6 * G[q] * J[q] + 2 * c / a * G[q + sy] * J[q + sy]) / J[q];
                 }
@@ -71,13 +88,20 @@ static void level(const cfo_grid *g, double *const *src, fields5 gx, fields5 gy,
     #pragma omp parallel for collapse(2)
     for (int i = 3; i <= gend; i++)
         for (int j = 2; j <= ny; j++)
-            for (int k = 2; k <= nz; k++) {
-                const size_t q = IX(i, j, k);
-                for (int n = 0; n < 5; n++) {
-                    const double *G = gy.v[n];
-                    dst.v[n][q] = wide ? 0.25 * (G[q - 1] + 2 * G[q] + G[q + 1])
-                                       : 0.125 * (G[q - 1] + 6 * G[q] + G[q + 1]);
-                }
+            for (int n = 0; n < 5; n++) {
+                const double *G = gy.v[n];
+                double *d = dst.v[n];
+                const size_t q0 = IX(i, j, 0);
+                if (wide)
+                    for (int k = 2; k <= nz; k++) {
+                        const size_t q = q0 + k;
+                        d[q] = 0.25 * (G[q - 1] + 2 * G[q] + G[q + 1]);
+                    }
+                else
+                    for (int k = 2; k <= nz; k++) {
+                        const size_t q = q0 + k;
+                        d[q] = 0.125 * (G[q - 1] + 6 * G[q] + G[q + 1]);
+                    }
             }
 }
 
@@ -88,22 +112,28 @@ static void sensor_energy(const cfo_grid *g, double **U, const double *J, const 
     GRID_LOCALS(g);
     static const double wgt[6] = {6, -15, 20, -15, 6, -1};
     fields5 gx = alloc5(n), gy = alloc5(n), l0 = alloc5(n), l1 = alloc5(n), acc = alloc5(n);
-    copy5(gx, U, n); copy5(gy, U, n); copy5(l0, U, n); copy5(l1, U, n); copy5(acc, U, n);
+    /* the reference initialises every temporary to U (Filter.cpp:121-136);
+     * acc is written on the whole interior before it is read and read only
+     * there, so its copy is left out */
+    copy5(gx, U, n); copy5(gy, U, n); copy5(l0, U, n); copy5(l1, U, n);
     fields5 prev = {{U[0], U[1], U[2], U[3], U[4]}};
     fields5 cur = l0, nxt = l1;
     for (int lev = 0; lev < 6; lev++) {
         level(g, prev.v, gx, gy, cur, J, Yp, wide);
+        const double w = wgt[lev];
         #pragma omp parallel for collapse(2)
         for (int i = 3; i <= gend; i++)
             for (int j = 2; j <= ny; j++)
-                for (int k = 2; k <= nz; k++) {
-                    const size_t q = IX(i, j, k);
-                    for (int v = 0; v < 5; v++) {
-                        double x = cur.v[v][q];
-                        if (lev == 0) acc.v[v][q] = 6 * x;
-                        else if (lev == 5) acc.v[v][q] = acc.v[v][q] - x;
-                        else acc.v[v][q] = acc.v[v][q] + wgt[lev] * x;
-                    }
+                for (int v = 0; v < 5; v++) {
+                    const double *x = cur.v[v];
+                    double *s = acc.v[v];
+                    const size_t q0 = IX(i, j, 0);
+                    if (lev == 0)
+                        for (int k = 2; k <= nz; k++) s[q0 + k] = 6 * x[q0 + k];
+                    else if (lev == 5)
+                        for (int k = 2; k <= nz; k++) s[q0 + k] = s[q0 + k] - x[q0 + k];
+                    else
+                        for (int k = 2; k <= nz; k++) s[q0 + k] = s[q0 + k] + w * x[q0 + k];
                 }
         prev = cur;
         fields5 t = cur; cur = nxt; nxt = t;

@@ -367,11 +367,11 @@ void cfo_Flux_X_limiter(const cfo_grid *g, double **a)
     #pragma omp parallel for collapse(2)
     for (int i = 2; i <= gend + 1; i++)
         for (int j = 2; j <= ny; j++)
-            for (int k = 2; k <= nz; k++) {
-                const double jL = J_u[IX(i, j - 1, k - 1)];
-                const double jR = J_u[IX(i - 1, j - 1, k - 1)];
-                for (int n = 0; n < 5; n++) {
-                    const double *U = a[A_U + n];
+            for (int n = 0; n < 5; n++) {
+                const double *U = a[A_U + n];
+                for (int k = 2; k <= nz; k++) {
+                    const double jL = J_u[IX(i, j - 1, k - 1)];
+                    const double jR = J_u[IX(i - 1, j - 1, k - 1)];
                     double *ML = &a[A_ML + n][IX(i, j - 1, k - 1)];
                     double *MR = &a[A_MR + n][IX(i - 1, j - 1, k - 1)];
                     if (i <= 3 || i >= gend)

@@ -56,7 +56,7 @@ def build_port(force: bool = False) -> Path:
             return lib
         BUILD.mkdir(exist_ok=True)
         tmp = BUILD / f"libcforacle.{os.getpid()}.tmp"
-        cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=gnu11",
+        cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=gnu11",
                "-Wall", "-Wno-unused-variable", "-o", str(tmp), *map(str, srcs), "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
