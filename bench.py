@@ -243,6 +243,13 @@ def cpu_rhs_port(g, host, faces):
     return step
 
 
+# the C restatement against the reference's own routine sources built by
+# the oracle recipe, one 128^3 RHS on the same 8 x86 cores (the reference
+# does not build on the Arm GPU host): restatement time / reference time
+PORT_OVER_REFERENCE = {"time_ratio": 0.80, "restatement_s": [1.01, 1.33], "reference_s": [1.26, 1.67],
+                       "where": "x86, 8 threads, 128^3 RHS (Filter + limited fluxes + Viscous_terms)"}
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -325,7 +332,7 @@ def main():
                 "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic", "config": cfg,
                 "cpu_baseline": {"value": value, "unit": "Mcell-updates/s", "cores": cores, "kind": "port",
-                                 "sample": sample},
+                                 "sample": sample, "port_over_reference": PORT_OVER_REFERENCE},
                 "e2e": {"value": value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -432,6 +439,7 @@ def main():
             csteps = 2 if g.cells >= 2_000_000 else 4
             cval, csec = time_cpu(g, host, csteps, 0)
             cpu = {"value": cval, "unit": "Mcell-updates/s", "cores": cpu_threads(), "kind": "port",
+                   "port_over_reference": PORT_OVER_REFERENCE,
                    "sample": f"{csteps} RHS evaluations of the full workload on the host cores "
                              f"(C restatement of the reference routines, OpenMP), {csec:.2f} s each"}
         except Exception as exc:

@@ -38,10 +38,10 @@ static void copy5(fields5 d, double **src, size_t n)
 }
 
 /* one x, y and z pass: dst = Z(Y(X(src))), using gx, gy as the
- * intermediate arrays (their out-of-box values are U copies).  Loops run
- * variable by variable with k innermost (contiguous, vectorisable); every
- * value is the reference's expression, so the order of the loops does not
- * change a bit. */
+ * intermediate arrays (their out-of-box values are U copies).  The x and
+ * z passes run variable by variable with k innermost (contiguous,
+ * vectorisable); every value is the reference's expression, so the order of
+ * the loops does not change a bit. */
 static void level(const cfo_grid *g, double *const *src, fields5 gx, fields5 gy, fields5 dst,
                   const double *J, const double *Yp, int wide)
 {
@@ -66,20 +66,19 @@ static void level(const cfo_grid *g, double *const *src, fields5 gx, fields5 gy,
                         d[q] = 0.125 * (s[q - sx] + 6 * s[q] + s[q + sx]);
                     }
             }
-    /* stretched y pass (Filter.cpp:186-208 / 863-883) */
+    /* stretched y pass (Filter.cpp:186-208 / 863-883): the spacings a, b,
+     * c once per cell for the five variables, as the reference forms them */
     #pragma omp parallel for collapse(2)
     for (int i = 3; i <= gend; i++)
         for (int j = 2; j <= ny; j++)
-            for (int n = 0; n < 5; n++) {
-                const double *G = gx.v[n];
-                double *d = gy.v[n];
-                const size_t q0 = IX(i, j, 0);
-                for (int k = 2; k <= nz; k++) {
-                    const size_t q = q0 + k;
-                    double a = Yp[q + sy] - Yp[q - sy];
-                    double b = Yp[q + sy] - Yp[q];
-                    double c = Yp[q] - Yp[q - sy];
-                    d[q] = wide
+            for (int k = 2; k <= nz; k++) {
+                const size_t q = IX(i, j, k);
+                double a = Yp[q + sy] - Yp[q - sy];
+                double b = Yp[q + sy] - Yp[q];
+                double c = Yp[q] - Yp[q - sy];
+                for (int n = 0; n < 5; n++) {
+                    const double *G = gx.v[n];
+                    gy.v[n][q] = wide
                         ? 0.5 * (b / a * G[q - sy] * J[q - sy] + G[q] * J[q] + c / a * G[q + sy] * J[q + sy]) / J[q]
                         : 0.125 * (2 * b / a * G[q - sy] * J[q - sy] + 6 * G[q] * J[q] + 2 * c / a * G[q + sy] * J[q + sy]) / J[q];
                 }
