@@ -43,21 +43,45 @@ FILTER_ARGS = (0.007, 1.0, 0.0)        # Roe_criterion, E_high, E_low (main.cpp:
 # viscous 36 + 4 arrays of 8 bytes)
 ALG_BYTES = {"Filter": 80, "Flux_X_limiter": 168, "Flux_Y_limiter": 176, "Flux_Z_limiter": 176,
              "Viscous_terms": 320, "Dual_time_stepping": 2680}
-# single-kernel routines eligible as "the dominant kernel" of the roofline
-# (Flux_Z_limiter is three launches: z weights, interior faces, edge faces)
-ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>"}
+# routines eligible as "the dominant kernel" of the roofline: the single
+# launches of Flux_X/Y_limiter and Flux_Z_limiter, whose interior-face
+# launch (the step's longest single launch) is timed together with its two
+# short companions (z weights, edge faces: about 5 % of the routine)
+ROOF_KERNELS = {"Flux_X_limiter": "k_flux<0,true,double>", "Flux_Y_limiter": "k_flux<1,true,double>",
+                "Flux_Z_limiter": "k_flux<2,true,double,ZP=1> (+ k_flux_zweights, k_flux<2,true,double,ZP=2>)"}
 # DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
 # launch on the 96^3 case divided by its cells) and FP64-pipe activity
 NCU_TRAFFIC_PER_CELL = {"Flux_X_limiter": (76.687360e6 + 11.400192e6) / (96 * 96 * 96),
-                        "Flux_Y_limiter": (76.323328e6 + 11.568640e6) / (96 * 96 * 96)}
-NCU_FP64_PIPE_PCT = {"Flux_X_limiter": 87.6, "Flux_Y_limiter": 87.3}
+                        "Flux_Y_limiter": (76.323328e6 + 11.568640e6) / (96 * 96 * 96),
+                        "Flux_Z_limiter": (81.8e6 + 12.1e6) / (96 * 96 * 93)}
+NCU_FP64_PIPE_PCT = {"Flux_X_limiter": 87.6, "Flux_Y_limiter": 87.3, "Flux_Z_limiter": 87.4}
 # floating-point operations per interior cell of the routine's algorithm:
 # the exact count of the oracle's restatement on the seeded 64x48x32 case
 # (tests/golden/flop_counts.json, made by tests/golden/make_flop_counts.py)
-ALG_FLOPS_PER_CELL = {"Flux_X_limiter": 1001.5, "Flux_Y_limiter": 998.3}
+ALG_FLOPS_PER_CELL = {"Flux_X_limiter": 1001.5, "Flux_Y_limiter": 998.3, "Flux_Z_limiter": 1023.7}
 FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (non-tensor), nominal
 LU_SUBITERATIONS = 10   # LU-SGS sub-iterations of one physical step of the fixed-count schedule
 L2_BYTES = 129 * 2 ** 20
+
+
+def fp64_peak(torch, blocks=152 * 8, iters=4096, reps=5):
+    """Measured FP64 rate of this GPU: sixteen independent FMA chains per
+    thread (cf_fp64_peak_probe), CUDA events around `reps` launches after
+    one warm-up; TFLOP/s (an FMA counted as two operations)."""
+    from channel_flow_gb300 import _lib
+    lib = _lib.load()
+    out = torch.zeros(blocks, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    _lib.check(lib, None, lib.cf_fp64_peak_probe(s.cuda_stream, blocks, iters, out.data_ptr()))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        _lib.check(lib, None, lib.cf_fp64_peak_probe(s.cuda_stream, blocks, iters, out.data_ptr()))
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return 2.0 * 16 * 256 * iters * blocks / (ms * 1e-3) / 1e12, ms
 
 
 def peaks():
@@ -398,6 +422,11 @@ def main():
     # roofline of the dominant single kernel (the slowest limited flux) with
     # the byte model; traffic = ncu DRAM bytes per cell x cells
     hbm, peak_kind = peaks()
+    try:
+        fp64_pk, fp64_ms = fp64_peak(torch)
+        fp64_kind = f"measured: FP64 FMA chains (cf_fp64_peak_probe), {fp64_ms:.2f} ms per launch"
+    except Exception as exc:   # reported, with the nominal figure in its place
+        fp64_pk, fp64_kind = FP64_NOMINAL_TFLOPS, f"nominal (probe failed: {exc})"
     dom = max(ROOF_KERNELS, key=lambda nm: per_routine[nm])
     achieved = ALG_BYTES[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e9
     traffic = NCU_TRAFFIC_PER_CELL.get(dom)
@@ -409,14 +438,13 @@ def main():
             "fp64_pipe_active_pct": NCU_FP64_PIPE_PCT.get(dom),
             "fp64": {"alg_flops_per_cell": ALG_FLOPS_PER_CELL[dom],
                      "achieved_tflops": ALG_FLOPS_PER_CELL[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e12,
-                     "peak_tflops": FP64_NOMINAL_TFLOPS, "peak_kind": "nominal",
-                     "frac": ALG_FLOPS_PER_CELL[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e12
-                     / FP64_NOMINAL_TFLOPS},
+                     "peak_tflops": fp64_pk, "peak_kind": fp64_kind, "nominal_tflops": FP64_NOMINAL_TFLOPS,
+                     "frac": ALG_FLOPS_PER_CELL[dom] * g.cells / (per_routine[dom] * 1e-3) / 1e12 / fp64_pk},
             "per_routine_ms": {k: round(v, 4) for k, v in per_routine.items()},
             "note": "FP64 on GB300 (1/64 of FP32 rate) is FP64-pipe bound (ncu: 84-88% pipe busy, "
                     "DRAM 1%): fp64.frac (the oracle's exact flop count per cell over the launch time, "
-                    "against the nominal FP64 peak) is the binding roofline; the HBM fraction is the "
-                    "byte-model figure"}
+                    "against the FP64 rate measured in this run by FMA chains) is the binding roofline; "
+                    "the HBM fraction is the byte-model figure"}
 
     # secondary measurements on the same workload: FP32 kernels, and one
     # dual-time pseudo-iteration (RHS + hyperplane LU-SGS) per precision

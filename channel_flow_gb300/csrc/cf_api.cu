@@ -145,6 +145,26 @@ __global__ void k_count_nonfinite(cf_dims d, const double *f, unsigned long long
     if (!isfinite(v)) atomicAdd(bad, 1ull);
 }
 
+// FP64 rate probe: sixteen independent FMA chains per thread, the loop
+// unrolled four times, so the FP64 pipe, not the FMA latency or the loop
+// control, bounds the kernel; the sum keeps the chains live.  a < 1 and b
+// small keep every value bounded.
+constexpr int CF_PROBE_CHAINS = 16;
+__global__ void __launch_bounds__(256) k_fp64_fma_chains(int iters, double a, double b, double *out)
+{
+    double x[CF_PROBE_CHAINS];
+#pragma unroll
+    for (int c = 0; c < CF_PROBE_CHAINS; c++) x[c] = 1e-3 * (threadIdx.x + c);
+#pragma unroll 4
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+        for (int c = 0; c < CF_PROBE_CHAINS; c++) x[c] = fma(x[c], a, b);
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < CF_PROBE_CHAINS; c++) s += x[c];
+    if (s == 12345.678) out[blockIdx.x] = s;   // never true; keeps the chains
+}
+
 inline bool exact(const cf_ctx *c) { return c->prec == CF_PREC_FP64_EXACT; }
 inline int kprec(const cf_ctx *c) { return c->prec == CF_PREC_FP32 ? 1 : 0; }
 
@@ -154,6 +174,13 @@ inline int kprec(const cf_ctx *c) { return c->prec == CF_PREC_FP32 ? 1 : 0; }
 extern "C" {
 
 int cf_library_version(void) { return CF_VERSION; }
+
+int cf_fp64_peak_probe(void *stream, int blocks, int iters, double *scratch_dev)
+{
+    if (blocks <= 0 || iters <= 0 || !scratch_dev) return CF_ERR_ARG;
+    k_fp64_fma_chains<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(iters, 0.9999999, 1e-9, scratch_dev);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
 
 const char *cf_error_string(int code)
 {

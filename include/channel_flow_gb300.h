@@ -121,6 +121,12 @@ const char *cf_last_error(const cf_ctx *ctx);
 const char *cf_error_string(int code);
 size_t cf_field_count(const cf_ctx *ctx); /* doubles per field: X_np*Y_m*Z_m */
 int cf_library_version(void);
+/* Measurement helper (no counterpart in the reference): FP64 rate probe.
+ * Launches `blocks` blocks of 256 threads, each running sixteen independent
+ * chains of `iters` FP64 fused multiply-adds (2 * 16 * 256 * iters * blocks
+ * floating-point operations), on cuda_stream; time it with events around
+ * the call.  scratch_dev: `blocks` doubles the kernel may write. */
+int cf_fp64_peak_probe(void *cuda_stream, int blocks, int iters, double *scratch_dev);
 
 /* ------------------------------------------------------------------ */
 /* host arrays and device mirrors                                        */
