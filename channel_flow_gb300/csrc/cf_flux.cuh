@@ -654,6 +654,103 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_flux(cf_dims d,
     }
 }
 
+#ifdef CF_WITH_FLOAT
+// FP32 x faces marching along x.  Each thread owns one (j, k) face column
+// of the box and walks a chunk of its x faces in order, keeping the six
+// cells i-2..i+3 of the current face's stencil for each variable in
+// registers: one new cell per variable and face instead of six, and the
+// next face's cell, metrics and sensor requested before the current face
+// is evaluated, so the loads of one face overlap the arithmetic of the
+// previous one.  (One thread per face reads six cells one x plane apart,
+// which L1 never reuses; those faces wait on L2.)  The arithmetic is
+// fast_states_x_limited / fast_lin_pair on the same values, so the fluxes
+// equal the per-face kernel's bit for bit.
+template <bool LIMITED>
+__global__ void __launch_bounds__(256, 3) k_flux_x_march(cf_dims d, cf_flux_args_f a, cf_box b, int chunk)
+{
+    const int k = b.k0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = b.j0 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (k >= b.k0 + b.nk || j >= b.j0 + b.nj) return;
+    const int ia = b.i0 + (int)blockIdx.z * chunk;
+    const int ib = min(ia + chunk, b.i0 + b.ni);
+    if (ia >= ib) return;
+    const ptrdiff_t s = (ptrdiff_t)d.plane();
+    const int f32 = a.f32_out;
+    // window: cells ia-2 .. ia+3 of row (j+1, k+1)
+    float u[5][6];
+    const size_t c0 = d.ix(ia, j + 1, k + 1);
+#pragma unroll
+    for (int n = 0; n < 5; n++)
+#pragma unroll
+        for (int t = 0; t < 6; t++) u[n][t] = a.U[n][c0 + (t - 2) * s];
+    float iJw[6];
+    if (!LIMITED) {
+#pragma unroll
+        for (int t = 0; t < 6; t++) iJw[t] = frcp<float>(a.J[c0 + (t - 2) * s]);
+    }
+    for (int i = ia; i < ib; i++) {
+        const size_t q = d.ix(i, j, k);
+        float m[9], mL[5], mR[5], F[6];
+#pragma unroll
+        for (int n = 0; n < 9; n++) m[n] = fmet<float>(a, n, q);
+        const float jf = fjf<float>(a, q);
+        const float ep = LIMITED ? float(a.Ep[q]) : 0.f;
+        // next face's new cell (i+4), requested before this face's arithmetic
+        float nx[5], nj = 0.f;
+        const bool more = i + 1 < ib;
+        const size_t cn = d.ix(i + 4, j + 1, k + 1);
+#pragma unroll
+        for (int n = 0; n < 5; n++) nx[n] = more ? a.U[n][cn] : 0.f;
+        if (!LIMITED && more) nj = a.J[cn];
+        if (LIMITED) {
+            const bool lo3 = (i <= 3) || (i >= d.gend);
+            const bool hi3 = (i + 1 <= 3) || (i + 1 >= d.gend);
+#pragma unroll
+            for (int n = 0; n < 5; n++) fast_pair<float, 1>(u[n], lo3, hi3, jf, jf, mL[n], mR[n]);
+            fast_flux_precond_roe<float>(mL, mR, m, 0, ep, jf, CF_DC(float, d, K), CF_DC(float, d, e), F);
+        } else {
+            if (i <= 3 || i >= d.gend - 1) {
+                states_x_linear<float>(d, a, i, j, k, mL, mR);
+            } else {
+                const float tl = frcp<float>(2.f * iJw[0] - 13.f * iJw[1] + 47.f * iJw[2] + 27.f * iJw[3] - 3.f * iJw[4]);
+                const float tr = frcp<float>(-3.f * iJw[1] + 27.f * iJw[2] + 47.f * iJw[3] - 13.f * iJw[4] + 2.f * iJw[5]);
+#pragma unroll
+                for (int n = 0; n < 5; n++) {
+                    const float *w = u[n];
+                    mL[n] = tl * (2.f * w[0] - 13.f * w[1] + 47.f * w[2] + 27.f * w[3] - 3.f * w[4]);
+                    mR[n] = tr * (-3.f * w[1] + 27.f * w[2] + 47.f * w[3] - 13.f * w[4] + 2.f * w[5]);
+                }
+            }
+            fast_flux_roe<float>(mL, mR, m, 0, jf, CF_DC(float, d, K), F);
+        }
+#pragma unroll
+        for (int n = 0; n < 5; n++) rhs_put<float>(a.F[n], q, F[n], f32);
+#pragma unroll
+        for (int n = 0; n < 5; n++) {
+#pragma unroll
+            for (int t = 0; t < 5; t++) u[n][t] = u[n][t + 1];
+            u[n][5] = nx[n];
+        }
+        if (!LIMITED) {
+#pragma unroll
+            for (int t = 0; t < 5; t++) iJw[t] = iJw[t + 1];
+            iJw[5] = more ? frcp<float>(nj) : 0.f;
+        }
+    }
+}
+
+// chunk of x faces per block: enough blocks for four per SM
+inline int flux_x_chunk(const cf_box &b)
+{
+    const long long cols = (long long)((b.nk + 31) / 32) * ((b.nj + 7) / 8);
+    const long long want = 152LL * 8;
+    long long nch = (want + cols - 1) / cols;
+    if (nch < 1) nch = 1;
+    int chunk = (int)((b.ni + nch - 1) / nch);
+    return chunk < 8 ? 8 : chunk;
+}
+#endif
+
 // face boxes of the reference's flux loops
 static inline cf_box flux_box(const cf_dims &d, int dir)
 {
@@ -778,13 +875,15 @@ inline cudaError_t launch_flux_f32(const cf_dims &d, const cf_flux_args &a, floa
     dim3 g = box_grid(b), t = box_block();
     if (dir == 2)
         return limited ? launch_flux_z<true, float>(d, fa, b, s) : launch_flux_z<false, float>(d, fa, b, s);
-    if (limited) {
-        if (dir == 0) k_flux<0, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-        else k_flux<1, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-    } else {
-        if (dir == 0) k_flux<0, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
-        else k_flux<1, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+    if (dir == 0) {
+        const int chunk = flux_x_chunk(b);
+        const dim3 gx = dim3(g.x, g.y, (unsigned)((b.ni + chunk - 1) / chunk));
+        if (limited) k_flux_x_march<true><<<gx, t, 0, s>>>(d, fa, b, chunk);
+        else k_flux_x_march<false><<<gx, t, 0, s>>>(d, fa, b, chunk);
+        return cudaGetLastError();
     }
+    if (limited) k_flux<1, true, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
+    else k_flux<1, false, float, cf_flux_args_f><<<g, t, 0, s>>>(d, fa, b);
     return cudaGetLastError();
 }
 #endif
