@@ -320,13 +320,14 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess physical-step comparison")
     ap.add_argument("--no-wavy", action="store_true", help="skip the 512x256x384 wavy-wall measurement")
-    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs", "mlp", "physical", "northstar"],
+    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs", "mlp", "physical", "northstar", "guess"],
                     help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
                          "(one LU-SGS pseudo-iteration per step, for profiling); mlp: the learned guess's "
                          "tensor-core GEMMs on --mlp-rows feature rows; physical: whole physical steps "
                          "(cf_step, sub-iterations to the 1e-6 tolerance, extrapolated start) of the "
                          "configuration 2/3 physics, for profiling; northstar: the FP64 against mixed+learned "
-                         "physical-step comparison alone")
+                         "physical-step comparison alone; guess: the learned guess's kernels on --grid after a "
+                         "short harvest, for profiling")
     ap.add_argument("--mlp-rows", type=int, default=2097152, help="rows (cells) of the --step mlp GEMMs")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
@@ -370,6 +371,21 @@ def main():
         r = mlp_gemms(torch, args.mlp_rows, max(2, args.steps), max(1, args.warmup))
         if rank == 0:
             print(json.dumps(r))
+        return 0
+    if args.step == "guess":
+        torch.cuda.set_device(local)
+        from channel_flow_gb300 import mlp, stepper
+        g, ctx, w, dt = northstar_case(torch, dims, "fp32")
+        st = stepper.Stepper(ctx, stepper.fields_from_workload(w, torch, g), deltaT=dt, **NS_STEP)
+        hist = [[u.clone() for u in st.f["U"]]]
+        for _ in range(5):
+            st.step(None)
+            hist.append([u.clone() for u in st.f["U"]])
+        net = mlp.LearnedGuess(capacity=g.cells, seed=0, lr=2e-3, batch=min(g.cells, 131072))
+        net.train(g, hist, epochs=2, batch=min(g.cells, 131072))
+        r = guess_breakdown(torch, net, g, hist[-3:], st.f["U_"], reps=max(1, args.steps))
+        ctx.close()
+        print(json.dumps({"step": "guess", "grid": list(dims), "ms": r}))
         return 0
     if args.step == "northstar":
         torch.cuda.set_device(local)

@@ -363,42 +363,46 @@ __global__ void __launch_bounds__(256) k_mlp_diffs(size_t N, mlp_levels L, float
 }
 
 constexpr int MLP_FROWS = 32;                 // rows per block
-constexpr int MLP_FPAIRS = MLP_K1 / 2;        // 160 column pairs (32-bit words) per row
-constexpr int MLP_FSTRIDE = MLP_FPAIRS + 1;   // padded row stride in words: lanes hit distinct banks
+constexpr int MLP_FPAIRS = MLP_K1 / 2;        // 160 32-bit words per row
+constexpr int MLP_FSTRIDE = MLP_K1 + 2;       // padded row stride in bf16: 161 words, lanes hit distinct banks
+constexpr int MLP_FWARPS = 10;                // one warp per (kind, variable)
 
-__global__ void __launch_bounds__(256) k_mlp_features_grid(mlp_grid g, size_t N, const float *__restrict__ D,
-                                                           const float *scale, long long M, long long Mpad,
-                                                           uint32_t *Xw)
+// Ten warps per block, warp w gathering the 27 stencil columns of kind
+// l = w / 5, variable v = w % 5 for the block's 32 rows (one lane per row),
+// the stencil offsets unrolled as constants; each warp also clears five of
+// the fifty padding columns.
+__global__ void __launch_bounds__(32 * MLP_FWARPS) k_mlp_features_grid(mlp_grid g, size_t N, const float *__restrict__ D,
+                                                                      const float *scale, long long M, long long Mpad,
+                                                                      uint32_t *Xw)
 {
-    __shared__ uint32_t tile[MLP_FROWS * MLP_FSTRIDE];
-    __shared__ float inv[10];
+    __shared__ __align__(16) __nv_bfloat16 tile[MLP_FROWS * MLP_FSTRIDE];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 10) inv[threadIdx.x] = 1.0f / scale[threadIdx.x];
-    __syncthreads();
     const long long r0 = (long long)blockIdx.x * MLP_FROWS;
     const long long r = r0 + lane;
     const bool live = r < M;
-    const size_t q = live ? g.cell(r) : 0;
-    const ptrdiff_t sx = (ptrdiff_t)g.Ym() * g.Zm(), sy = g.Zm();
-    for (int pr = warp; pr < MLP_FPAIRS; pr += 8) {
-        float f[2] = {0.f, 0.f};
+    const int l = warp / 5, v = warp % 5;
+    const float inv = 1.0f / scale[5 * l + v];
+    __nv_bfloat16 *row = tile + lane * MLP_FSTRIDE + 135 * l + 27 * v;
+    if (live) {
+        const ptrdiff_t sx = (ptrdiff_t)g.Ym() * g.Zm(), sy = g.Zm();
+        const float *src = D + (size_t)(5 * l + v) * N + g.cell(r);
 #pragma unroll
-        for (int e = 0; e < 2; e++) {
-            const int c = 2 * pr + e;
-            if (live && c < MLP_IN) {
-                const int l = c / 135, rem = c % 135, v = rem / 27, st = rem % 27;
-                const ptrdiff_t p = (ptrdiff_t)q + (st / 9 - 1) * sx + ((st / 3) % 3 - 1) * sy + (st % 3 - 1);
-                f[e] = D[(size_t)(5 * l + v) * N + (size_t)p] * inv[5 * l + v];
-            }
+        for (int st = 0; st < 27; st++) {
+            const ptrdiff_t off = (st / 9 - 1) * sx + ((st / 3) % 3 - 1) * sy + (st % 3 - 1);
+            row[st] = __float2bfloat16(src[off] * inv);
         }
-        __nv_bfloat162 h = __floats2bfloat162_rn(f[0], f[1]);
-        tile[lane * MLP_FSTRIDE + pr] = *reinterpret_cast<uint32_t *>(&h);
+    } else {
+#pragma unroll
+        for (int st = 0; st < 27; st++) row[st] = __float2bfloat16(0.f);
     }
+#pragma unroll
+    for (int e = 0; e < 5; e++) tile[lane * MLP_FSTRIDE + MLP_IN + 5 * warp + e] = __float2bfloat16(0.f);
     __syncthreads();
     const long long rows = Mpad - r0 < MLP_FROWS ? Mpad - r0 : MLP_FROWS;
+    const uint32_t *t32 = reinterpret_cast<const uint32_t *>(tile);
     for (int w = threadIdx.x; w < rows * MLP_FPAIRS; w += blockDim.x) {
         const int rr = w / MLP_FPAIRS, pr = w % MLP_FPAIRS;
-        Xw[(size_t)r0 * MLP_FPAIRS + w] = tile[rr * MLP_FSTRIDE + pr];
+        Xw[(size_t)r0 * MLP_FPAIRS + w] = t32[rr * (MLP_FSTRIDE / 2) + pr];
     }
 }
 
@@ -516,15 +520,20 @@ __global__ void k_mlp_base_sums(mlp_grid g, mlp_levels20 L, long long M, double 
 }
 
 // the feature scales on the device (no host round trip): scale[y] =
-// sqrt(sum over the nb partial sums of row y / M), 1 where that is 0
+// sqrt(sum over the nb partial sums of row y / M), 1 where that is 0; one
+// warp per row, lane-strided sums and a shuffle tree
 __global__ void k_mlp_scale_finish(const double *partial, int nb, long long M, float *scale)
 {
-    const int y = threadIdx.x;
+    const int y = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (y >= 10) return;
     double t = 0;
-    for (int b = 0; b < nb; b++) t += partial[(size_t)y * nb + b];
-    const double r = sqrt(t / (double)M);
-    scale[y] = r > 0 ? (float)r : 1.0f;
+    for (int b = lane; b < nb; b += 32) t += partial[(size_t)y * nb + b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) {
+        const double r = sqrt(t / (double)M);
+        scale[y] = r > 0 ? (float)r : 1.0f;
+    }
 }
 
 // per-block sums over rows of T.Y, Y.Y and T.T for each of the 5 outputs
@@ -746,8 +755,8 @@ int cf_mlp_features_grid(void *stream, int X, int Y, int Z, const double *const 
     const size_t N = (size_t)(X + 6) * g.Ym() * g.Zm();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     k_mlp_diffs<<<nblk((long long)N, 256), 256, 0, s>>>(N, levels(levels15), diff_scratch);
-    k_mlp_features_grid<<<nblk(Mpad, MLP_FROWS), 256, 0, s>>>(g, N, diff_scratch, scale, M, Mpad,
-                                                               static_cast<uint32_t *>(Xout));
+    k_mlp_features_grid<<<nblk(Mpad, MLP_FROWS), 32 * MLP_FWARPS, 0, s>>>(g, N, diff_scratch, scale, M, Mpad,
+                                                                          static_cast<uint32_t *>(Xout));
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
@@ -867,7 +876,7 @@ int cf_mlp_scale(void *stream, int X, int Y, int Z, const double *const *lv, dou
     const long long M = (long long)X * Y * Z;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     k_mlp_sq_partial<1><<<dim3((unsigned)nblocks, 10), 256, 0, s>>>(g, L, M, partial_dev);
-    k_mlp_scale_finish<<<1, 32, 0, s>>>(partial_dev, nblocks, M, scale10_dev);
+    k_mlp_scale_finish<<<1, 320, 0, s>>>(partial_dev, nblocks, M, scale10_dev);
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 

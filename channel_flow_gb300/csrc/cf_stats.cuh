@@ -216,13 +216,24 @@ __device__ __forceinline__ double st_shear(const cf_dims &d, const cf_stat_args 
 #endif
 }
 
-// Jsum = sum over j of 1/J[3][j][3] in the reference's order (Driven_force.cpp:38-42)
-__global__ void k_bulk_jsum(cf_dims d, const double *J, double *jsum)
+// Jsum = sum over j of 1/J[3][j][3] in the reference's order (Driven_force.cpp:38-42):
+// the quotients in parallel, then one thread adds them in order (one block
+// of 256 threads, rows in chunks of 256)
+__global__ void __launch_bounds__(256) k_bulk_jsum(cf_dims d, const double *J, double *jsum)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    __shared__ double q[256];
     double s = 0;
-    for (int j = 2; j <= d.ny; j++) s = s + 1. / J[d.ix(3, j, 3)];
-    *jsum = s;
+    for (int j0 = 2; j0 <= d.ny; j0 += 256) {
+        const int j = j0 + (int)threadIdx.x;
+        if (j <= d.ny) q[threadIdx.x] = 1. / J[d.ix(3, j, 3)];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int n = min(256, d.ny - j0 + 1);
+            for (int t = 0; t < n; t++) s = s + q[t];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *jsum = s;
 }
 
 // Partial row sums: block (r, c) sums the elements of row r in i-chunk c.

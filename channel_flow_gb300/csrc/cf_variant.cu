@@ -322,7 +322,7 @@ cudaError_t statistic(const cf_dims &d, const cf_stat_args &a, double *acc, doub
 cudaError_t bulk_rows(const cf_dims &d, const double *U2, const double *J, double *jsum_dev, double *rows,
                       double *partial, size_t partial_len, cudaStream_t s)
 {
-    k_bulk_jsum<<<1, 32, 0, s>>>(d, J, jsum_dev);
+    k_bulk_jsum<<<1, 256, 0, s>>>(d, J, jsum_dev);
     cf_stat_args a{};
     a.U[1] = U2;
     a.J = J;
