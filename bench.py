@@ -621,14 +621,19 @@ def northstar_case(torch, dims, precision):
 
 def physical_steps(torch, g, precision, steps, warmup):
     """`warmup` then `steps` timed physical steps (cf_step to the tolerance
-    1e-6 from the extrapolated start) of the configuration 2/3 physics on
-    grid g: CUDA event time per step and per sub-iteration."""
+    1e-6 from the extrapolated start, Statistic every step) of the
+    configuration 2/3 physics on grid g: CUDA event time per step and per
+    sub-iteration.  The timed steps are bracketed by cudaProfilerStart/Stop."""
     from channel_flow_gb300 import stepper
     g, ctx, w, dt = northstar_case(torch, (g.X_out, g.Y_out, g.Z_out), precision)
     st = stepper.Stepper(ctx, stepper.fields_from_workload(w, torch, g), deltaT=dt, **NS_STEP)
+    st.kw["statistic_step"] = 1 << 30          # Statistic accumulates every step, as in the comparison
     for n in range(max(warmup, 3)):
         st.step("extrapolate" if n >= 2 else None)
     its, ms = [], []
+    # the timed steps alone for a profiler started with --profile-from-start off
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
     for _ in range(steps):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -638,6 +643,7 @@ def physical_steps(torch, g, precision, steps, warmup):
         torch.cuda.synchronize()
         its.append(it)
         ms.append(e0.elapsed_time(e1))
+    torch.cuda.cudart().cudaProfilerStop()
     ctx.close()
     return {"step": "physical", "grid": [g.X_out, g.Y_out, g.Z_out], "precision": precision,
             "subiterations": its, "ms_per_step": ms, "ms_per_subiteration": sum(ms) / max(1, sum(its))}
