@@ -212,6 +212,15 @@ class Context:
     def download(self, host: np.ndarray):
         self._ok(self.lib.cf_download(self.h, host.ctypes.data))
 
+    def upload_async(self, host: np.ndarray, stream):
+        """Queue the upload of a registered (pinned) host array on `stream`."""
+        self._ok(self.lib.cf_upload_async(self.h, host.ctypes.data, stream if isinstance(stream, int) else int(stream)))
+
+    def download_async(self, host: np.ndarray, stream):
+        """Queue the download into a registered (pinned) host array on `stream`."""
+        self._ok(self.lib.cf_download_async(self.h, host.ctypes.data,
+                                            stream if isinstance(stream, int) else int(stream)))
+
     @property
     def field_count(self) -> int:
         return int(self.lib.cf_field_count(self.h))

@@ -85,6 +85,8 @@ _SIGS = {
     "cf_upload": ([P, P], C.c_int),
     "cf_download": ([P, P], C.c_int),
     "cf_device_ptr": ([P, P], P),
+    "cf_upload_async": ([P, P, P], C.c_int),
+    "cf_download_async": ([P, P, P], C.c_int),
     "cf_check_finite": ([P, P], C.c_int),
     "cf_Y_boundary_condition": ([P, C.c_int] + [P] * 6, C.c_int),
     "cf_Z_boundary_condition": ([P, C.c_int] + [P] * 6, C.c_int),

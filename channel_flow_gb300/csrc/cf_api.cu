@@ -380,6 +380,24 @@ int cf_download(cf_ctx *c, double *host)
     return cuda_check(c, cudaStreamSynchronize(c->stream), "cf_download sync");
 }
 
+int cf_upload_async(cf_ctx *c, const double *host, void *stream)
+{
+    if (!c) return CF_ERR_ARG;
+    auto it = c->mirrors.find(host);
+    if (it == c->mirrors.end()) return fail(c, CF_ERR_ARG, "cf_upload_async: pointer not registered");
+    return cuda_check(c, cudaMemcpyAsync(it->second, host, c->d.total() * sizeof(double), cudaMemcpyHostToDevice,
+                                         (cudaStream_t)stream), "cf_upload_async");
+}
+
+int cf_download_async(cf_ctx *c, double *host, void *stream)
+{
+    if (!c) return CF_ERR_ARG;
+    auto it = c->mirrors.find(host);
+    if (it == c->mirrors.end()) return fail(c, CF_ERR_ARG, "cf_download_async: pointer not registered");
+    return cuda_check(c, cudaMemcpyAsync(host, it->second, c->d.total() * sizeof(double), cudaMemcpyDeviceToHost,
+                                         (cudaStream_t)stream), "cf_download_async");
+}
+
 double *cf_device_ptr(cf_ctx *c, const double *p) { return c ? R(c, p) : nullptr; }
 
 int cf_check_finite(cf_ctx *c, const double *field)

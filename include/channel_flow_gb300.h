@@ -136,6 +136,13 @@ int cf_unregister(cf_ctx *ctx, double *host);
 int cf_upload(cf_ctx *ctx, const double *host);
 int cf_download(cf_ctx *ctx, double *host);
 double *cf_device_ptr(cf_ctx *ctx, const double *host_or_device);
+/* The same copies queued on cuda_stream (cudaStream_t, NULL = legacy
+ * default) without waiting for them: with pinned host arrays a caller can
+ * overlap the copies of one step with the routines of another, ordering
+ * the two streams with CUDA events.  The host array must stay untouched
+ * until the copy has completed. */
+int cf_upload_async(cf_ctx *ctx, const double *host, void *cuda_stream);
+int cf_download_async(cf_ctx *ctx, double *host, void *cuda_stream);
 
 /* 0 if every interior value of the field is finite, else CF_ERR_NONFINITE
  * (synchronises the stream). */

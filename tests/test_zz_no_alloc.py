@@ -8,7 +8,8 @@ whole device - use the entry point without a context, whose only scratch is
 a fixed file-scope device array.  Two calls in a row, on different inputs,
 must give what the existing entry point gives (the scratch keeps the
 previous call's contents, so the second call checks that nothing stale is
-read), and a grid larger than the array allows must be refused.
+read) and what the C oracle gives, bit for bit, and a grid larger than the
+array allows must be refused.
 
 This file is named so that pytest collects it last.
 """
@@ -50,6 +51,30 @@ def test_noalloc_dplusgs_matches_context_entry_point(cuda_lib):
             np.testing.assert_allclose(er_got, er_want, rtol=RTOL, atol=0)
     finally:
         ctx.close()
+
+
+def test_noalloc_dplusgs_equals_oracle_bit_for_bit(port, cuda_lib):
+    """The entry point is compiled without FMA contraction, like the exact
+    build: every written array equals the C oracle's DPLUSGS (the
+    defined-index restatement of the reference's) bit for bit; the residual
+    norms, summed in another order, agree to 1e-12."""
+    import torch
+    import channel_flow_gb300 as cf
+
+    r = routines.BY_NAME["DPLUSGS"]
+    for dims in (cases.GRIDS[0], cases.GRIDS[2]):
+        g = cases.grid(dims)
+        for seed in (5, 31):                      # two calls in a row per grid
+            a = cases.dt_case(g, seed)
+            want = cases.copy_case(a)
+            er_want = routines.run_cpu(port, r, g, want)
+            got = _to_dev(a)
+            er_got = cf.dplusgs_noalloc(g, cases.DELTA_T, *got)
+            torch.cuda.synchronize()
+            host = [x.cpu().numpy() for x in got]
+            diff = routines.compare(r, g, host, want)
+            assert all(v == 0 for v in diff.values()), f"{dims} seed {seed}: differing entries per slot {diff}"
+            np.testing.assert_allclose(er_got, er_want, rtol=RTOL, atol=0)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(cuda_lib):
