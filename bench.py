@@ -320,15 +320,23 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the 256x192x192 secondary measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess physical-step comparison")
     ap.add_argument("--no-wavy", action="store_true", help="skip the 512x256x384 wavy-wall measurement")
-    ap.add_argument("--step", default="rhs", choices=["rhs", "lusgs", "mlp", "physical", "northstar", "guess"],
+    ap.add_argument("--step", default="rhs",
+                    choices=["rhs", "lusgs", "mlp", "physical", "northstar", "guess", "schedule"],
                     help="rhs: the benchmark (one RHS per step); lusgs: time Dual_time_stepping alone "
                          "(one LU-SGS pseudo-iteration per step, for profiling); mlp: the learned guess's "
                          "tensor-core GEMMs on --mlp-rows feature rows; physical: whole physical steps "
                          "(cf_step, sub-iterations to the 1e-6 tolerance, extrapolated start) of the "
                          "configuration 2/3 physics, for profiling; northstar: the FP64 against mixed+learned "
                          "physical-step comparison alone; guess: the learned guess's kernels on --grid after a "
-                         "short harvest, for profiling")
+                         "short harvest, for profiling; schedule: a configuration's fixed schedule (--config) "
+                         "in FP64 and FP32 with the profiles compared")
     ap.add_argument("--mlp-rows", type=int, default=2097152, help="rows (cells) of the --step mlp GEMMs")
+    ap.add_argument("--config", default="0", choices=sorted(SCHEDULES),
+                    help="--step schedule: which configuration's fixed schedule to run")
+    ap.add_argument("--schedule-steps", type=int, default=0, help="--step schedule: steps (0 = the configuration's)")
+    ap.add_argument("--compare-steps", type=int, default=0,
+                    help="--step schedule: run FP64 for this many steps only and compare there (0 = all)")
+    ap.add_argument("--dt-factor", type=float, default=1.0, help="--step schedule: time step / (0.005 h/U_b)")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
 
@@ -386,6 +394,13 @@ def main():
         r = guess_breakdown(torch, net, g, hist[-3:], st.f["U_"], reps=max(1, args.steps))
         ctx.close()
         print(json.dumps({"step": "guess", "grid": list(dims), "ms": r}))
+        return 0
+    if args.step == "schedule":
+        torch.cuda.set_device(local)
+        r = schedule_run(torch, args.config, steps=args.schedule_steps or None,
+                         compare_steps=args.compare_steps or None, dt_factor=args.dt_factor)
+        if rank == 0:
+            print(json.dumps({"step": "schedule", **r}))
         return 0
     if args.step == "northstar":
         torch.cuda.set_device(local)
@@ -649,6 +664,112 @@ def physical_steps(torch, g, precision, steps, warmup):
             "subiterations": its, "ms_per_step": ms, "ms_per_subiteration": sum(ms) / max(1, sum(its))}
 
 
+# The configurations' fixed schedules: 10 LU-SGS sub-iterations per step
+# (the tolerance test never met), limited MUSCL-5 + Roe with the consistent
+# face-state scaling and the Filter at every sub-iteration, Mach 0.5,
+# seeded laminar state with wall-damped +-5 % velocity noise; Statistic
+# accumulates every step.  Config 4 has the wavy lower wall (0.05 h, wavelength
+# pi h) with the metrics of cf_wavy_metrics.
+SCHEDULES = {
+    "0": {"dims": (64, 64, 64), "re": 2800.0, "wavy": False, "steps": 100},
+    "2": {"dims": (256, 192, 192), "re": 5600.0, "wavy": False, "steps": 1000},
+    "4": {"dims": (512, 256, 384), "re": 11000.0, "wavy": True, "steps": 500},
+}
+
+
+def schedule_case(torch, key, precision, dt_factor):
+    """Context (consistent scheme), device workload and time step of
+    schedule `key`."""
+    import channel_flow_gb300 as cf
+    from channel_flow_gb300 import synthetic as syn
+    spec = SCHEDULES[key]
+    g = syn.channel_physics(syn.channel_grid(*spec["dims"]), 0.5, spec["re"])
+    ctx = cf.Context(g, precision=precision, gamma=GAMMA, scheme="consistent")
+    if spec["wavy"]:
+        w, _ = wavy_workload(ctx, g, torch, wall_damped=True)
+    else:
+        cm = syn.flat_metrics(g, GAMMA, "cell")
+        host = {"U": syn.channel_state(g, cm["J"], seed=SEED, mach=0.5, noise=0.05, jitter=0.01, gamma=GAMMA,
+                                       wall_damped=True),
+                "J": cm["J"], "cm": [cm[n] for n in syn.METRIC_NAMES], "Yp": syn.y_points(g, gamma=GAMMA)}
+        w = DeviceWorkload(ctx, g, host, torch)
+        del host
+    return g, ctx, w, syn.time_step(g, 0.5) * dt_factor
+
+
+def schedule_run(torch, key, steps=None, compare_steps=None, precisions=("fp64", "fp32"), dt_factor=1.0):
+    """Run schedule `key` for `steps` physical steps per precision (the
+    FP64 run for `compare_steps` only, when given): CUDA-event time per
+    step, and at the FP64 run's last step the FP32 run's mean-velocity and
+    Reynolds-stress profiles and state against the FP64 run's (the FP64 GPU
+    path is the FP64 oracle: it equals the C restatement to 1e-12 per
+    routine and bit for bit in its no-FMA build)."""
+    import tempfile
+    from channel_flow_gb300 import stepper
+    spec = SCHEDULES[key]
+    steps = steps or spec["steps"]
+    out = {"config": key, "grid": list(spec["dims"]), "re_bulk_2h": spec["re"], "mach": 0.5,
+           "wavy_wall": spec["wavy"], "subiterations_per_step": LU_SUBITERATIONS, "dt_factor": dt_factor,
+           "scheme": "limited MUSCL-5 + Roe (consistent face-state scaling), Viscous_terms, Filter every "
+                     "sub-iteration, Dual_time_stepping; Statistic every step"}
+    ref = None
+    for prec in precisions:
+        n_steps = compare_steps if (prec == "fp64" and compare_steps) else steps
+        g, ctx, w, dt = schedule_case(torch, key, prec, dt_factor)
+        out["deltaT_s"] = dt
+        tmp = tempfile.TemporaryDirectory()
+        ctx.set_output_dir(tmp.name)
+        st = stepper.Stepper(ctx, stepper.fields_from_workload(w, torch, g), deltaT=dt,
+                             max_iterations=LU_SUBITERATIONS, tolerance=0.0, limiter=True, filter=True,
+                             statistic_step=1 << 30)
+        ctx.statistic_reset()
+        ms, r, at_cmp = [], {"steps": n_steps}, None
+        cmp_at = compare_steps or steps
+        try:
+            for n in range(1, n_steps + 1):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                st.step(None)
+                e1.record()
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                if n == cmp_at:
+                    at_cmp = (stat_profiles(ctx.statistic_read(), g, n), [u.clone() for u in st.f["U"]])
+        except Exception as exc:     # a diverged run is reported with its step
+            r["failed_at_step"] = len(ms) + 1
+            r["error"] = str(exc)
+        r["s_per_step_mean"] = float(np.mean(ms)) * 1e-3 if ms else None
+        r["s_total"] = float(np.sum(ms)) * 1e-3
+        r["ms_per_subiteration"] = float(np.mean(ms)) / LU_SUBITERATIONS if ms else None
+        if at_cmp is not None:
+            prof, state = at_cmp
+            r["profiles_at_step"] = cmp_at
+            r["U_centre_over_Ub"] = float(np.max(prof["U"])) / syn_bulk_velocity(g)
+            if ref is None:
+                ref = at_cmp
+            else:
+                umax = max(float(np.max(np.abs(ref[0]["U"]))), 1e-300)
+                r["profile_max_rel_err_vs_fp64"] = {
+                    k: float(np.max(np.abs(prof[k] - ref[0][k]))) /
+                    (umax if k in ("U", "V", "W") else max(float(np.max(np.abs(ref[0][k]))), 1e-300))
+                    for k in prof}
+                r["state_max_rel_err_vs_fp64"] = [
+                    float((state[v] - ref[1][v]).abs().max()) / max(float(ref[1][v].abs().max()), 1e-300)
+                    for v in range(5)]
+        out[prec] = r
+        ctx.close()
+        tmp.cleanup()
+        del st, w
+        torch.cuda.empty_cache()
+    return out
+
+
+def syn_bulk_velocity(g):
+    from channel_flow_gb300 import synthetic as syn
+    return syn.bulk_velocity(g, 0.5)
+
+
 def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=4, epochs=200, batch=131072,
                                online=0, learned_cap=20):
     """Wall time per physical step at equal pseudo-time tolerance on the
@@ -845,7 +966,7 @@ def mlp_gemms(torch, rows, steps=5, warmup=2):
     return out
 
 
-def wavy_workload(ctx, g, torch, amplitude_over_h=0.05, wavelength_over_h=math.pi):
+def wavy_workload(ctx, g, torch, amplitude_over_h=0.05, wavelength_over_h=math.pi, wall_damped=False):
     """The benchmark channel with a wavy lower wall (amplitude 0.05 h,
     wavelength pi h: two waves over 2 pi h) and the conservative metrics of
     cf_wavy_metrics; seeded laminar-plus-noise state at Mach 0.5."""
@@ -853,7 +974,8 @@ def wavy_workload(ctx, g, torch, amplitude_over_h=0.05, wavelength_over_h=math.p
     wall = wavy.wall_for(g, amplitude_over_h, wavelength_over_h, stretching=GAMMA, conservative=True)
     m = wavy.channel_metrics(g, wall)
     J = m["J"].cpu().numpy()
-    host = {"U": syn.channel_state(g, J, seed=SEED, mach=0.5, noise=0.05, jitter=0.01, gamma=GAMMA), "J": J,
+    host = {"U": syn.channel_state(g, J, seed=SEED, mach=0.5, noise=0.05, jitter=0.01, gamma=GAMMA,
+                                   wall_damped=wall_damped), "J": J,
             "cm": [t.cpu().numpy() for t in m["cm"]], "Yp": m["Yp"].cpu().numpy()}
     w = DeviceWorkload(ctx, g, host, torch)
     del host

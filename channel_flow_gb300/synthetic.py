@@ -156,7 +156,7 @@ def y_points(g: Grid, gamma: float = 2.8):
 
 def channel_state(g: Grid, J, seed: int = 0, mach: float = 0.5, noise: float = 0.05,
                   jitter: float = 0.01, rho_b: float = RHO_REF, gamma: float = 1.5,
-                  wall_damped: bool = False):
+                  wall_damped: bool = False, yy=None):
     """Seeded channel state U/J = (rho, rho u, rho v, rho w, E)/J on every
     cell of the array: laminar parabola u = 1.5 U_b (1 - eta^2) plus uniform
     +-noise*U_b on u, v, w, and +-jitter relative noise on rho and T (the
@@ -164,14 +164,19 @@ def channel_state(g: Grid, J, seed: int = 0, mach: float = 0.5, noise: float = 0
     avoided).  U_b = mach * sqrt(K R T_wall).  ``wall_damped``: the
     velocity noise is scaled by the parabola's shape 1 - eta^2, so it
     vanishes at the no-slip walls (the noise keeps its +-noise*U_b
-    amplitude on the centre line)."""
+    amplitude on the centre line).  ``yy``: the stretched wall-normal
+    position per j (0 .. 2) to use instead of evaluating the tanh map; with
+    it the state is built from correctly rounded operations only, so it is
+    the same on every platform."""
     rng = np.random.default_rng(seed)
     X, Y, Z = g.shape
     ub = mach * math.sqrt(g.K * g.R * T_WALL)
     j = np.arange(Y, dtype=np.float64)
     eta = np.clip(1 - 2 * (j - 1.5) * g.deltaET, -1.0, 1.0)          # +1 bottom wall .. -1 top
     # position in the stretched coordinate mapped back to [-1, 1]
-    yy = 1 - 1.0 / math.tanh(gamma) * np.tanh(gamma * eta)            # 0 .. 2
+    if yy is None:
+        yy = 1 - 1.0 / math.tanh(gamma) * np.tanh(gamma * eta)        # 0 .. 2
+    yy = np.asarray(yy, dtype=np.float64)
     prof = 1.5 * ub * (1 - (yy - 1) ** 2)
     amp = noise * ub * ((1 - (yy - 1) ** 2)[None, :, None] if wall_damped else 1.0)
     rho = rho_b * (1 + jitter * rng.uniform(-1, 1, g.shape))

@@ -309,3 +309,44 @@ def channel_step_case(g, gamma=2.0, seed=0, mach=0.5, port=None):
             "vF": [z() for _ in range(4)], "LL": [z() for _ in range(4)], "ML": [z() for _ in range(4)],
             "MR": [z() for _ in range(5)], "NR": [z() for _ in range(5)], "NL": [z() for _ in range(5)],
             "Residual": [z() for _ in range(5)]}
+
+
+def config0_case():
+    """The 64^3 plain-FP64 channel schedule of tests/golden/config0_64_run.json
+    (made by tests/golden/make_config0_run.py): (grid, fields, fixture).
+    The static inputs come from the stored arrays and the state from the
+    stored wall-normal profile, so every host builds the same bits."""
+    import bz2
+    import json
+    from pathlib import Path
+    here = Path(__file__).resolve().parent / "golden"
+    meta = json.loads((here / "config0_64_run.json").read_text())
+    g = syn.channel_physics(syn.channel_grid(*meta["dims"]), meta["mach"], meta["re_bulk"])
+    raw = bz2.decompress((here / "config0_64_static.bz2").read_bytes())
+    n = int(np.prod(g.shape))
+    st = np.frombuffer(raw, dtype=np.float64).reshape(len(meta["static_names"]), *g.shape).copy()
+    J = st[0]
+    yy = np.array([float.fromhex(x) for x in meta["yy"]])
+    U = syn.channel_state(g, J, seed=meta["seed"], mach=meta["mach"], noise=0.05, jitter=0.01, gamma=meta["gamma"],
+                          wall_damped=True, yy=yy)
+    assert st.shape[0] * n * 8 == len(raw)
+    z = lambda: np.zeros(g.shape)
+    f = {"U_": [u.copy() for u in U], "U": [u.copy() for u in U], "Uq": [u.copy() for u in U], "J": J,
+         "Y_point": st[1], "cell_metric": list(st[2:11]),
+         "face_J": [st[11 + 10 * d] for d in range(3)],
+         "face_metric": [list(st[12 + 10 * d:21 + 10 * d]) for d in range(3)],
+         "Ep": [z() for _ in range(3)], "inF": [[z() for _ in range(5)] for _ in range(3)],
+         "vF": [z() for _ in range(4)], "LL": [z() for _ in range(4)], "ML": [z() for _ in range(4)],
+         "MR": [z() for _ in range(5)], "NR": [z() for _ in range(5)], "NL": [z() for _ in range(5)],
+         "Residual": [z() for _ in range(5)]}
+    meta["deltaT_value"] = float.fromhex(meta["deltaT"])
+    return g, f, meta
+
+
+def state_digest(fields, to_numpy=np.asarray):
+    """SHA-256 over U_, U and Uq (five arrays each, in order)."""
+    h = hashlib.sha256()
+    for key in ("U_", "U", "Uq"):
+        for a in fields[key]:
+            h.update(np.ascontiguousarray(to_numpy(a)).tobytes())
+    return h.hexdigest()
