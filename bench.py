@@ -95,6 +95,17 @@ def peaks():
 # --------------------------------------------------------------------------
 # workload
 
+LU_SCHEDULE = None   # --lu-schedule
+
+
+def new_context(cf, g, **kw):
+    """A context with the bench's sweep schedule (--lu-schedule)."""
+    ctx = cf.Context(g, **kw)
+    if LU_SCHEDULE:
+        ctx.set_lu_schedule(LU_SCHEDULE)
+    return ctx
+
+
 def make_host_workload(g):
     """numpy arrays of the benchmark channel (host, set-up only)."""
     from channel_flow_gb300 import synthetic as syn
@@ -337,8 +348,12 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=0,
                     help="--step schedule: run FP64 for this many steps only and compare there (0 = all)")
     ap.add_argument("--dt-factor", type=float, default=1.0, help="--step schedule: time step / (0.005 h/U_b)")
+    ap.add_argument("--lu-schedule", default=None, choices=["wavefront", "pencil", "planes"],
+                    help="sweep schedule of Dual_time_stepping (default: the library's)")
     args = ap.parse_args()
     dims = tuple(int(x) for x in args.grid.split("x"))
+    global LU_SCHEDULE
+    LU_SCHEDULE = args.lu_schedule
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -421,7 +436,7 @@ def main():
         dist.init_process_group("gloo")
     torch.cuda.set_device(local)
     host = make_host_workload(g)
-    ctx = cf.Context(g, precision=args.precision, gamma=GAMMA)
+    ctx = new_context(cf, g, precision=args.precision, gamma=GAMMA)
     w = DeviceWorkload(ctx, g, host, torch)
     calls = rhs_calls(ctx, w, lambda x: x.data_ptr())
     stream = torch.cuda.current_stream()
@@ -629,7 +644,7 @@ def northstar_case(torch, dims, precision):
     host = {"U": syn.channel_state(g, J, seed=SEED, mach=NS_MACH, noise=0.05, jitter=0.01, gamma=GAMMA,
                                    wall_damped=True),
             "J": J, "cm": [cm[n] for n in syn.METRIC_NAMES], "Yp": syn.y_points(g, gamma=GAMMA)}
-    ctx = cf.Context(g, precision=precision, gamma=GAMMA, scheme="consistent")
+    ctx = new_context(cf, g, precision=precision, gamma=GAMMA, scheme="consistent")
     w = DeviceWorkload(ctx, g, host, torch)
     return g, ctx, w, syn.time_step(g, NS_MACH) * NS_DT_FACTOR
 
@@ -684,7 +699,7 @@ def schedule_case(torch, key, precision, dt_factor):
     from channel_flow_gb300 import synthetic as syn
     spec = SCHEDULES[key]
     g = syn.channel_physics(syn.channel_grid(*spec["dims"]), 0.5, spec["re"])
-    ctx = cf.Context(g, precision=precision, gamma=GAMMA, scheme="consistent")
+    ctx = new_context(cf, g, precision=precision, gamma=GAMMA, scheme="consistent")
     if spec["wavy"]:
         w, _ = wavy_workload(ctx, g, torch, wall_damped=True)
     else:
@@ -1004,7 +1019,7 @@ def secondary(ctx, g, w, calls, stream, torch, args):
     ctx.set_precision(prec0)
     if (g.X_out, g.Y_out, g.Z_out) != (256, 192, 192) and not args.no_large:
         g2 = syn.channel_grid(256, 192, 192)
-        ctx2 = cf.Context(g2, precision="fp64", gamma=GAMMA)
+        ctx2 = new_context(cf, g2, precision="fp64", gamma=GAMMA)
         w2 = DeviceWorkload(ctx2, g2, make_host_workload(g2), torch)
         calls2 = rhs_calls(ctx2, w2, lambda x: x.data_ptr())
         out["256x192x192"] = {}
@@ -1018,7 +1033,7 @@ def secondary(ctx, g, w, calls, stream, torch, args):
         # the 50 M-cell channel with a wavy lower wall (metrics from cf_wavy_metrics)
         try:
             g3 = syn.channel_grid(512, 256, 384)
-            ctx3 = cf.Context(g3, precision="fp64", gamma=GAMMA)
+            ctx3 = new_context(cf, g3, precision="fp64", gamma=GAMMA)
             w3, wall = wavy_workload(ctx3, g3, torch)
             calls3 = rhs_calls(ctx3, w3, lambda x: x.data_ptr())
             r = {"wall": {"amplitude_over_h": 0.05, "wavelength_over_h": math.pi, "metrics": "conservative"}}

@@ -77,10 +77,11 @@ class Context:
         self._ok(self.lib.cf_set_stream(self.h, stream if isinstance(stream, int) else int(stream)))
 
     def set_lu_schedule(self, schedule: str):
-        """'wavefront' (default) or 'planes': how the hyperplane sweeps of
-        Dual_time_stepping are launched; both give the same results."""
+        """'wavefront' (default), 'pencil' or 'planes': how the hyperplane
+        sweeps of Dual_time_stepping are launched; all give the same results."""
         self._ok(self.lib.cf_set_lu_schedule(self.h, {"wavefront": _lib.CF_LU_WAVEFRONT,
-                                                      "planes": _lib.CF_LU_PLANES}[schedule]))
+                                                      "planes": _lib.CF_LU_PLANES,
+                                                      "pencil": _lib.CF_LU_PENCIL}[schedule]))
 
     def set_scheme(self, scheme: str):
         """'reference' (default: the reference's face-state scaling of the

@@ -12,7 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libcfgb300.so"
 
 CF_OK, CF_ERR_ARG, CF_ERR_CUDA, CF_ERR_NONFINITE, CF_ERR_NOMEM, CF_ERR_STATE, CF_ERR_TIMEOUT = range(7)
-CF_LU_WAVEFRONT, CF_LU_PLANES = 0, 1
+CF_LU_WAVEFRONT, CF_LU_PLANES, CF_LU_PENCIL = 0, 1, 2
 PREC = {"fp64_exact": 0, "fp64": 1, "fp32": 2}
 SCHEME = {"reference": 0, "consistent": 1}
 

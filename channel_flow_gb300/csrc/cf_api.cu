@@ -43,6 +43,7 @@ struct cf_ctx {
     int lu_schedule = CF_LU_WAVEFRONT;                // hyperplane sweep schedule
     unsigned wait_limit = CF_WAVE_SPIN_LIMIT;         // polls of a wavefront dependency wait
     int *tile_order = nullptr;        // wavefront tiles sorted by plane (device)
+    int *pencil_order = nullptr;      // pencils sorted by pj + pk (device)
     long long *trace = nullptr;       // wavefront trace: [2 sweeps][tiles][4] stamps, when enabled
     size_t trace_tiles = 0;
     cudaGraphExec_t dts_exec = nullptr;               // Dual_time_stepping as one graph
@@ -256,6 +257,7 @@ void cf_destroy(cf_ctx *c)
     if (c->dts_exec) cudaGraphExecDestroy(c->dts_exec);
     if (c->stat_acc) cudaFree(c->stat_acc);
     if (c->tile_order) cudaFree(c->tile_order);
+    if (c->pencil_order) cudaFree(c->pencil_order);
     if (c->trace) cudaFree(c->trace);
     if (c->cap) cudaStreamDestroy(c->cap);
     if (c->side) cudaStreamDestroy(c->side);
@@ -295,7 +297,8 @@ int cf_set_wait_limit(cf_ctx *c, unsigned polls)
 
 int cf_set_lu_schedule(cf_ctx *c, int schedule)
 {
-    if (!c || (schedule != CF_LU_WAVEFRONT && schedule != CF_LU_PLANES)) return CF_ERR_ARG;
+    if (!c || (schedule != CF_LU_WAVEFRONT && schedule != CF_LU_PLANES && schedule != CF_LU_PENCIL))
+        return CF_ERR_ARG;
     c->lu_schedule = schedule;
     return CF_OK;
 }
@@ -608,7 +611,7 @@ int cf_Filter(cf_ctx *c, int, double Roe_criterion, double E_high, double E_low,
     a.Yp = R(c, Y_point);
     a.J = R(c, J);
     a.Ep[0] = R(c, EpX); a.Ep[1] = R(c, EpY); a.Ep[2] = R(c, EpZ);
-    double *s = scratch(c, "filter", 16);
+    double *s = scratch(c, "filter", 17);
     if (!s) return fail(c, CF_ERR_NOMEM, "Filter: scratch allocation failed");
     const size_t n = c->d.total();
     int f = 0;
@@ -617,6 +620,7 @@ int cf_Filter(cf_ctx *c, int, double Roe_criterion, double E_high, double E_low,
     for (int v = 0; v < 4; v++) a.acc[v] = s + n * f++;
     a.cA = s + n * f++;
     a.cC = s + n * f++;
+    a.cB = s + n * f++;
     a.Eh = s + n * f++;
     a.E2h = s + n * f++;
     // FP64 exact: the reference's expression trees (no FMA), so the switch
@@ -789,6 +793,80 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
     return CF_OK;
 }
 
+// pencils and scratch of the pencil sweeps (cf_pencil.cuh)
+static int pencil_setup(cf_ctx *c, cf_wave_args &w)
+{
+    const cf_dims &d = c->d;
+    w.d = d;
+    w.npj = (d.Y_out + CF_PENCIL_TJ - 1) / CF_PENCIL_TJ;
+    w.npk = (d.Z_out + CF_PENCIL_TK - 1) / CF_PENCIL_TK;
+    w.npencils = w.npj * w.npk;
+    w.nplanes = d.X_out + (CF_PENCIL_TJ - 1) + (CF_PENCIL_TK - 1);
+    w.ntiles = w.npencils;
+    if (!c->pencil_order) {
+        // topological order of both sweeps: pencils by pj + pk
+        std::vector<int> order;
+        order.reserve((size_t)w.npencils);
+        for (int p = 0; p <= w.npj + w.npk - 2; p++)
+            for (int b = 0; b < w.npj; b++) {
+                const int k = p - b;
+                if (k >= 0 && k < w.npk) order.push_back(b * w.npk + k);
+            }
+        if (cudaMalloc(&c->pencil_order, order.size() * sizeof(int)) != cudaSuccess) {
+            c->pencil_order = nullptr;
+            return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: pencil table allocation failed");
+        }
+        if (int rc = cuda_check(c, cudaMemcpy(c->pencil_order, order.data(), order.size() * sizeof(int),
+                                              cudaMemcpyHostToDevice), "pencil table")) return rc;
+    }
+    w.order = c->pencil_order;
+    const size_t T8 = sizeof(double);       // sized for double; the FP32 kernels use half
+    const size_t np = (size_t)w.npencils;
+    const size_t pack = np * w.nplanes * CF_WAVE_PACK * 32 * T8;
+    const size_t nl = np * w.nplanes * 5 * 32 * T8;
+    const size_t xg = np * 5 * 32 * T8;
+    // exchange words: 64 bits per 32-bit part of a value (two parts for double)
+    const size_t yex = np * d.X_out * 5 * CF_PENCIL_TK * 2 * sizeof(unsigned long long);
+    const size_t zex = np * d.X_out * 5 * CF_PENCIL_TJ * 2 * sizeof(unsigned long long);
+    const size_t flags = ((np + 3) * sizeof(int) + 255) / 256 * 256;
+    const size_t total = pack + nl + xg + yex + zex + flags;
+    const bool fresh = !c->scratch["lu_pencil"].first || c->scratch["lu_pencil"].second < total;
+    unsigned char *base = static_cast<unsigned char *>(scratch_bytes(c, "lu_pencil", total));
+    if (!base) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: pencil scratch allocation failed");
+    // a new buffer: exchange tags and the epoch start at zero (the first
+    // call's tags are 2 and 3)
+    if (fresh)
+        if (int rc = cuda_check(c, cudaMemset(base + pack + nl + xg, 0, yex + zex + flags), "pencil scratch"))
+            return rc;
+    w.pack = base;
+    w.nl = base + pack;
+    w.xg = base + pack + nl;
+    w.yex = base + pack + nl + xg;
+    w.zex = base + pack + nl + xg + yex;
+    w.flags = reinterpret_cast<int *>(base + pack + nl + xg + yex + zex);
+    w.counter = w.flags + w.npencils;
+    w.err = w.flags + w.npencils + 1;
+    w.dep_limit = c->wait_limit;
+    w.trace = nullptr;
+    if (c->trace_tiles) {
+        // per sweep and pencil: the claim, then the end of each block wait
+        const size_t per = (size_t)w.npencils * ((w.nplanes + CF_PENCIL_PUB - 1) / CF_PENCIL_PUB + 1);
+        const size_t units = (per + 3) / 4;
+        if (c->trace_tiles != units) {
+            if (c->trace) cudaFree(c->trace);
+            c->trace = nullptr;
+            if (cudaMalloc(&c->trace, 2 * 4 * units * sizeof(long long)) != cudaSuccess) {
+                c->trace = nullptr;
+                c->trace_tiles = 0;
+                return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: trace allocation failed");
+            }
+            c->trace_tiles = units;
+        }
+        w.trace = c->trace;
+    }
+    return CF_OK;
+}
+
 // The whole Dual_time_stepping call on stream s: assembly, one forward and
 // one backward hyperplane sweep, NL <- NR, update and norms into er_dev.
 //
@@ -800,8 +878,9 @@ static int wave_setup(cf_ctx *c, cf_wave_args &w)
 // has already recomputed from MR and fixed coefficients.  It is run once.
 //
 // Schedules: CF_LU_WAVEFRONT, one persistent tiled launch per sweep
-// (cf_wave.cuh); CF_LU_PLANES, one launch per hyperplane from a per-cell
-// coefficient pack.  Both give the same bits.
+// (cf_wave.cuh); CF_LU_PENCIL, one persistent launch per sweep of warps
+// sweeping 4x8 pencils (cf_pencil.cuh); CF_LU_PLANES, one launch per
+// hyperplane from a per-cell coefficient pack.  All give the same bits.
 static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, const cf_wave_args &w, double dt,
                                cudaStream_t s)
 {
@@ -809,7 +888,33 @@ static cudaError_t enqueue_dts(cf_ctx *c, const cf_lu_args &a, double *pack, con
     const bool ex = exact(c);
     const int pr = ex ? 0 : kprec(c);
     cudaError_t e = cudaSuccess;
-    if (c->lu_schedule == CF_LU_WAVEFRONT) {
+    if (c->lu_schedule == CF_LU_PENCIL) {
+        // as the tiled wavefront below: FP64 assembles inside the pack
+        const bool asm_in_pack = pr != 1;
+        const bool st = pr == 1 && a.f32_rhs && a.f32_lu && a.m32[0] && a.U32[0] && a.J32 && a.dUq32[0];
+        auto prepare = st ? cf_drv::lu_prepare : cf_fast::lu_prepare;
+        auto ppack = st ? cf_drv::lu_pencil_pack : cf_fast::lu_pencil_pack;
+        auto psweep = st ? cf_drv::lu_pencil_sweep : cf_fast::lu_pencil_sweep;
+        e = asm_in_pack ? (ex ? cf_exact::lu_zero(d, a, s) : cf_fast::lu_zero(d, a, s))
+                        : prepare(d, a, dt, true, pr, s);
+        const size_t fl = ((size_t)w.npencils + 1) * sizeof(int);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.err, 0, sizeof(int), s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_pencil_pack(d, a, w, dt, false, true, 0, s)
+                                     : ppack(d, a, w, dt, false, asm_in_pack, pr, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_pencil_sweep(a, w, true, 0, s) : psweep(a, w, true, pr, s);
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_pencil_pack(d, a, w, dt, true, false, 0, s)
+                                     : ppack(d, a, w, dt, true, false, pr, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.flags, 0, fl, s);
+        cf_wave_args wb = w;
+        if (w.trace) wb.trace = w.trace + 4 * c->trace_tiles;
+        if (e == cudaSuccess) e = ex ? cf_exact::lu_pencil_sweep(a, wb, false, 0, s) : psweep(a, wb, false, pr, s);
+        if (pr == 1) {
+            auto finish = st ? cf_drv::lu_finish : cf_fast::lu_finish;
+            if (e == cudaSuccess) e = finish(d, a, c->er_dev, pr, s);
+            return e;
+        }
+    } else if (c->lu_schedule == CF_LU_WAVEFRONT) {
         // FP64: the assembly happens inside the forward tile pack (one pass
         // over the cells less); FP32: its own box kernel, which measured
         // faster than the heavier FP32 pack kernel doing both
@@ -916,7 +1021,7 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     a.f32_rhs = (f32_rhs && kprec(c) == 1) ? 1 : 0;
     // with the wavefront, MR, NL and NR pass between the step driver's own
     // FP32 kernels only
-    a.f32_lu = (a.f32_rhs && c->lu_schedule == CF_LU_WAVEFRONT) ? 1 : 0;
+    a.f32_lu = (a.f32_rhs && c->lu_schedule != CF_LU_PLANES) ? 1 : 0;
     if (static_metrics && kprec(c) == 1)
         for (int n = 0; n < 9; n++) {
             a.m32[n] = met32_get(c, a.m[n]);
@@ -937,6 +1042,8 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     cf_wave_args w{};
     if (c->lu_schedule == CF_LU_WAVEFRONT) {
         if (int rc = wave_setup(c, w)) return rc;
+    } else if (c->lu_schedule == CF_LU_PENCIL) {
+        if (int rc = pencil_setup(c, w)) return rc;
     } else {
         pack = scratch(c, "lu_pack", CF_LU_PACK);
         if (!pack) return fail(c, CF_ERR_NOMEM, "Dual_time_stepping: coefficient pack allocation failed");
@@ -967,7 +1074,7 @@ static int dts_common(cf_ctx *c, double deltaT, double *er1, double *er2, double
     if (int rc = cuda_check(c, cudaGraphLaunch(c->dts_exec, c->stream), "Dual_time_stepping")) return rc;
     int *err_host = reinterpret_cast<int *>(c->er_host + 12);
     *err_host = 0;
-    if (c->lu_schedule == CF_LU_WAVEFRONT)
+    if (c->lu_schedule != CF_LU_PLANES)
         if (int rc = cuda_check(c, cudaMemcpyAsync(err_host, w.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
                                 "Dual_time_stepping")) return rc;
     double *er[5] = {er1, er2, er3, er4, er5};

@@ -15,6 +15,17 @@
 // only rho, rho u, rho v, rho w are filtered: the sensor E (Filter.cpp:
 // 790-804) never reads the filtered energy.
 //
+// The FP32 build uses the high-pass form instead: with G the three passes
+// (values outside the box read as U), the deconvolution residual is
+// u - u* = (I - G~)^5 (I - G) u, where G~ is G on fields that are zero
+// outside the box (1 - (6x - 15x^2 + 20x^3 - 15x^4 + 6x^5 - x^6) =
+// (1 - x)^6, and the affine level map splits into U + the linear part).  So
+// each level stores h_(l+1) = -(G - I) h_l, formed from differences of
+// neighbouring values, pass by pass ((G - I) = (Gz - I) + Gz (Gy - I) +
+// Gz Gy (Gx - I)), and the sixth is u - u* itself: the FP32 rounding is
+// then relative to the small high-pass values rather than to u, which is
+// what the sensor's energy |u - u*|^2 resolves, and no sum is carried.
+//
 // EXACT (no-FMA build) keeps the reference's expression trees, with the
 // metric ratios b/a and c/a of the y pass formed once per call; otherwise
 // the y pass uses per-cell weights A = (b/a) J(j-1)/J(j), C = (c/a)
@@ -43,6 +54,7 @@ struct filt_fields {
     ST *acc[4];             // deconvolution sum
     ST *lev[2][4];          // both level fields: level 0 copies U into their ghost ring
     const ST *cA, *cC;      // y-pass coefficients (b/a, c/a when EXACT)
+    const ST *cB;           // high-pass form: A + C - 1 of the per-cell weights
     const double *J;
 };
 
@@ -54,7 +66,8 @@ __device__ __forceinline__ bool filt_inside(const cf_dims &d, int i, int j, int 
 // y-pass coefficients, once per call (Filter.cpp:186-208)
 template <typename T, typename ST, bool EXACT>
 __global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__restrict__ Yp,
-                                                     const double *__restrict__ J, ST *cA, ST *cC, cf_box b)
+                                                     const double *__restrict__ J, ST *cA, ST *cC, ST *cB,
+                                                     cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k), s = d.Zm;
@@ -73,6 +86,9 @@ __global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__
         const float ia = 1.0f / a_, iJ = 1.0f / float(J[q]);
         cA[q] = ST(b_ * ia * (float(J[q - s]) * iJ));
         cC[q] = ST(c_ * ia * (float(J[q + s]) * iJ));
+        // A + C - 1 = (b (J(j-1) - J(j)) + c (J(j+1) - J(j))) / (a J(j)),
+        // with the J differences formed in FP64 (they cancel)
+        cB[q] = ST((b_ * float(J[q - s] - J[q]) + c_ * float(J[q + s] - J[q])) * ia * iJ);
     } else {
         const double a_ = Yp[q + s] - Yp[q - s];
         const double b_ = Yp[q + s] - Yp[q];
@@ -88,16 +104,17 @@ __global__ void __launch_bounds__(256) k_filter_coef(cf_dims d, const double *__
 // ring of both level fields (as ST), so the later levels read their input
 // field alone, with no per-load choice between two arrays.  Offsets are
 // 32-bit (the launcher checks the array size).
-template <typename T, typename SRC, typename ST, bool L0>
+template <typename T, typename SRC, typename ST, bool L0, bool HF>
 __device__ __forceinline__ void filt_load4(const filt_fields<ST> &f, bool ghost, unsigned q, T *x)
 {
 #pragma unroll
     for (int v = 0; v < 4; v++) x[v] = T(static_cast<const SRC *>(f.src[v])[q]);
     if (L0 && ghost) {
+        // the high-pass levels are zero outside the box
 #pragma unroll
         for (int v = 0; v < 4; v++) {
-            f.lev[0][v][q] = ST(x[v]);
-            f.lev[1][v][q] = ST(x[v]);
+            f.lev[0][v][q] = HF ? ST(0) : ST(x[v]);
+            f.lev[1][v][q] = HF ? ST(0) : ST(x[v]);
         }
     }
 }
@@ -107,11 +124,13 @@ __device__ __forceinline__ void filt_load4(const filt_fields<ST> &f, bool ghost,
 // has plane i+2 in flight, and the y-pass coefficients and the
 // deconvolution sum of plane i are requested before the x pass, so the
 // passes wait on no global load.
-template <typename T, typename SRC, typename ST, bool WIDE, bool EXACT, bool L0>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf_dims d, filt_fields<ST> f, int level, int fti)
+template <typename T, typename SRC, typename ST, bool WIDE, bool EXACT, bool L0, bool HF>
+__global__ void __launch_bounds__(256, HF ? 3 : sizeof(T) == 4 ? 4 : 2) k_filter_level(cf_dims d, filt_fields<ST> f, int level, int fti)
 {
     __shared__ T sgx[4][FT_HJ][FT_HK];     // x pass, rows j0-1..j0+8, columns k0-1..k0+32
     __shared__ T sgy[4][FT_J][FT_HK];      // y pass, rows j0..j0+7
+    __shared__ T sfv[HF ? 4 : 1][FT_HJ][FT_HK];   // high-pass form: the level's input on the halo
+    constexpr T cxz = T(WIDE ? 0.25 : 0.125), cy = T(WIDE ? 0.5 : 0.25);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
     const int k0 = 2 + (int)blockIdx.x * FT_K, j0 = 2 + (int)blockIdx.y * FT_J;
     const int i0 = 3 + (int)blockIdx.z * fti;
@@ -138,9 +157,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
 #pragma unroll
         for (int v = 0; v < 4; v++) sm[o][v] = s0[o][v] = sp[o][v] = sn[o][v] = T(0);
         if (pv[o]) {
-            filt_load4<T, SRC, ST, L0>(f, level0 && (!hin[o] || i0 - 1 < 3), (unsigned)(i0 - 1) * P + qh[o], sm[o]);
-            filt_load4<T, SRC, ST, L0>(f, level0 && !hin[o], (unsigned)i0 * P + qh[o], s0[o]);
-            filt_load4<T, SRC, ST, L0>(f, level0 && (!hin[o] || i0 + 1 > d.gend), (unsigned)(i0 + 1) * P + qh[o], sp[o]);
+            filt_load4<T, SRC, ST, L0, HF>(f, level0 && (!hin[o] || i0 - 1 < 3), (unsigned)(i0 - 1) * P + qh[o], sm[o]);
+            filt_load4<T, SRC, ST, L0, HF>(f, level0 && !hin[o], (unsigned)i0 * P + qh[o], s0[o]);
+            filt_load4<T, SRC, ST, L0, HF>(f, level0 && (!hin[o] || i0 + 1 > d.gend), (unsigned)(i0 + 1) * P + qh[o], sp[o]);
         }
     }
     const int jy = j0 + ty;                  // y-pass / output row of this thread
@@ -160,14 +179,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
         const unsigned qi = (unsigned)i * P;
         // requests for this plane's y-pass coefficients and sum, and the
         // input plane i+2
-        T cAv[2] = {T(0), T(0)}, cCv[2] = {T(0), T(0)}, ac[4] = {T(0), T(0), T(0), T(0)};
+        T cAv[2] = {T(0), T(0)}, cCv[2] = {T(0), T(0)}, cBv[2] = {T(0), T(0)}, ac[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
         for (int o = 0; o < 2; o++)
             if (ycol[o]) {
                 cAv[o] = T(f.cA[qi + qy + 32 * o]);
                 cCv[o] = T(f.cC[qi + qy + 32 * o]);
+                if (HF) cBv[o] = T(f.cB[qi + qy + 32 * o]);
             }
-        if (outp && level > 0) {
+        if (!HF && outp && level > 0) {
 #pragma unroll
             for (int v = 0; v < 4; v++) ac[v] = T(f.acc[v][qi + qz]);
         }
@@ -175,7 +195,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
 #pragma unroll
             for (int o = 0; o < 2; o++)
                 if (pv[o])
-                    filt_load4<T, SRC, ST, L0>(f, level0 && (!hin[o] || i + 2 > d.gend), qi + 2 * P + qh[o], sn[o]);
+                    filt_load4<T, SRC, ST, L0, HF>(f, level0 && (!hin[o] || i + 2 > d.gend), qi + 2 * P + qh[o], sn[o]);
         }
         // x pass (Filter.cpp:156-170, 835-849); plane i lies inside the box
 #pragma unroll
@@ -186,6 +206,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
 #pragma unroll
             for (int v = 0; v < 4; v++) {
                 T g = s0[o][v];
+                if (HF) {
+                    // (Gx - I) f: differences of neighbours, zero outside the box
+                    sfv[v][r][c] = s0[o][v];
+                    sgx[v][r][c] = in ? cxz * ((sm[o][v] - s0[o][v]) + (sp[o][v] - s0[o][v])) : T(0);
+                    continue;
+                }
                 if (EXACT) {
                     if (in)
                         g = WIDE ? T(0.25) * (sm[o][v] + T(2) * s0[o][v] + sp[o][v])
@@ -209,11 +235,23 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
                 if (!ycol[o]) {
 #pragma unroll
                     for (int v = 0; v < 4; v++)
-                        sgy[v][ty][c] = EXACT ? sgx[v][ty + 1][c] : T(WIDE ? 2.0 : 4.0 / 3.0) * sgx[v][ty + 1][c];
+                        sgy[v][ty][c] = HF ? T(0)
+                                           : EXACT ? sgx[v][ty + 1][c] : T(WIDE ? 2.0 : 4.0 / 3.0) * sgx[v][ty + 1][c];
                     continue;
                 }
                 const T A = cAv[o], C = cCv[o];
-                if (EXACT) {
+                if (HF) {
+                    // (Gy Gx - I) f = (Gy - I) f + Gy (Gx - I) f, with
+                    // (Gy - I) g = cy (A (g(j-1) - g) + C (g(j+1) - g) + B g)
+                    const T B = cBv[o];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const T fm = sfv[v][ty][c], f0 = sfv[v][ty + 1][c], fp = sfv[v][ty + 2][c];
+                        const T em = sgx[v][ty][c], e0 = sgx[v][ty + 1][c], ep = sgx[v][ty + 2][c];
+                        sgy[v][ty][c] = e0 + cy * (A * ((fm - f0) + (em - e0)) + C * ((fp - f0) + (ep - e0)) +
+                                                   B * (f0 + e0));
+                    }
+                } else if (EXACT) {
                     const size_t q = d.ix(i, jy, kk);
                     const size_t s = d.Zm;
                     const T Jm = T(f.J[q - s]), J0 = T(f.J[q]), Jp = T(f.J[q + s]);
@@ -235,6 +273,17 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
                 }
             }
         }
+        // high-pass form: the z pass's input values, read before the barrier
+        // after which the next plane's x pass rewrites sfv
+        T zfm[4], zf0[4], zfp[4];
+        if (HF && outp) {
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                zfm[v] = sfv[v][ty + 1][tx];
+                zf0[v] = sfv[v][ty + 1][tx + 1];
+                zfp[v] = sfv[v][ty + 1][tx + 2];
+            }
+        }
         __syncthreads();
         // z pass (Filter.cpp:224-239, 896-910) and the deconvolution sum
         if (outp) {
@@ -242,6 +291,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_filter_level(cf
 #pragma unroll
             for (int v = 0; v < 4; v++) {
                 const T gm = sgy[v][ty][tx], g0 = sgy[v][ty][tx + 1], gp = sgy[v][ty][tx + 2];
+                if (HF) {
+                    // next high-pass level h <- h - G h = -(G - I) h, with
+                    // (G - I) f = (Gz - I) f + Gz (Gy Gx - I) f; the last
+                    // level's h is u - u* and goes to acc
+                    const T dev = g0 + cxz * (((zfm[v] - zf0[v]) + (zfp[v] - zf0[v])) + ((gm - g0) + (gp - g0)));
+                    (last ? f.acc[v] : f.dst[v])[q] = ST(-dev);
+                    continue;
+                }
                 // the contracted build's passes carry the factors NX (x),
                 // NX / c0 (y) and NX (z); c0 / NX^2 is 1/32 (wide) or 3/256
                 // (narrow), both exact
@@ -278,11 +335,22 @@ template <typename ST>
 struct filt_ptr4 {
     ST *p[4];
 };
-template <typename T, typename ST>
+// HF (high-pass form): acc holds h = u - u*, and with velocity V = m/rho
+// of the state, m/rho - (m - h_m)/(rho - h_rho) = (h_m - V h_rho)/(rho - h_rho)
+template <typename T, typename ST, bool HF>
 __global__ void k_filter_energy4(cf_dims d, cf_ptr5 U, filt_ptr4<ST> acc, double *E, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const size_t q = d.ix(i, j, k);
+    if (HF) {
+        const T rho = T(U.p[0][q]), hr = T(acc.p[0][q]);
+        const T irho = frcp<T>(rho), iden = frcp<T>(rho - hr);
+        const T Ue = (T(acc.p[1][q]) - T(U.p[1][q]) * irho * hr) * iden;
+        const T Ve = (T(acc.p[2][q]) - T(U.p[2][q]) * irho * hr) * iden;
+        const T We = (T(acc.p[3][q]) - T(U.p[3][q]) * irho * hr) * iden;
+        E[q] = double(Ue * Ue + Ve * Ve + We * We);
+        return;
+    }
     T u1 = T(U.p[0][q]), f1 = T(acc.p[0][q]);
 #ifdef CF_FAST_MATH
     // two reciprocals instead of six divisions
@@ -341,12 +409,12 @@ __global__ void k_filter_ep(cf_dims d, const double *__restrict__ Eh, const doub
     Ep[d.ix(i, j, k)] = Emax >= T(crit) ? hi : lo;
 }
 
-template <typename T, typename SRC, typename ST, bool EXACT>
+template <typename T, typename SRC, typename ST, bool EXACT, bool HF>
 static cudaError_t filter_level_launch(const cf_dims &d, const filt_fields<ST> &f, bool wide, int level,
                                        cudaStream_t s)
 {
-    // planes per block: one wave of the resident blocks (4 per SM in FP32,
-    // 2 in FP64), x cut into as many chunks as fill it
+    // planes per block: one wave of the resident blocks (3 per SM in the
+    // FP32 high-pass form, 2 in FP64), x cut into as many chunks as fill it
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -358,7 +426,7 @@ static cudaError_t filter_level_launch(const cf_dims &d, const filt_fields<ST> &
     if (d.total() >= (size_t(1) << 31)) return cudaErrorInvalidValue;   // 32-bit offsets
     // chunks minimising (waves of resident blocks) x (planes per block +
     // the two extra planes a block loads before its first)
-    const int slots = sms * (sizeof(T) == 4 ? 4 : 2);
+    const int slots = sms * (HF ? 3 : sizeof(T) == 4 ? 4 : 2);
     int chunks = 1;
     long best = -1;
     for (int c = 1; c <= d.X_out; c++) {
@@ -369,11 +437,11 @@ static cudaError_t filter_level_launch(const cf_dims &d, const filt_fields<ST> &
     const dim3 g((unsigned)tk, (unsigned)tj, (unsigned)((d.X_out + fti - 1) / fti));
     const dim3 t(32, 8);
     if (level == 0) {
-        if (wide) k_filter_level<T, SRC, ST, true, EXACT, true><<<g, t, 0, s>>>(d, f, level, fti);
-        else k_filter_level<T, SRC, ST, false, EXACT, true><<<g, t, 0, s>>>(d, f, level, fti);
+        if (wide) k_filter_level<T, SRC, ST, true, EXACT, true, HF><<<g, t, 0, s>>>(d, f, level, fti);
+        else k_filter_level<T, SRC, ST, false, EXACT, true, HF><<<g, t, 0, s>>>(d, f, level, fti);
     } else {
-        if (wide) k_filter_level<T, SRC, ST, true, EXACT, false><<<g, t, 0, s>>>(d, f, level, fti);
-        else k_filter_level<T, SRC, ST, false, EXACT, false><<<g, t, 0, s>>>(d, f, level, fti);
+        if (wide) k_filter_level<T, SRC, ST, true, EXACT, false, HF><<<g, t, 0, s>>>(d, f, level, fti);
+        else k_filter_level<T, SRC, ST, false, EXACT, false, HF><<<g, t, 0, s>>>(d, f, level, fti);
     }
     return cudaSuccess;
 }
@@ -388,7 +456,12 @@ cudaError_t launch_filter(const cf_dims &d, const cf_filter_args &a, double crit
     const cf_box bi = make_box(3, d.gend, 2, d.ny, 2, d.nz);
     const dim3 g = box_grid(bi), t = box_block();
     ST *cA = static_cast<ST *>(a.cA), *cC = static_cast<ST *>(a.cC);
-    k_filter_coef<T, ST, EXACT><<<g, t, 0, s>>>(d, a.Yp, a.J, cA, cC, bi);
+    // FP32: the high-pass form (each level holds h_(l+1) = (I - G) h_l, h_0 = u,
+    // and h_6 = u - u*), whose FP32 rounding is relative to the small
+    // high-pass values instead of to u
+    constexpr bool HF = sizeof(T) == 4 && !EXACT;
+    ST *cB = static_cast<ST *>(a.cB);
+    k_filter_coef<T, ST, EXACT><<<g, t, 0, s>>>(d, a.Yp, a.J, cA, cC, cB, bi);
     filt_fields<ST> f;
     for (int v = 0; v < 4; v++) {
         f.U[v] = a.U[v];
@@ -396,6 +469,7 @@ cudaError_t launch_filter(const cf_dims &d, const cf_filter_args &a, double crit
     }
     f.cA = cA;
     f.cC = cC;
+    f.cB = cB;
     f.J = a.J;
     cf_ptr5 U;
     filt_ptr4<ST> acc;
@@ -409,11 +483,11 @@ cudaError_t launch_filter(const cf_dims &d, const cf_filter_args &a, double crit
                 f.src[v] = lev == 0 ? static_cast<const void *>(a.U[v]) : a.lev[(lev - 1) & 1][v];
                 f.dst[v] = static_cast<ST *>(a.lev[lev & 1][v]);
             }
-            const cudaError_t e = lev == 0 ? filter_level_launch<T, double, ST, EXACT>(d, f, wide != 0, lev, s)
-                                           : filter_level_launch<T, ST, ST, EXACT>(d, f, wide != 0, lev, s);
+            const cudaError_t e = lev == 0 ? filter_level_launch<T, double, ST, EXACT, HF>(d, f, wide != 0, lev, s)
+                                           : filter_level_launch<T, ST, ST, EXACT, HF>(d, f, wide != 0, lev, s);
             if (e != cudaSuccess) return e;
         }
-        k_filter_energy4<T, ST><<<g, t, 0, s>>>(d, U, acc, wide ? a.E2h : a.Eh, bi);
+        k_filter_energy4<T, ST, HF><<<g, t, 0, s>>>(d, U, acc, wide ? a.E2h : a.Eh, bi);
     }
     cf_box bx = make_box(0, 1, 2, d.ny, 2, d.nz);
     k_filter_efill_x<<<box_grid(bx), t, 0, s>>>(d, a.Eh, a.E2h, bx);

@@ -37,6 +37,10 @@ constexpr int CF_LU_PACK = 52;   // doubles per cell of the sweep coefficient pa
     cudaError_t lu_wave_pack(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt,  \
                              bool upper, bool assemble, int prec, cudaStream_t s);                      \
     cudaError_t lu_zero(const cf_dims &d, const cf_lu_args &a, cudaStream_t s);                         \
+    cudaError_t lu_pencil_pack(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt, \
+                               bool upper, bool assemble, int prec, cudaStream_t s);                    \
+    cudaError_t lu_pencil_sweep(const cf_lu_args &a, const cf_wave_args &w, bool fwd, int prec,         \
+                                cudaStream_t s);                                                        \
     cudaError_t lu_wave_sweep(const cf_lu_args &a, const cf_wave_args &w, bool fwd, int prec,           \
                               cudaStream_t s);                                                          \
     cudaError_t lu_jacobi(const cf_dims &d, const cf_lu_args &a, double dt, int prec, cudaStream_t s); \

@@ -120,8 +120,8 @@ struct cf_filter_args {
     double *Ep[3];          // EpX, EpY, EpZ
     // scratch: two level fields and the deconvolution sum per filtered
     // variable, the y-pass coefficients (double, or float in the FP32
-    // build), and the sensor energies
-    void *lev[2][4], *acc[4], *cA, *cC;
+    // build; cB only in the FP32 build), and the sensor energies
+    void *lev[2][4], *acc[4], *cA, *cC, *cB;
     double *Eh, *E2h;
 };
 
@@ -160,7 +160,15 @@ struct cf_wave_args {
                              // copy waits keep CF_WAVE_SPIN_LIMIT)
     long long *trace;        // optional: per tile 4 global-timer stamps (claimed, inputs ready,
                              // pack landed, done); NULL when tracing is off
+    // pencil schedule (cf_pencil.cuh): 4 x 8 (j, k) pencils through every x
+    // plane; order, pack, nl, flags (steps done per pencil), counter, err and
+    // dep_limit take the pencil meaning, the face fields are these
+    int npj, npk, npencils, nplanes;
+    void *xg;                // terms from the x ghost cells: [npencils][5][32]
+    void *yex, *zex;         // terms crossing pencil faces: [npencils][X_out][5][8], [npencils][X_out][5][4]
 };
+constexpr int CF_PENCIL_TJ = 4, CF_PENCIL_TK = 8;
+constexpr int CF_PENCIL_PUB = 4;    // steps between two publications of a pencil's count
 
 struct cf_stat_args {
     const double *U[5];      // U1_..U5_

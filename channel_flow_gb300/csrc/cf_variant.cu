@@ -9,6 +9,7 @@
 #include "cf_filter.cuh"
 #include "cf_lusgs.cuh"
 #include "cf_wave.cuh"
+#include "cf_pencil.cuh"
 #include "cf_stats.cuh"
 #include "cf_launch.h"
 
@@ -205,6 +206,54 @@ cudaError_t lu_wave_pack(const cf_dims &d, const cf_lu_args &a, const cf_wave_ar
 {
     return CF_DISPATCH(prec, lu_wave_pack_t<double>(d, a, w, dt, upper, assemble, s),
                        lu_wave_pack_t<float>(d, a, w, dt, upper, assemble, s));
+}
+
+template <typename T>
+static cudaError_t lu_pencil_pack_t(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt,
+                                    bool upper, bool assemble, cudaStream_t s)
+{
+    if (upper) {
+        cf_box b = make_box(3, d.gend, 2, d.ny, 2, d.nz);
+        k_lu_pencil_ghost_upper<T><<<box_grid(b), box_block(), 0, s>>>(a, w, b);
+        return cudaGetLastError();
+    }
+    k_lu_pencil_epoch<<<1, 1, 0, s>>>(w);
+    const size_t smem = (size_t)WV_PACK * 256 * sizeof(T);
+    void (*kf)(cf_lu_args, wave_args, T) = assemble ? k_lu_pencil_pack<T, true> : k_lu_pencil_pack<T, false>;
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)w.npencils * (unsigned)((d.X_out + 7) / 8);
+    kf<<<blocks, 256, smem, s>>>(a, w, T(dt));
+    return cudaGetLastError();
+}
+// pencil packs (forward, with the assembly when asked) or the backward
+// sweep's upper ghost terms
+cudaError_t lu_pencil_pack(const cf_dims &d, const cf_lu_args &a, const cf_wave_args &w, double dt, bool upper,
+                           bool assemble, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_pencil_pack_t<double>(d, a, w, dt, upper, assemble, s),
+                       lu_pencil_pack_t<float>(d, a, w, dt, upper, assemble, s));
+}
+
+template <typename T>
+static cudaError_t lu_pencil_sweep_t(const cf_lu_args &a, const cf_wave_args &w, bool fwd, cudaStream_t s)
+{
+    const size_t smem = pc_smem_bytes<T>(fwd);
+    void (*kf)(cf_lu_args, wave_args) = fwd ? k_lu_pencil<T, true> : k_lu_pencil<T, false>;
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, occ = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    constexpr int warps = pc_geom<T>::WARPS;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, 32 * warps, smem)) != cudaSuccess) return e;
+    const int blocks = std::min((w.npencils + warps - 1) / warps, std::max(1, occ) * sms);
+    kf<<<blocks, 32 * warps, smem, s>>>(a, w);
+    return cudaGetLastError();
+}
+cudaError_t lu_pencil_sweep(const cf_lu_args &a, const cf_wave_args &w, bool fwd, int prec, cudaStream_t s)
+{
+    return CF_DISPATCH(prec, lu_pencil_sweep_t<double>(a, w, fwd, s), lu_pencil_sweep_t<float>(a, w, fwd, s));
 }
 
 // the zeroing of lu_prepare alone (NL, NR of every index, ghosts included)

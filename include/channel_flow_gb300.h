@@ -79,9 +79,13 @@ int cf_set_stream(cf_ctx *ctx, void *cuda_stream); /* cudaStream_t; NULL = legac
 int cf_set_stretching(cf_ctx *ctx, double gamma);
 /* Schedule of the hyperplane sweeps of Dual_time_stepping (same results):
  * CF_LU_WAVEFRONT (default) runs each sweep as one persistent launch over
- * 4x8x8-cell tiles; CF_LU_PLANES launches one kernel per hyperplane. */
+ * 4x8x8-cell tiles; CF_LU_PLANES launches one kernel per hyperplane;
+ * CF_LU_PENCIL runs each sweep as one persistent launch in which a warp
+ * sweeps a 4x8 (j, k) pencil through every x plane, one cell per lane and
+ * step. */
 #define CF_LU_WAVEFRONT 0
 #define CF_LU_PLANES 1
+#define CF_LU_PENCIL 2
 int cf_set_lu_schedule(cf_ctx *ctx, int schedule);
 /* Polls of a wavefront dependency wait (a tile waiting for the done flags
  * of its upstream tiles) before it gives up, sets the error word and the

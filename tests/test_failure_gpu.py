@@ -2,8 +2,8 @@
 made to run out on purpose (a short wait limit; nothing faults or hangs),
 and a non-finite value injected on the host.
 
-* With the wavefront's dependency-wait limit set to one poll, tiles stop
-  waiting for their upstream neighbours: Dual_time_stepping returns
+* With the sweeps' dependency-wait limit set to one poll, tiles (or
+  pencils) stop waiting for their upstream neighbours: Dual_time_stepping returns
   CF_ERR_TIMEOUT (its results are then invalid) instead of hanging, and
   the next call on the same context at the default limit equals the
   oracle bit for bit again.
@@ -21,12 +21,14 @@ from channel_flow_gb300 import _lib
 pytestmark = pytest.mark.gpu
 
 
-def test_wavefront_wait_runs_out_then_recovers(port, cuda_lib):
+@pytest.mark.parametrize("schedule", ["wavefront", "pencil"])
+def test_wavefront_wait_runs_out_then_recovers(schedule, port, cuda_lib):
     import channel_flow_gb300 as cf
     r = routines.BY_NAME["Dual_time_stepping"]
     g = cases.grid((32, 24, 40))
     ctx = cf.Context(g, precision="fp64_exact")
     try:
+        ctx.set_lu_schedule(schedule)
         a = r.build(g, 23)
         ctx.set_wait_limit(1)
         with pytest.raises(cf.CFError) as exc:

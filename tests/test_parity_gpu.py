@@ -20,6 +20,7 @@ pytestmark = pytest.mark.gpu
 GOLDEN = json.loads((Path(__file__).parent / "golden" / "reference_outputs.json").read_text())
 RTOL_FP64 = 1e-12
 RTOL_FP32 = {"Filter": None}   # FP32 switch decisions may differ: test_gpu_fp32_filter_switch
+CONFIG0_GRID = (64, 64, 64)
 
 
 @pytest.fixture(scope="module")
@@ -160,12 +161,12 @@ def test_gpu_fp32_filter_switch(port, ctx_factory):
         assert frac <= 0.01, (i, frac)
 
 
-@pytest.mark.parametrize("schedule", ["wavefront", "planes"])
-@pytest.mark.parametrize("dims", cases.GRIDS + [(13, 9, 17)])
+@pytest.mark.parametrize("schedule", ["wavefront", "pencil", "planes"])
+@pytest.mark.parametrize("dims", cases.GRIDS + [(13, 9, 17), (6, 6, 7), (20, 7, 9), CONFIG0_GRID])
 def test_gpu_dts_schedules_exact(dims, schedule, port, cuda_lib):
-    """Both sweep schedules of Dual_time_stepping (tiled wavefront, one
-    launch per hyperplane) equal the oracle bit for bit, on grids with
-    partial tiles."""
+    """Every sweep schedule of Dual_time_stepping (tiled wavefront, pencils,
+    one launch per hyperplane) equals the oracle bit for bit, on grids with
+    partial tiles and pencils."""
     import channel_flow_gb300 as cf
     r = routines.BY_NAME["Dual_time_stepping"]
     g = cases.grid(dims)
@@ -180,17 +181,18 @@ def test_gpu_dts_schedules_exact(dims, schedule, port, cuda_lib):
         ctx.close()
 
 
+@pytest.mark.parametrize("other", ["planes", "pencil"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_gpu_dts_schedules_agree(precision, cuda_lib):
-    """The two schedules agree in the contracted and FP32 builds to the
+def test_gpu_dts_schedules_agree(precision, other, cuda_lib):
+    """The schedules agree in the contracted and FP32 builds to the
     rounding of those builds (FMA contraction may pair the per-direction
-    sums differently in the two kernels)."""
+    sums differently in different kernels)."""
     import channel_flow_gb300 as cf
     r = routines.BY_NAME["Dual_time_stepping"]
     dims = (13, 9, 17)
     g = cases.grid(dims)
     outs = []
-    for schedule in ("wavefront", "planes"):
+    for schedule in ("wavefront", other):
         ctx = cf.Context(g, precision=precision)
         try:
             ctx.set_lu_schedule(schedule)
@@ -205,9 +207,6 @@ def test_gpu_dts_schedules_agree(precision, cuda_lib):
         scale = max(float(np.max(np.abs(a1[i]))), 1e-300)
         assert float(np.max(np.abs(a0[i] - a1[i]))) / scale <= tol, i
     np.testing.assert_allclose(np.asarray(e0), np.asarray(e1), rtol=tol * 10, atol=0)
-
-
-CONFIG0_GRID = (64, 64, 64)
 
 
 @pytest.mark.parametrize("name", [r.name for r in routines.ROUTINES])
