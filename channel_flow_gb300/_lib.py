@@ -75,6 +75,7 @@ _SIGS = {
     "cf_set_lu_schedule": ([P, C.c_int], C.c_int),
     "cf_set_scheme": ([P, C.c_int], C.c_int),
     "cf_fp64_peak_probe": ([P, C.c_int, C.c_int, P], C.c_int),
+    "cf_reciprocal_check": ([P, P, P, C.c_size_t], C.c_int),
     "cf_set_wait_limit": ([P, C.c_uint], C.c_int),
     "cf_lu_trace": ([P, C.c_int], C.c_int),
     "cf_lu_trace_read": ([P, P, C.c_size_t], C.c_int),

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/channel_flow_gb300.h"
+#include "cf_common.cuh"
 #include "cf_launch.h"
 
 #define CF_VERSION 100
@@ -166,6 +167,13 @@ __global__ void __launch_bounds__(256) k_fp64_fma_chains(int iters, double a, do
     if (s == 12345.678) out[blockIdx.x] = s;   // never true; keeps the chains
 }
 
+// the contracted build's reciprocal (frcp<double> of cf_common.cuh) of n values
+__global__ void __launch_bounds__(256) k_reciprocal(const double *d, double *out, size_t n)
+{
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) out[q] = frcp<double>(d[q]);
+}
+
 inline bool exact(const cf_ctx *c) { return c->prec == CF_PREC_FP64_EXACT; }
 inline int kprec(const cf_ctx *c) { return c->prec == CF_PREC_FP32 ? 1 : 0; }
 
@@ -180,6 +188,14 @@ int cf_fp64_peak_probe(void *stream, int blocks, int iters, double *scratch_dev)
 {
     if (blocks <= 0 || iters <= 0 || !scratch_dev) return CF_ERR_ARG;
     k_fp64_fma_chains<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(iters, 0.9999999, 1e-9, scratch_dev);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+int cf_reciprocal_check(void *stream, const double *d_dev, double *out_dev, size_t n)
+{
+    if (!d_dev || !out_dev) return CF_ERR_ARG;
+    if (n == 0) return CF_OK;
+    k_reciprocal<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(d_dev, out_dev, n);
     return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 

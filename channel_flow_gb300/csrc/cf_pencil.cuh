@@ -82,7 +82,7 @@ __device__ __forceinline__ T *pc_xg(const wave_args &w, int pencil)
 // (z face) values of PC_W words each
 template <typename T>
 struct pc_w {
-    static constexpr int W = (int)(sizeof(T) / 4);
+    static constexpr int W = wv_w<T>::W;
 };
 template <typename T>
 __device__ __forceinline__ unsigned long long *pc_yex(const wave_args &w, int pencil, int ci)
@@ -95,63 +95,6 @@ __device__ __forceinline__ unsigned long long *pc_zex(const wave_args &w, int pe
     return static_cast<unsigned long long *>(w.zex) + ((size_t)pencil * w.d.X_out + ci) * 5 * PC_TJ * pc_w<T>::W;
 }
 
-__device__ __forceinline__ void pc_st64(unsigned long long *p, unsigned long long v)
-{
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long pc_ld64(const unsigned long long *p)
-{
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// value v as PC_W tagged words at dst (word k: bits 32k..32k+31 of v)
-__device__ __forceinline__ void pc_put(unsigned long long *dst, float v, unsigned tag)
-{
-    pc_st64(dst, ((unsigned long long)tag << 32) | __float_as_uint(v));
-}
-__device__ __forceinline__ void pc_put(unsigned long long *dst, double v, unsigned tag)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    pc_st64(dst, ((unsigned long long)tag << 32) | (b & 0xffffffffull));
-    pc_st64(dst + 1, ((unsigned long long)tag << 32) | (b >> 32));
-}
-__device__ __forceinline__ float pc_get(const unsigned *x, float) { return __uint_as_float(x[0]); }
-__device__ __forceinline__ double pc_get(const unsigned *x, double)
-{
-    return __longlong_as_double((long long)(((unsigned long long)x[1] << 32) | x[0]));
-}
-
-// the sweep's tag: 2 epoch (forward) or 2 epoch + 1 (backward)
-__device__ __forceinline__ unsigned pc_tag(const wave_args &w, bool fwd)
-{
-    return 2u * (unsigned)w.flags[w.npencils + 2] + (fwd ? 0u : 1u);
-}
-
-// terms of ghost cell qg (N = 0) as tagged exchange words
-template <typename T, bool UPPER>
-__device__ __forceinline__ void pc_ghost_words(const cf_dims &d, const cf_lu_args &a, size_t qg, int dir,
-                                               const lu_den<T> &den, unsigned long long *face, int nslot, int f,
-                                               unsigned tag)
-{
-    const lstate<T> s = lu_state<T>(d, a, qg);
-    const lsplit<T> A = wave_split<T>(d, a, qg, s, dir);
-    T P[12], o[5];
-    wave_split12<T, UPPER>(A, P);
-    wave_scale<T>(P, den);
-    const T zero[5] = {T(0), T(0), T(0), T(0), T(0)};
-    if (UPPER) wave_upper_terms<T>(P, zero, den, o);
-    else wave_lower_terms<T>(P, zero, den, o);
-#pragma unroll
-    for (int n = 0; n < 5; n++) pc_put(face + (n * nslot + f) * pc_w<T>::W, o[n], tag);
-}
-
-// one thread: the next epoch of the exchange tags
-__global__ void k_lu_pencil_epoch(wave_args w)
-{
-    w.flags[w.npencils + 2] += 1;
-}
 
 // Pencil packs: one block of 256 threads per 8 x-planes of a pencil (cell
 // li*32 + lane), the values formed as for the tile pack in shared memory,
@@ -201,10 +144,10 @@ __global__ void __launch_bounds__(256) k_lu_pencil_pack(cf_lu_args a, wave_args 
             P[(45 + n) * 256] = MR[n];
         }
         if (i == 3) wave_ghost_term<T, false>(d, a, q - d.plane(), 0, den[0], pc_xg<T>(w, pencil), 32, lane);
-        if (j == 2) pc_ghost_words<T, false>(d, a, q - (size_t)d.Zm, 1, den[1], pc_yex<T>(w, pencil, i - 3), PC_TK,
-                                             lk, pc_tag(w, true));
-        if (k == 2) pc_ghost_words<T, false>(d, a, q - 1, 2, den[2], pc_zex<T>(w, pencil, i - 3), PC_TJ, lj,
-                                             pc_tag(w, true));
+        if (j == 2) wave_ghost_words<T, false>(d, a, q - (size_t)d.Zm, 1, den[1], pc_yex<T>(w, pencil, i - 3), PC_TK,
+                                             lk, wv_tag(w, w.npencils, true));
+        if (k == 2) wave_ghost_words<T, false>(d, a, q - 1, 2, den[2], pc_zex<T>(w, pencil, i - 3), PC_TJ, lj,
+                                             wv_tag(w, w.npencils, true));
     }
     __syncthreads();
     // plane-major write: warp wp takes planes p0 + wp, p0 + wp + 8, ...;
@@ -232,10 +175,10 @@ __global__ void __launch_bounds__(256) k_lu_pencil_ghost_upper(cf_lu_args a, wav
     const int pencil = (cj / PC_TJ) * w.npk + ck / PC_TK, lj = cj % PC_TJ, lk = ck % PC_TK;
     const lu_den<T> dXI(CF_DC(T, d, dXI)), dET(CF_DC(T, d, dET)), dZT(CF_DC(T, d, dZT));
     if (i == d.gend) wave_ghost_term<T, true>(d, a, q + d.plane(), 0, dXI, pc_xg<T>(w, pencil), 32, lj * PC_TK + lk);
-    if (j == d.ny) pc_ghost_words<T, true>(d, a, q + (size_t)d.Zm, 1, dET, pc_yex<T>(w, pencil, i - 3), PC_TK, lk,
-                                           pc_tag(w, false));
-    if (k == d.nz) pc_ghost_words<T, true>(d, a, q + 1, 2, dZT, pc_zex<T>(w, pencil, i - 3), PC_TJ, lj,
-                                           pc_tag(w, false));
+    if (j == d.ny) wave_ghost_words<T, true>(d, a, q + (size_t)d.Zm, 1, dET, pc_yex<T>(w, pencil, i - 3), PC_TK, lk,
+                                           wv_tag(w, w.npencils, false));
+    if (k == d.nz) wave_ghost_words<T, true>(d, a, q + 1, 2, dZT, pc_zex<T>(w, pencil, i - 3), PC_TJ, lj,
+                                           wv_tag(w, w.npencils, false));
 }
 
 // the five terms a cell owes its neighbour along direction W, from the
@@ -304,7 +247,7 @@ __global__ void __launch_bounds__(32 * pc_geom<T>::WARPS) k_lu_pencil(cf_lu_args
     __syncwarp();
     const lu_den<T> den[3] = {lu_den<T>(CF_DC(T, d, dXI)), lu_den<T>(CF_DC(T, d, dET)), lu_den<T>(CF_DC(T, d, dZT))};
     const int NP = w.nplanes;
-    const unsigned tag = pc_tag(w, FWD);
+    const unsigned tag = wv_tag(w, w.npencils, FWD);
     const unsigned pbytes = (unsigned)(NV * 32 * sizeof(T)), nbytes = (unsigned)(5 * 32 * sizeof(T));
     unsigned gs = 0;                       // this warp's steps over all its pencils (ring slot and phase)
     int slot = 0;
@@ -348,7 +291,7 @@ __global__ void __launch_bounds__(32 * pc_geom<T>::WARPS) k_lu_pencil(cf_lu_args
         for (int m = 0; m < NPRE; m++) {
             const int e = lane + 32 * m;
             const unsigned long long *ad = e < WORDS ? pc_word_addr<T, FWD>(w, pencil, 0, e, NP, tj, tk) : nullptr;
-            pre[m] = ad ? pc_ld64(ad) : 0ull;
+            pre[m] = ad ? wv_ld64(ad) : 0ull;
         }
         T xo[5], yo[5], zo[5];
 #pragma unroll
@@ -383,7 +326,7 @@ __global__ void __launch_bounds__(32 * pc_geom<T>::WARPS) k_lu_pencil(cf_lu_args
                             }
                             if ((it & 1023u) == 0 && ld_acquire(w.err) != 0) break;
                             __nanosleep(20);
-                            pre[m] = pc_ld64(ad);
+                            pre[m] = wv_ld64(ad);
                         }
                         v = (unsigned)(pre[m] & 0xffffffffull);
                     }
@@ -395,7 +338,7 @@ __global__ void __launch_bounds__(32 * pc_geom<T>::WARPS) k_lu_pencil(cf_lu_args
                     const int e = lane + 32 * m;
                     const unsigned long long *ad =
                         e < WORDS ? pc_word_addr<T, FWD>(w, pencil, s + PC_PUB, e, NP, tj, tk) : nullptr;
-                    pre[m] = ad ? pc_ld64(ad) : 0ull;
+                    pre[m] = ad ? wv_ld64(ad) : 0ull;
                 }
                 __syncwarp();
             }
@@ -427,11 +370,11 @@ __global__ void __launch_bounds__(32 * pc_geom<T>::WARPS) k_lu_pencil(cf_lu_args
                 }
                 if (yedge_in) {
 #pragma unroll
-                    for (int n = 0; n < 5; n++) yin[n] = pc_get(xch[warp][t][n][lk], T(0));
+                    for (int n = 0; n < 5; n++) yin[n] = wv_get(xch[warp][t][n][lk], T(0));
                 }
                 if (zedge_in) {
 #pragma unroll
-                    for (int n = 0; n < 5; n++) zin[n] = pc_get(xch[warp][t][n][PC_TK + lj], T(0));
+                    for (int n = 0; n < 5; n++) zin[n] = wv_get(xch[warp][t][n][PC_TK + lj], T(0));
                 }
                 const T *P = ring + (gs % PC_DEPTH) * NS * 32 + lane;   // value m at P[(m - WO) * 32]
                 T S[5], N[5];
@@ -461,12 +404,12 @@ __global__ void __launch_bounds__(32 * pc_geom<T>::WARPS) k_lu_pencil(cf_lu_args
                 if (yedge_out && yto >= 0) {
                     unsigned long long *e = pc_yex<T>(w, yto, ci);
 #pragma unroll
-                    for (int n = 0; n < 5; n++) pc_put(e + (n * PC_TK + lk) * W, yo[n], tag);
+                    for (int n = 0; n < 5; n++) wv_put(e + (n * PC_TK + lk) * W, yo[n], tag);
                 }
                 if (zedge_out && zto >= 0) {
                     unsigned long long *e = pc_zex<T>(w, zto, ci);
 #pragma unroll
-                    for (int n = 0; n < 5; n++) pc_put(e + (n * PC_TJ + lj) * W, zo[n], tag);
+                    for (int n = 0; n < 5; n++) wv_put(e + (n * PC_TJ + lj) * W, zo[n], tag);
                 }
                 const size_t q = d.ix(i, j, k);
                 if (FWD) {

@@ -217,7 +217,7 @@ static cudaError_t lu_pencil_pack_t(const cf_dims &d, const cf_lu_args &a, const
         k_lu_pencil_ghost_upper<T><<<box_grid(b), box_block(), 0, s>>>(a, w, b);
         return cudaGetLastError();
     }
-    k_lu_pencil_epoch<<<1, 1, 0, s>>>(w);
+    k_lu_wave_epoch<<<1, 1, 0, s>>>(w, w.npencils);
     const size_t smem = (size_t)WV_PACK * 256 * sizeof(T);
     void (*kf)(cf_lu_args, wave_args, T) = assemble ? k_lu_pencil_pack<T, true> : k_lu_pencil_pack<T, false>;
     cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

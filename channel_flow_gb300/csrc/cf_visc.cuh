@@ -12,10 +12,11 @@
 
 namespace CF_NS {
 
-// the primitive scratch holds the compute type: FP64, or FP32 in the FP32
-// build (the FP64 allocation reinterpreted), so the face kernel's many
-// neighbour reads need no FP64 -> FP32 conversion (a conversion issues to
-// GB300's FP64 pipe, 1/64 of the FP32 rate)
+// the primitive scratch holds the compute type: FP64 (four arrays), or in
+// the FP32 build one float4 (u, v, w, T) per cell over the first two
+// arrays' allocation, so the face kernels' nine to eleven neighbour reads
+// are one 16-byte load each and need no FP64 -> FP32 conversion (a
+// conversion issues to GB300's FP64 pipe, 1/64 of the FP32 rate)
 __device__ __forceinline__ void prim_st(double *p, size_t q, double v) { p[q] = v; }
 __device__ __forceinline__ void prim_st(double *p, size_t q, float v) { reinterpret_cast<float *>(p)[q] = v; }
 template <typename T>
@@ -49,10 +50,14 @@ __global__ void k_visc_prim(cf_dims d, cf_visc_args a, size_t n)
     T Jq = T(a.J[q]);
     T P = (T(a.U[4][q]) - T(0.5) * rho * VV) * (K - T(1)) * Jq;
     T Tt = P / (rho * R) / Jq;
-    prim_st(a.prim[0], q, U);
-    prim_st(a.prim[1], q, V);
-    prim_st(a.prim[2], q, W);
-    prim_st(a.prim[3], q, Tt);
+    if (sizeof(T) == 4) {
+        reinterpret_cast<float4 *>(a.prim[0])[q] = make_float4(float(U), float(V), float(W), float(Tt));
+    } else {
+        prim_st(a.prim[0], q, U);
+        prim_st(a.prim[1], q, V);
+        prim_st(a.prim[2], q, W);
+        prim_st(a.prim[3], q, Tt);
+    }
 }
 
 template <typename T>
@@ -69,6 +74,12 @@ __device__ __forceinline__ vcell<T> ld(const cf_visc_args &a, size_t q)
 {
     return vcell<T>{prim_ld<T>(a.prim[0], q), prim_ld<T>(a.prim[1], q), prim_ld<T>(a.prim[2], q),
                     prim_ld<T>(a.prim[3], q)};
+}
+template <>
+__device__ __forceinline__ vcell<float> ld<float>(const cf_visc_args &a, size_t q)
+{
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(a.prim[0]) + q);
+    return vcell<float>{v.x, v.y, v.z, v.w};
 }
 
 // one-sided difference c - n (Viscous_terms.cpp:400-415)

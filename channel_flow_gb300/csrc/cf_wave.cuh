@@ -205,6 +205,79 @@ __device__ __forceinline__ void st_release(int *p, int v)
     asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
+// Exchange words (the pencil schedule, cf_pencil.cuh): 64 bits per 32-bit
+// part of a value (two parts for double), the part in the low half and a
+// 32-bit tag naming the sweep in the high half, stored and loaded with
+// relaxed 64-bit accesses.  A word either holds this sweep's value or shows
+// that it does not yet, so a consumer polls the words themselves and its
+// producer needs no fence and no flag.  The tag is 2 epoch (forward) or
+// 2 epoch + 1 (backward), the epoch a device counter bumped once per call.
+template <typename T>
+struct wv_w {
+    static constexpr int W = (int)(sizeof(T) / 4);
+};
+
+__device__ __forceinline__ void wv_st64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long wv_ld64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void wv_put(unsigned long long *dst, float v, unsigned tag)
+{
+    wv_st64(dst, ((unsigned long long)tag << 32) | __float_as_uint(v));
+}
+__device__ __forceinline__ void wv_put(unsigned long long *dst, double v, unsigned tag)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    wv_st64(dst, ((unsigned long long)tag << 32) | (b & 0xffffffffull));
+    wv_st64(dst + 1, ((unsigned long long)tag << 32) | (b >> 32));
+}
+__device__ __forceinline__ float wv_get(const unsigned *x, float) { return __uint_as_float(x[0]); }
+__device__ __forceinline__ double wv_get(const unsigned *x, double)
+{
+    return __longlong_as_double((long long)(((unsigned long long)x[1] << 32) | x[0]));
+}
+
+// the epoch word after the claim counter and the error word
+__device__ __forceinline__ int *wv_epoch(const wave_args &w, int nunits)
+{
+    return w.flags + nunits + 2;
+}
+__device__ __forceinline__ unsigned wv_tag(const wave_args &w, int nunits, bool fwd)
+{
+    return 2u * (unsigned)*wv_epoch(w, nunits) + (fwd ? 0u : 1u);
+}
+
+// one thread: the next epoch of the exchange tags
+__global__ void k_lu_wave_epoch(wave_args w, int nunits)
+{
+    *wv_epoch(w, nunits) += 1;
+}
+
+
+// the same terms as tagged exchange words
+template <typename T, bool UPPER>
+__device__ __forceinline__ void wave_ghost_words(const cf_dims &d, const cf_lu_args &a, size_t qg, int dir,
+                                                 const lu_den<T> &den, unsigned long long *face, int nslot, int f,
+                                                 unsigned tag)
+{
+    const lstate<T> s = lu_state<T>(d, a, qg);
+    const lsplit<T> A = wave_split<T>(d, a, qg, s, dir);
+    T P[12], o[5];
+    wave_split12<T, UPPER>(A, P);
+    wave_scale<T>(P, den);
+    const T zero[5] = {T(0), T(0), T(0), T(0), T(0)};
+    if (UPPER) wave_upper_terms<T>(P, zero, den, o);
+    else wave_lower_terms<T>(P, zero, den, o);
+#pragma unroll
+    for (int n = 0; n < 5; n++) wv_put(face + (n * nslot + f) * wv_w<T>::W, o[n], tag);
+}
+
 template <typename T>
 __device__ __forceinline__ T ld_cg(const void *base, size_t q)
 {

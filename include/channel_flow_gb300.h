@@ -131,6 +131,12 @@ int cf_library_version(void);
  * floating-point operations), on cuda_stream; time it with events around
  * the call.  scratch_dev: `blocks` doubles the kernel may write. */
 int cf_fp64_peak_probe(void *cuda_stream, int blocks, int iters, double *scratch_dev);
+/* No counterpart in the reference: a check of the contracted FP64 build's
+ * reciprocal (the hardware's approximate FP64 reciprocal refined by two
+ * Newton-Raphson steps, used in place of divisions): out_dev[q] = 1/d_dev[q]
+ * as the kernels form it, for n device doubles, on cuda_stream.  Normal
+ * inputs only: subnormal d flush to zero and, like d = 0, give NaN. */
+int cf_reciprocal_check(void *cuda_stream, const double *d_dev, double *out_dev, size_t n);
 
 /* ------------------------------------------------------------------ */
 /* host arrays and device mirrors                                        */
