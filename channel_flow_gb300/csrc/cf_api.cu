@@ -568,7 +568,11 @@ CF_FLUX_ENTRY(Flux_Z, 2, false)
 // viscous terms
 
 // f32_io: in FP32 mode, LL/ML/NL and vF hold FP32 values (the step driver)
-static int viscous_common(cf_ctx *c, double **p, bool f32_io, bool static_metrics = false)
+// step_copies: the FP32 step driver's copies of U_ and J for this
+// sub-iteration are current (the viscous terms then run as one pass that
+// writes vF only)
+static int viscous_common(cf_ctx *c, double **p, bool f32_io, bool static_metrics = false,
+                          bool step_copies = false)
 {
     if (!c || !p) return CF_ERR_ARG;
     // read: U (0-4), J (9), face metric sets (19-48); written: vF (5-8),
@@ -603,6 +607,16 @@ static int viscous_common(cf_ctx *c, double **p, bool f32_io, bool static_metric
         if (m32 && !a.Jf32[f]) return fail(c, CF_ERR_NOMEM, "Viscous_terms: FP32 metric copy allocation failed");
         for (int n = 0; n < 9; n++)
             if (m32 && !a.mf32[f][n]) return fail(c, CF_ERR_NOMEM, "Viscous_terms: FP32 metric copy allocation failed");
+    }
+    for (int n = 0; n < 5; n++) a.U32[n] = nullptr;
+    a.J32 = nullptr;
+    if (step_copies && a.f32_io && m32) {
+        // the sub-iteration's FP32 copies of U_ and J (made by Flux_X)
+        const float *sh = reinterpret_cast<const float *>(scratch(c, "flux_f32", 4));
+        if (!sh) return fail(c, CF_ERR_NOMEM, "Viscous_terms: scratch allocation failed");
+        const size_t n = c->d.total();
+        for (int v = 0; v < 5; v++) a.U32[v] = sh + v * n;
+        a.J32 = sh + 5 * n;
     }
     cudaError_t e = exact(c) ? cf_exact::viscous(c->d, a, 0, c->stream)
                     : (a.f32_io && m32) ? cf_drv::viscous(c->d, a, kprec(c), c->stream)
@@ -1497,7 +1511,7 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         }
         c->stream = main;
         if (int rc = cuda_check(c, cudaEventRecord(c->ev_join, c->side), "cf_step")) return rc;
-        if (int rc = viscous_common(c, visc, f32_rhs, static_m)) return rc;
+        if (int rc = viscous_common(c, visc, f32_rhs, static_m, f32_rhs)) return rc;
         if (int rc = cuda_check(c, cudaStreamWaitEvent(main, c->ev_join, 0), "cf_step")) return rc;
         if (int rc = dts_common(c, pp->deltaT, &er[0], &er[1], &er[2], &er[3], &er[4], nullptr, nullptr, dts,
                                 f32_rhs, static_m, f32_rhs)) return rc;

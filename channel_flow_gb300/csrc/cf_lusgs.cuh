@@ -275,6 +275,9 @@ __global__ void __launch_bounds__(256) k_lu_assemble(cf_dims d, cf_lu_args a, cf
     const int f32 = a.f32_lu;
 #pragma unroll
     for (int n = 0; n < 5; n++) rhs_put<T>(a.MR[n], q, MR[n], f32);
+    // the FP32 step driver's sweeps overwrite N at every interior cell, so
+    // its build forms no initial NL, NR
+    if (sizeof(T) == 4 && cf_step_layout) return;
     ldiag<T> g = lu_diag<T>(d, a, q, s, deltaT);
     T nl[5] = {g.d11 * MR[0], g.d22 * MR[1], g.d22 * MR[2], g.d22 * MR[3], g.d51 * MR[0] + g.d22 * MR[4]};
 #pragma unroll
@@ -673,7 +676,8 @@ __device__ __forceinline__ void lu_update_cell_f32(const cf_dims &d, const cf_lu
     for (int n = 0; n < 5; n++) {
         a.U_[n][q] = u[n] + f2d(dc[n] * iJ);
         const double x = f2d(e[n]), r = x * x;
-        a.Res[n][q] = r;
+        // the step driver reads no Residual array: only the drop-in writes it
+        if (!cf_step_layout) a.Res[n][q] = r;
         acc[n] = fma(r, r, acc[n]);
     }
 }
@@ -693,11 +697,13 @@ __global__ void __launch_bounds__(256) k_lu_update(cf_dims d, cf_lu_args a, cf_b
             if (sizeof(T) == 4) {
                 // FP32: also NL <- NR here (the arrays may hold FP32 values,
                 // which the FP64 copy kernel would pair up wrongly)
+                // (the step driver reads neither NL nor Residual afterwards:
+                // its build writes neither)
                 float nr[5];
 #pragma unroll
                 for (int n = 0; n < 5; n++) {
                     nr[n] = rhs_get<float>(a.NR[n], q, a.f32_lu);
-                    rhs_put<float>(a.NL[n], q, nr[n], a.f32_lu);
+                    if (!cf_step_layout) rhs_put<float>(a.NL[n], q, nr[n], a.f32_lu);
                 }
                 lu_update_cell_f32(d, a, q, nr, r2);
             } else {

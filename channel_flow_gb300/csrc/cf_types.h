@@ -111,6 +111,8 @@ struct cf_visc_args {
     int f32_io;                // FP32 build: LL/ML/NL and vF hold FP32 values (the step driver's internal use)
     int reserved;
     const float *Jf32[3], *mf32[3][9];   // FP32 copies of the face sets (or null)
+    // FP32 step driver: this sub-iteration's FP32 copies of U_ and J (or null)
+    const float *U32[5], *J32;
 };
 
 struct cf_filter_args {

@@ -633,7 +633,9 @@ __global__ void __launch_bounds__(32 * WV_WARPS) k_lu_wave(cf_lu_args a, wave_ar
             if (FWD) static_cast<T *>(w.nl)[(size_t)tile * WV_SM_NL + v] = x;
             if (li < ti && lj < tj && lk < tk) {
                 const size_t q = d.ix(i0 + li, j0 + lj, k0 + lk);
-                if (FWD) rhs_put<T>(a.NL[n], q, x, a.f32_lu);
+                // (the FP32 step driver reads the forward N from the tile
+                // layout only)
+                if (FWD && !(sizeof(T) == 4 && cf_step_layout)) rhs_put<T>(a.NL[n], q, x, a.f32_lu);
                 else rhs_put<T>(a.NR[n], q, x, a.f32_lu);
             }
         }
