@@ -297,10 +297,17 @@ __device__ __forceinline__ void visc_face_z(const vconst<T> &k, const vmet<T> &M
 }
 
 // FACE 0/1/2: the x, y or z face of every cell, one launch each (the
-// register footprint of one face: no spills in FP64, and in FP32 twice the
-// resident warps of a kernel doing all three faces, which measured slower)
+// register footprint of one face: in FP32 twice the resident warps of a
+// kernel doing all three faces, which measured slower).  Blocks per SM:
+// FP32 3; FP64 2 in the contracted build (128 registers, no spills), 1 in
+// the no-FMA build (whose longer expression trees would spill at 128)
+#ifdef CF_FAST_MATH
+constexpr int VF_FP64_BLOCKS = 2;
+#else
+constexpr int VF_FP64_BLOCKS = 1;
+#endif
 template <typename T, int FACE>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : VF_FP64_BLOCKS) k_visc_faces(cf_dims d, cf_visc_args a, cf_box b)
 {
     CF_BOX_INDEX(b, i, j, k);
     const vconst<T> kc = visc_consts<T>(d);
