@@ -377,7 +377,7 @@ __device__ __forceinline__ float4 visc_prim32(const cf_dims &d, const cf_visc_ar
     return make_float4(U, V, W, Tt);
 }
 
-__global__ void __launch_bounds__(256, 2) k_visc_march(cf_dims d, cf_visc_args a, int fti)
+__global__ void __launch_bounds__(256, 3) k_visc_march(cf_dims d, cf_visc_args a, int fti)
 {
     __shared__ float4 sp[3][VM_HJ][VM_HK];
     __shared__ float syf[4][VM_TJ + 1][VM_TK];
