@@ -951,8 +951,7 @@ def mlp_gemms(torch, rows, steps=5, warmup=2):
         ("fwd_L3", lambda: net.gemm(net.H2, net.W3b, M, N3, H, mlp.EPI_BIAS, b3, net.Y, None, N3), M, N3, H),
         ("bwd_dH2", lambda: net.gemm(net.dY, net.W3p, M, H, K3, mlp.EPI_F32, None, net.dH, None, H), M, H, K3),
         ("bwd_dH1", lambda: net.gemm(net.dZ2, net.W2T, M, H, H, mlp.EPI_F32, None, net.dH, None, H), M, H, H),
-        ("bwd_dW1", lambda: net.gemm(net.dZ1T, net.XT, H, K1, M, mlp.EPI_F32, None, net.view("W1", g), None, K1),
-         H, K1, M),
+        ("bwd_dW1", lambda: net.gemm_wgrad(net.dZ1T, net.XT, H, K1, M, net.view("W1", g)), H, K1, M),
     ]
     # one full training step first, so that every operand holds data
     net.step(M, M)

@@ -116,6 +116,7 @@ _SIGS = {
     "cf_step_scale": ([P, P, C.c_int], C.c_int),
     "cf_step_residuals": ([P, P, C.c_int, P], C.c_int),
     "cf_gemm_bf16": ([P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P], C.c_int),
+    "cf_gemm_bf16_splitk": ([P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P], C.c_int),
     "cf_mlp_features": ([P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
     "cf_mlp_targets": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, C.c_longlong, C.c_longlong, P], C.c_int),
     "cf_mlp_apply": ([P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P], C.c_int),

@@ -104,7 +104,10 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
     constexpr uint32_t IDESC = mma_idesc(BM, BN);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-    const int KT = K / BK;
+    // split K (EPI_F32 only): CTA z forms the partial product over K-slabs
+    // kt0 .. kt1-1 into its own slice of the output
+    const int KT = K / BK, kt0 = (int)(((long long)KT * blockIdx.z) / gridDim.z),
+              kt1 = (int)(((long long)KT * (blockIdx.z + 1)) / gridDim.z);
     unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(dsm) + 1023) &
                                                             ~static_cast<uintptr_t>(1023));
     const uint32_t sbase = saddr(base);
@@ -129,10 +132,10 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
 
     if (warp == 0 && lane == 0) {
         // TMA producer
-        for (int kt = 0; kt < KT; kt++) {
-            const int s = kt % STAGES;
-            const uint32_t ph = (uint32_t)(kt / STAGES) & 1u;
-            if (kt >= STAGES && !mbar_wait(saddr(&empty[s]), ph ^ 1u)) {
+        for (int kt = kt0; kt < kt1; kt++) {
+            const int t = kt - kt0, s = t % STAGES;
+            const uint32_t ph = (uint32_t)(t / STAGES) & 1u;
+            if (t >= STAGES && !mbar_wait(saddr(&empty[s]), ph ^ 1u)) {
                 atomicOr(err, 1);
                 break;
             }
@@ -151,9 +154,9 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         bool ok = true;
-        for (int kt = 0; kt < KT; kt++) {
-            const int s = kt % STAGES;
-            const uint32_t ph = (uint32_t)(kt / STAGES) & 1u;
+        for (int kt = kt0; kt < kt1; kt++) {
+            const int t = kt - kt0, s = t % STAGES;
+            const uint32_t ph = (uint32_t)(t / STAGES) & 1u;
             if (!mbar_wait(saddr(&full[s]), ph)) {
                 atomicOr(err, 2);
                 ok = false;
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
 #pragma unroll
             for (int kk = 0; kk < BK / 16; kk++) {
                 const uint64_t ad = sw128_desc(da + kk * 32), bd = sw128_desc(db + kk * 32);
-                const uint32_t acc = (kt | kk) != 0;
+                const uint32_t acc = (t | kk) != 0;
                 asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
                              :: "r"(tmem), "l"(ad), "l"(bd), "r"(IDESC), "r"(acc) : "memory");
@@ -214,7 +217,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
                     o[0] = *reinterpret_cast<const uint4 *>(&h[0]);
                     o[1] = *reinterpret_cast<const uint4 *>(&h[8]);
                 } else {
-                    float4 *o = reinterpret_cast<float4 *>(e.outf + (size_t)row * e.ldo + col);
+                    float4 *o = reinterpret_cast<float4 *>(e.outf + (size_t)blockIdx.z * M * e.ldo +
+                                                           (size_t)row * e.ldo + col);
 #pragma unroll
                     for (int t = 0; t < 4; t++) o[t] = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]);
                 }
@@ -263,21 +267,32 @@ static bool make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int bo
 
 template <int BN, int STAGES>
 static cudaError_t launch_gemm_st(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K,
-                                  const gemm_epi &e, int *err, cudaStream_t s)
+                                  const gemm_epi &e, int *err, cudaStream_t s, int splits)
 {
     constexpr size_t smem = (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 1024;
     cudaError_t r = cudaFuncSetAttribute(k_gemm_tn<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (r != cudaSuccess) return r;
-    dim3 g((unsigned)(M / BM), (unsigned)(N / BN));
+    dim3 g((unsigned)(M / BM), (unsigned)(N / BN), (unsigned)splits);
     k_gemm_tn<BN, STAGES><<<g, 128, smem, s>>>(ta, tb, M, N, K, e, err);
     return cudaGetLastError();
 }
 
 template <int BN>
 static cudaError_t launch_gemm(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K, const gemm_epi &e,
-                               int *err, cudaStream_t s)
+                               int *err, cudaStream_t s, int splits = 1)
 {
-    return K <= 512 ? launch_gemm_st<BN, 2>(ta, tb, M, N, K, e, err, s) : launch_gemm_st<BN, 4>(ta, tb, M, N, K, e, err, s);
+    return K / splits <= 512 ? launch_gemm_st<BN, 2>(ta, tb, M, N, K, e, err, s, splits)
+                             : launch_gemm_st<BN, 4>(ta, tb, M, N, K, e, err, s, splits);
+}
+
+// out[i] = the sum of the split-K partials of element i, in split order
+__global__ void k_splitk_sum(const float *partial, int splits, size_t n, float *out)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float v = 0.f;
+    for (int z = 0; z < splits; z++) v += partial[(size_t)z * n + i];
+    out[i] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -720,6 +735,35 @@ int cf_gemm_bf16(void *stream, const void *A, const void *B, int M, int N, int K
     default: r = launch_gemm<16>(ta, tb, M, N, K, e, err_dev, s); break;
     }
     return r == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
+
+// C = A B^T in FP32 with K split over `splits` CTAs per output tile
+// (see channel_flow_gb300.h)
+int cf_gemm_bf16_splitk(void *stream, const void *A, const void *B, int M, int N, int K, int splits,
+                        float *partial, float *out, int *err_dev)
+{
+    if (!A || !B || !out || !partial || !err_dev || splits < 1) return CF_ERR_ARG;
+    if (M <= 0 || N <= 0 || K <= 0 || M % BM || K % BK || N % 16 || splits > K / BK) return CF_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) return CF_ERR_ARG;
+    int bn = 0;
+    for (int c : {256, 128, 64, 32, 16})
+        if (N % c == 0) { bn = c; break; }
+    CUtensorMap ta, tb;
+    if (!make_map(&ta, A, M, K, BM) || !make_map(&tb, B, N, K, bn)) return CF_ERR_CUDA;
+    gemm_epi e{EPI_F32, nullptr, partial, nullptr, nullptr, N};
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t r;
+    switch (bn) {
+    case 256: r = launch_gemm<256>(ta, tb, M, N, K, e, err_dev, s, splits); break;
+    case 128: r = launch_gemm<128>(ta, tb, M, N, K, e, err_dev, s, splits); break;
+    case 64: r = launch_gemm<64>(ta, tb, M, N, K, e, err_dev, s, splits); break;
+    case 32: r = launch_gemm<32>(ta, tb, M, N, K, e, err_dev, s, splits); break;
+    default: r = launch_gemm<16>(ta, tb, M, N, K, e, err_dev, s, splits); break;
+    }
+    if (r != cudaSuccess) return CF_ERR_CUDA;
+    const size_t n = (size_t)M * N;
+    k_splitk_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(partial, splits, n, out);
+    return cudaGetLastError() == cudaSuccess ? CF_OK : CF_ERR_CUDA;
 }
 
 static mlp_levels levels(const double *const *u15)

@@ -37,6 +37,7 @@ from . import _lib
 
 IN, K1, H, OUT, N3, K3 = 270, 320, 128, 5, 16, 64
 EPI_F32, EPI_SILU, EPI_BIAS = 0, 1, 2
+WGRAD_PARTIAL = 1 << 23          # floats of split-K partial products (32 MB)
 
 # flat parameter vector: W1 [128 x 320], b1 [128], W2 [128 x 128], b2 [128],
 # W3T [128 x 16] (the transposed output layer), b3 [16]
@@ -126,6 +127,10 @@ class LearnedGuess:
         self.partial = torch.zeros(M // 256 * 6, dtype=f32, device=dev)
         self.rms_partial = torch.zeros(30 * 512, dtype=torch.float64, device=dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        # split-K partial products of the weight gradients (their outputs are
+        # one to five 128-row tiles, their reduction runs over the rows)
+        self.sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        self.wpart = torch.zeros(WGRAD_PARTIAL, dtype=f32, device=dev)
         self.scale = torch.ones(10, dtype=f32, device=dev)
         self.coef = np.ones(10)                             # predictor a[0..4], b[5..9] (quadratic extrapolation)
         self.D = None                                       # FP32 time differences of the whole-grid feature rows
@@ -163,6 +168,16 @@ class LearnedGuess:
                                    None if zout is None else zout.data_ptr(), ldo, self.err.data_ptr())
         self._ok(rc, "cf_gemm_bf16")
 
+    def gemm_wgrad(self, A, B, M, N, K, out):
+        """out[M x N] (FP32) = A B^T with the reduction over K (rows) split
+        so that about two waves of CTAs run (cf_gemm_bf16_splitk)."""
+        bn = next(c for c in (256, 128, 64, 32, 16) if N % c == 0)
+        tiles = (M // 128) * (N // bn)
+        splits = max(1, min(K // 64, -(-2 * self.sms // tiles), WGRAD_PARTIAL // (M * N)))
+        rc = self.lib.cf_gemm_bf16_splitk(self._s(), A.data_ptr(), B.data_ptr(), M, N, K, splits,
+                                          self.wpart.data_ptr(), out.data_ptr(), self.err.data_ptr())
+        self._ok(rc, "cf_gemm_bf16_splitk")
+
     def check_device(self):
         if int(self.err.item()):
             raise RuntimeError("a tensor-core GEMM wait ran out on the device")
@@ -193,9 +208,9 @@ class LearnedGuess:
         # weight gradients: reductions over the rows as K of the GEMM
         for src, dst, cols in ((self.H2, self.H2T, H), (self.H1, self.H1T, H), (self.X, self.XT, K1)):
             self._ok(self.lib.cf_transpose_bf16(s, src.data_ptr(), Mpad, cols, dst.data_ptr()), "cf_transpose_bf16")
-        self.gemm(self.H2T, self.dYT, H, N3, Mpad, EPI_F32, None, self.view("W3T", self.g), None, N3)
-        self.gemm(self.dZ2T, self.H1T, H, H, Mpad, EPI_F32, None, self.view("W2", self.g), None, H)
-        self.gemm(self.dZ1T, self.XT, H, K1, Mpad, EPI_F32, None, self.view("W1", self.g), None, K1)
+        self.gemm_wgrad(self.H2T, self.dYT, H, N3, Mpad, self.view("W3T", self.g))
+        self.gemm_wgrad(self.dZ2T, self.H1T, H, H, Mpad, self.view("W2", self.g))
+        self.gemm_wgrad(self.dZ1T, self.XT, H, K1, Mpad, self.view("W1", self.g))
         for src, name, cols in ((self.dZ1, "b1", H), (self.dZ2, "b2", H)):
             self._ok(self.lib.cf_colsum_bf16(s, src.data_ptr(), Mpad, cols, self.view(name, self.g).data_ptr()),
                      "cf_colsum_bf16")

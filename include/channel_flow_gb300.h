@@ -404,6 +404,14 @@ int cf_step_residuals(cf_ctx *ctx, double *out, int cap, int *count);
  * gets a nonzero bit if a bounded device wait ran out. */
 int cf_gemm_bf16(void *cuda_stream, const void *A, const void *B, int M, int N, int K, int epilogue,
                  const float *bias, void *out, float *zout, int ldo, int *err_dev);
+/* C = A B^T in FP32 (out [M x N], row-major) with the reduction dimension
+ * split over `splits` CTAs per 128-row output tile, for products whose
+ * output has few tiles and whose K is long (the weight gradients, K =
+ * rows): each split writes its partial product to partial (splits x M x N
+ * floats), then the partials are summed in split order.  1 <= splits <=
+ * K / 64; the other constraints as cf_gemm_bf16's. */
+int cf_gemm_bf16_splitk(void *cuda_stream, const void *A, const void *B, int M, int N, int K, int splits,
+                        float *partial, float *out, int *err_dev);
 
 
 /* The per-cell MLP of the learned initial guess (270 -> 128 -> 128 -> 5,

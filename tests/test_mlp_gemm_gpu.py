@@ -59,3 +59,30 @@ def test_gemm_bias_f32(cuda_lib):
     ref, bias, out, _ = _run(256, 16, 128, 2, seed=2)
     zr = ref + bias
     assert float((out - zr).abs().max() / zr.abs().max()) <= 1e-5
+
+
+@pytest.mark.parametrize("M,N,K,splits", [(128, 320, 131072, 60), (128, 128, 65536, 300), (128, 16, 8192, 128),
+                                          (256, 64, 4096, 7), (128, 320, 640, 10), (128, 64, 512, 1)])
+def test_gemm_splitk_fp32_out(M, N, K, splits, cuda_lib):
+    """The weight-gradient form: K split over `splits` CTAs per tile (uneven
+    slab counts included), partials summed in split order, against the
+    FP32 product of the same BF16 values."""
+    import torch
+    from channel_flow_gb300 import _lib
+    lib = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    A = torch.randn(M, K, generator=g, device="cuda").to(torch.bfloat16)
+    B = torch.randn(N, K, generator=g, device="cuda").to(torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    partial = torch.full((splits * M * N,), float("nan"), device="cuda")
+    out = torch.full((M, N), float("nan"), device="cuda")
+    rc = lib.cf_gemm_bf16_splitk(torch.cuda.current_stream().cuda_stream, A.data_ptr(), B.data_ptr(), M, N, K,
+                                 splits, partial.data_ptr(), out.data_ptr(), err.data_ptr())
+    torch.cuda.synchronize()
+    assert rc == 0 and int(err.item()) == 0
+    ref = A.float() @ B.float().t()
+    rel = float((out - ref).abs().max() / ref.abs().max())
+    assert rel <= 1e-5, rel
+    # more splits than K-slabs is refused before any launch
+    assert lib.cf_gemm_bf16_splitk(None, A.data_ptr(), B.data_ptr(), M, N, K, K // 64 + 1, partial.data_ptr(),
+                                   out.data_ptr(), err.data_ptr()) == _lib.CF_ERR_ARG
