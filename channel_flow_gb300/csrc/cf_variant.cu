@@ -193,11 +193,8 @@ static cudaError_t lu_wave_pack_t(const cf_dims &d, const cf_lu_args &a, const c
         k_lu_tile_ghost_upper<T><<<box_grid(b), box_block(), 0, s>>>(a, w, b);
         return cudaGetLastError();
     }
-    const size_t smem = (size_t)WV_CELLS * WV_PACK * sizeof(T);
     void (*kf)(cf_lu_args, wave_args, T) = assemble ? k_lu_tile_pack<T, true> : k_lu_tile_pack<T, false>;
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    kf<<<w.ntiles, WV_CELLS, smem, s>>>(a, w, T(dt));
+    kf<<<w.ntiles, WV_CELLS, 0, s>>>(a, w, T(dt));
     return cudaGetLastError();
 }
 // assemble: the forward pack also assembles MR (no lu_prepare assembly pass)

@@ -284,29 +284,18 @@ __device__ __forceinline__ T ld_cg(const void *base, size_t q)
     return __ldcg(static_cast<const T *>(base) + q);
 }
 
-// shared-memory tile -> global with one bulk async copy (TMA), waiting until
-// the shared source may be reused
-__device__ __forceinline__ void wave_bulk_store(void *gdst, const void *ssrc, unsigned bytes)
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
-                 :: "l"(gdst), "r"(smem_u32(ssrc)), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-
 // Tile packs, one block (256 threads, one per cell) per tile, after
-// k_lu_assemble (MR written); each pack is assembled in shared memory and
-// stored with one bulk copy.  Also the terms of the ghost neighbours on
-// the three lower faces of the domain.
+// k_lu_assemble (MR written).  Value m of the tile's cells is 256
+// consecutive elements of the pack, so each thread stores its cell's values
+// straight to HBM and every warp store is one contiguous 128-byte (FP64:
+// 256-byte) row; no shared-memory staging limits the blocks per SM.  Also
+// the terms of the ghost neighbours on the three lower faces of the domain.
 // ASM: also the assembly of the tile's cells (lu_mr, MR written), which the
 // wavefront then needs no separate pass for; the initial NL, NR of the
 // assembly kernel are not formed (the sweeps overwrite every interior cell)
 template <typename T, bool ASM>
 __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w, T dt)
 {
-    extern __shared__ __align__(128) unsigned char pack_smem[];
-    T *sp = reinterpret_cast<T *>(pack_smem);     // [WV_PACK][WV_CELLS]
     const cf_dims &d = w.d;
     const int tile = blockIdx.x;
     int ta, tb, tc;
@@ -316,7 +305,8 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
     const int i = 3 + ta * WV_TI + li, j = 2 + tb * WV_TJ + lj, k = 2 + tc * WV_TK + lk;
     const bool in = i <= d.gend && j <= d.ny && k <= d.nz;
     const lu_den<T> den[3] = {lu_den<T>(CF_DC(T, d, dXI)), lu_den<T>(CF_DC(T, d, dET)), lu_den<T>(CF_DC(T, d, dZT))};
-    T *P = sp + c;                                // value m of this cell at P[m * WV_CELLS]
+    // value m of this cell at P[m * WV_CELLS] of the tile's pack
+    T *P = static_cast<T *>(w.pack) + (size_t)tile * WV_CELLS * WV_PACK + c;
     lsplit<T> A[3];
     ldiag<T> g;
     size_t q = 0;
@@ -350,9 +340,6 @@ __global__ void __launch_bounds__(256) k_lu_tile_pack(cf_lu_args a, wave_args w,
             P[(45 + n) * WV_CELLS] = MR[n];
         }
     }
-    const unsigned bytes = (unsigned)(WV_CELLS * WV_PACK * sizeof(T));
-    __syncthreads();
-    if (c == 0) wave_bulk_store(static_cast<T *>(w.pack) + (size_t)tile * WV_CELLS * WV_PACK, sp, bytes);
     if (in) {
         if (i == 3) wave_ghost_term<T, false>(d, a, q - d.plane(), 0, den[0], wave_face<T>(w, 0, tile), WV_FX,
                                               lj * WV_TK + lk);
