@@ -30,6 +30,7 @@ struct cf_ctx {
     double E[5] = {0, 0, 0, 0, 0};    // running maxima of the residual norms (main.cpp:63, 387-391)
     std::vector<double> er_hist;      // normalised er1..er5 of every iteration of the last cf_step
     std::unordered_map<const double *, float *> met32;   // FP32 copies of fixed metric arrays (cf_step)
+    const double *shadow_j = nullptr;   // the fixed J whose FP32 J, 1/J the flux shadow holds (cf_step)
     std::unordered_map<const double *, double *> mirrors;
     std::unordered_map<std::string, std::pair<double *, size_t>> scratch;
     std::vector<int> nijk;            // plane tables, Hyperplane layout (host)
@@ -535,11 +536,17 @@ static int flux_common(cf_ctx *c, const char *who, int dir, bool limited, double
             for (int n = 0; n < 10; n++)
                 if (!m32[n]) return fail(c, CF_ERR_NOMEM, "%s: FP32 metric copy allocation failed", who);
         }
+        // with fixed metrics the shadow's J and 1/J, once made from this J,
+        // stay current: only U is converted again (a null J skips them)
+        const double *J_in = a.J;
+        if (static_metrics && !reuse_shadow && a.J && c->shadow_j == a.J) a.J = nullptr;
         // the step driver's layout (FP32 outputs, FP32 metric copies): the
         // variant compiled for it
         auto fn = (a.f32_out && static_metrics) ? cf_drv::flux_f32 : cf_fast::flux_f32;
-        return cuda_check(c, fn(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow, static_metrics ? m32 : nullptr,
-                                dir, limited, c->stream), who);
+        const int rc = cuda_check(c, fn(c->d, a, reinterpret_cast<float *>(sh), !reuse_shadow,
+                                        static_metrics ? m32 : nullptr, dir, limited, c->stream), who);
+        if (!reuse_shadow) c->shadow_j = (rc == CF_OK && static_metrics) ? J_in : nullptr;
+        return rc;
     }
     cudaError_t e = exact(c) ? cf_exact::flux(c->d, a, dir, limited, 0, c->stream)
                              : cf_fast::flux(c->d, a, dir, limited, 0, c->stream);
@@ -1365,6 +1372,7 @@ int cf_step_reset(cf_ctx *c)
         for (auto &m : c->met32) cudaFree(m.second);
         c->met32.clear();
     }
+    c->shadow_j = nullptr;
     return CF_OK;
 }
 
