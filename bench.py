@@ -412,20 +412,23 @@ def main():
         return 0
     if args.step == "schedule":
         torch.cuda.set_device(local)
-        r = schedule_run(torch, args.config, steps=args.schedule_steps or None,
-                         compare_steps=args.compare_steps or None, dt_factor=args.dt_factor)
+        with solver_stream(torch):
+            r = schedule_run(torch, args.config, steps=args.schedule_steps or None,
+                             compare_steps=args.compare_steps or None, dt_factor=args.dt_factor)
         if rank == 0:
             print(json.dumps({"step": "schedule", **r}))
         return 0
     if args.step == "northstar":
         torch.cuda.set_device(local)
-        r = physical_step_to_tolerance(torch)
+        with solver_stream(torch):
+            r = physical_step_to_tolerance(torch)
         if rank == 0:
             print(json.dumps({"step": "northstar", "physical_step_to_tolerance": r}))
         return 0
     if args.step == "physical":
         torch.cuda.set_device(local)
-        r = physical_steps(torch, g, args.precision, args.steps, args.warmup)
+        with solver_stream(torch):
+            r = physical_steps(torch, g, args.precision, args.steps, args.warmup)
         if rank == 0:
             print(json.dumps(r))
         return 0
@@ -649,6 +652,13 @@ def northstar_case(torch, dims, precision):
     return g, ctx, w, syn.time_step(g, NS_MACH) * NS_DT_FACTOR
 
 
+def solver_stream(torch):
+    """The physical steps run on a stream of the highest priority: cf_step's
+    Statistic (its own stream, the least priority) then fills what the
+    solver's kernels leave of the SMs instead of taking SMs from them."""
+    return torch.cuda.stream(torch.cuda.Stream(priority=-1))
+
+
 def physical_steps(torch, g, precision, steps, warmup):
     """`warmup` then `steps` timed physical steps (cf_step to the tolerance
     1e-6 from the extrapolated start, Statistic every step) of the
@@ -660,23 +670,27 @@ def physical_steps(torch, g, precision, steps, warmup):
     st.kw["statistic_step"] = 1 << 30          # Statistic accumulates every step, as in the comparison
     for n in range(max(warmup, 3)):
         st.step("extrapolate" if n >= 2 else None)
-    its, ms = [], []
-    # the timed steps alone for a profiler started with --profile-from-start off
+    its = []
+    # the timed steps alone for a profiler started with --profile-from-start
+    # off; timed as one region that ends after the last step's Statistic
+    # (each step's Statistic runs beside the next step)
+    ctx.statistic_flush()
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
     for _ in range(steps):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        it = st.step("extrapolate")[0]
-        e1.record()
-        torch.cuda.synchronize()
-        its.append(it)
-        ms.append(e0.elapsed_time(e1))
+        its.append(st.step("extrapolate")[0])
+    ctx.statistic_flush()
+    e1.record()
+    torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStop()
+    total = e0.elapsed_time(e1)
     ctx.close()
     return {"step": "physical", "grid": [g.X_out, g.Y_out, g.Z_out], "precision": precision,
-            "subiterations": its, "ms_per_step": ms, "ms_per_subiteration": sum(ms) / max(1, sum(its))}
+            "subiterations": its, "ms_total": total, "ms_per_step": total / max(1, steps),
+            "ms_per_subiteration": total / max(1, sum(its))}
 
 
 # The configurations' fixed schedules: 10 LU-SGS sub-iterations per step
@@ -738,25 +752,30 @@ def schedule_run(torch, key, steps=None, compare_steps=None, precisions=("fp64",
                              max_iterations=LU_SUBITERATIONS, tolerance=0.0, limiter=True, filter=True,
                              statistic_step=1 << 30)
         ctx.statistic_reset()
-        ms, r, at_cmp = [], {"steps": n_steps}, None
+        done, r, at_cmp = 0, {"steps": n_steps}, None
         cmp_at = compare_steps or steps
+        # one timed region over the steps, ending after the last step's
+        # Statistic (each step's Statistic runs beside the next step)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
         try:
             for n in range(1, n_steps + 1):
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record()
                 st.step(None)
-                e1.record()
-                torch.cuda.synchronize()
-                ms.append(e0.elapsed_time(e1))
+                done = n
                 if n == cmp_at:
                     at_cmp = (stat_profiles(ctx.statistic_read(), g, n), [u.clone() for u in st.f["U"]])
+            ctx.statistic_flush()
         except Exception as exc:     # a diverged run is reported with its step
-            r["failed_at_step"] = len(ms) + 1
+            r["failed_at_step"] = done + 1
             r["error"] = str(exc)
-        r["s_per_step_mean"] = float(np.mean(ms)) * 1e-3 if ms else None
-        r["s_total"] = float(np.sum(ms)) * 1e-3
-        r["ms_per_subiteration"] = float(np.mean(ms)) / LU_SUBITERATIONS if ms else None
+        e1.record()
+        torch.cuda.synchronize()
+        total = e0.elapsed_time(e1)
+        r["s_per_step_mean"] = total / done * 1e-3 if done else None
+        r["s_total"] = total * 1e-3
+        r["ms_per_subiteration"] = total / done / LU_SUBITERATIONS if done else None
         if at_cmp is not None:
             prof, state = at_cmp
             r["profiles_at_step"] = cmp_at
@@ -853,22 +872,26 @@ def physical_step_to_tolerance(torch, dims=(256, 192, 192), harvest=48, evals=4,
         ctx.step_scale(E)
         ctx.statistic_reset()
         st.kw["statistic_step"] = 1 << 30
-        its, ms, last = [], [], []
+        its, last = [], []
+        # the timed steps as one region that ends after the last step's
+        # Statistic (each step's Statistic runs beside the next step)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
         for _ in range(evals):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
             it, er, q = st.step(guess)
-            e1.record()
-            torch.cuda.synchronize()
             its.append(it)
-            ms.append(e0.elapsed_time(e1))
             last.append(float(max(er[:4])))
+        ctx.statistic_flush()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / evals
         st.kw["max_iterations"] = NS_STEP["max_iterations"]
         prof = stat_profiles(ctx.statistic_read(), g, evals)
         final = [u.clone() for u in st.f["U"]]
-        r = {"subiterations": its, "ms_per_step": [round(x, 3) for x in ms],
-             "s_per_step_mean": float(np.mean(ms)) * 1e-3, "final_max_er_over_E": last}
+        r = {"subiterations": its, "ms_per_step": round(ms, 3),
+             "s_per_step_mean": ms * 1e-3, "final_max_er_over_E": last}
         if ref is None:
             ref = (prof, final)
         else:
@@ -1055,7 +1078,8 @@ def secondary(ctx, g, w, calls, stream, torch, args):
             out["mlp_gemm"] = {"error": repr(exc)}
     if not args.no_large and not args.no_learned:
         try:
-            out["physical_step_to_tolerance"] = physical_step_to_tolerance(torch)
+            with solver_stream(torch):
+                out["physical_step_to_tolerance"] = physical_step_to_tolerance(torch)
         except Exception as exc:
             out["physical_step_to_tolerance"] = {"error": repr(exc)}
     out["note"] = ("per grid: physical step = 10 LU-SGS sub-iterations x (RHS + Dual_time_stepping), the "

@@ -134,6 +134,10 @@ class Context:
     def statistic_reset(self):
         self._ok(self.lib.cf_statistic_reset(self.h))
 
+    def statistic_flush(self):
+        """Completes the Statistic the last step left running (host part)."""
+        self._ok(self.lib.cf_statistic_flush(self.h))
+
     def Output(self, step, *arrays, myid=0):
         """U1..U5, U1q..U5q, J -> LES%05d.bin"""
         if len(arrays) != 11:

@@ -109,6 +109,7 @@ _SIGS = {
     "cf_Statistic": ([P, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(P)], C.c_int),
     "cf_statistic_read": ([P, P], C.c_int),
     "cf_statistic_reset": ([P], C.c_int),
+    "cf_statistic_flush": ([P], C.c_int),
     "cf_Output": ([P, C.c_int, C.c_int] + [P] * 11, C.c_int),
     "cf_Initial_condition": ([P, C.c_int] + [P] * 16, C.c_int),
     "cf_step": ([P, P, C.c_int, P, P, P, P], C.c_int),

@@ -42,6 +42,13 @@ struct cf_ctx {
     cudaStream_t cap = nullptr;       // private stream for graph capture
     cudaStream_t side = nullptr;      // cf_step: Flux_Y/Z beside the viscous terms
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // cf_step's Statistic: its kernels on a stream of their own, from a copy
+    // of the step's final U_, beside the next call's work; the host part
+    // (accumulators to the host, the files) of step stat_step is pending
+    cudaStream_t stat_stream = nullptr;
+    cudaEvent_t ev_stat = nullptr;
+    bool stat_pending = false;
+    int stat_step = 0, stat_every = 0;
     int lu_schedule = CF_LU_WAVEFRONT;                // hyperplane sweep schedule
     unsigned wait_limit = CF_WAVE_SPIN_LIMIT;         // polls of a wavefront dependency wait
     int *tile_order = nullptr;        // wavefront tiles sorted by plane (device)
@@ -266,6 +273,7 @@ int cf_create(const cf_grid *g, int precision, cf_ctx **out)
 void cf_destroy(cf_ctx *c)
 {
     if (!c) return;
+    cf_statistic_flush(c);
     for (auto &m : c->mirrors) cudaFree(m.second);
     for (auto &s : c->scratch) cudaFree(s.second.first);
     if (c->ijk_dev) cudaFree(c->ijk_dev);
@@ -280,6 +288,8 @@ void cf_destroy(cf_ctx *c)
     if (c->side) cudaStreamDestroy(c->side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->stat_stream) cudaStreamDestroy(c->stat_stream);
+    if (c->ev_stat) cudaEventDestroy(c->ev_stat);
     for (auto &m : c->met32) cudaFree(m.second);
     delete c;
 }
@@ -1190,8 +1200,9 @@ int cf_Driven_force(cf_ctx *c, int, double *U2_, double *J, double *Q, double *E
     if (!c || !U2_ || !J) return CF_ERR_ARG;
     const cf_dims &d = c->d;
     double *rows = scratch(c, "bulk_rows", 1);            // Y_m row sums + Jsum, inside one field
+    // (its own partials: cf_step's Statistic may still be running beside it)
     const size_t plen = (size_t)4 * 152 * 9 + (size_t)d.Ym * 64;
-    double *partial = static_cast<double *>(scratch_bytes(c, "stat_partial", plen * sizeof(double)));
+    double *partial = static_cast<double *>(scratch_bytes(c, "bulk_partial", plen * sizeof(double)));
     if (!rows || !partial) return fail(c, CF_ERR_NOMEM, "Driven_force: scratch allocation failed");
     double *jsum = rows + d.Ym;
     cudaError_t e = cf_fast::bulk_rows(d, R(c, U2_), R(c, J), jsum, rows, partial, plen, c->stream);
@@ -1222,6 +1233,7 @@ static int stat_alloc(cf_ctx *c)
 int cf_statistic_reset(cf_ctx *c)
 {
     if (!c) return CF_ERR_ARG;
+    if (int rc = cf_statistic_flush(c)) return rc;
     if (int rc = stat_alloc(c)) return rc;
     c->sxy_bottom = c->sxy_up = 0;
     return cuda_check(c, cudaMemsetAsync(c->stat_acc, 0, (size_t)17 * c->d.Ym * sizeof(double), c->stream),
@@ -1231,6 +1243,7 @@ int cf_statistic_reset(cf_ctx *c)
 int cf_statistic_read(cf_ctx *c, double *out)
 {
     if (!c || !out) return CF_ERR_ARG;
+    if (int rc = cf_statistic_flush(c)) return rc;
     if (int rc = stat_alloc(c)) return rc;
     const size_t n = (size_t)17 * c->d.Ym;
     if (int rc = cuda_check(c, cudaMemcpyAsync(out, c->stat_acc, n * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1241,12 +1254,11 @@ int cf_statistic_read(cf_ctx *c, double *out)
     return CF_OK;
 }
 
-int cf_Statistic(cf_ctx *c, int, int step, int, int statistic_step, double **p)
+namespace {
+
+// The Statistic's kernels (row sums added to the accumulators) on stream s
+static int stat_launch(cf_ctx *c, double **p, cudaStream_t s)
 {
-    if (!c || !p) return CF_ERR_ARG;
-    if (statistic_step <= 0) return fail(c, CF_ERR_ARG, "Statistic: statistic_step must be positive");
-    for (int i = 0; i < 16; i++)
-        if (!p[i]) return fail(c, CF_ERR_ARG, "Statistic: array argument %d is NULL", i);
     if (int rc = stat_alloc(c)) return rc;
     const cf_dims &d = c->d;
     cf_stat_args a;
@@ -1254,17 +1266,27 @@ int cf_Statistic(cf_ctx *c, int, int step, int, int statistic_step, double **p)
     a.J = R(c, p[5]);
     a.Jv = R(c, p[6]);
     for (int n = 0; n < 9; n++) a.m[n] = R(c, p[7 + n]);
-    const size_t plen = (size_t)4 * 152 * 9 + (size_t)d.Ym * 64;
+    // row partials: up to Y_m rows x (X_out/4 + 1) chunks x 9 sums
+    const size_t plen = (size_t)d.Ym * (size_t)(d.X_out / 4 + 1) * 9;
     double *partial = static_cast<double *>(scratch_bytes(c, "stat_partial", plen * sizeof(double)));
     if (!partial) return fail(c, CF_ERR_NOMEM, "Statistic: scratch allocation failed");
-    cudaError_t e = exact(c) ? cf_exact::statistic(d, a, c->stat_acc, partial, plen, c->stream)
-                             : cf_fast::statistic(d, a, c->stat_acc, partial, plen, c->stream);
-    if (int rc = cuda_check(c, e, "Statistic")) return rc;
+    cudaError_t e = exact(c) ? cf_exact::statistic(d, a, c->stat_acc, partial, plen, s)
+                             : cf_fast::statistic(d, a, c->stat_acc, partial, plen, s);
+    return cuda_check(c, e, "Statistic");
+}
+
+// The Statistic's host part after its kernels on stream s (Statistic.cpp:
+// 900-1068): the accumulators to the host, the wall shear increments to
+// Shear_stress.dat and, when step % statistic_step == 0, ND%05d.dat,
+// st%05d.dat and cleared accumulators
+static int stat_host(cf_ctx *c, int step, int statistic_step, cudaStream_t s)
+{
+    const cf_dims &d = c->d;
     const int Ym = d.Ym, ny = d.ny;
     std::vector<double> h((size_t)17 * Ym);
     if (int rc = cuda_check(c, cudaMemcpyAsync(h.data(), c->stat_acc, h.size() * sizeof(double),
-                                               cudaMemcpyDeviceToHost, c->stream), "Statistic")) return rc;
-    if (int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "Statistic")) return rc;
+                                               cudaMemcpyDeviceToHost, s), "Statistic")) return rc;
+    if (int rc = cuda_check(c, cudaStreamSynchronize(s), "Statistic")) return rc;
     const double XZ = (double)d.X_out, ZZ = (double)d.Z_out;
     // wall shear-stress increments (Statistic.cpp:900-920)
     const double s1 = h[(size_t)7 * Ym + 1] / XZ / ZZ, sn = h[(size_t)7 * Ym + ny] / XZ / ZZ;
@@ -1292,10 +1314,72 @@ int cf_Statistic(cf_ctx *c, int, int step, int, int statistic_step, double **p)
             for (int j = 2; j <= ny; j++) std::fprintf(f, "%.16f\n", h[(size_t)r * Ym + j] * inv);
         std::fclose(f);
         c->sxy_bottom = c->sxy_up = 0;
-        if (int rc = cuda_check(c, cudaMemsetAsync(c->stat_acc, 0, h.size() * sizeof(double), c->stream),
-                                "Statistic")) return rc;
+        if (int rc = cuda_check(c, cudaMemsetAsync(c->stat_acc, 0, h.size() * sizeof(double), s), "Statistic"))
+            return rc;
+        if (int rc = cuda_check(c, cudaStreamSynchronize(s), "Statistic")) return rc;
     }
     return CF_OK;
+}
+
+}  // namespace
+
+// completes the pending Statistic of the last cf_step (its host part)
+int cf_statistic_flush(cf_ctx *c)
+{
+    if (!c) return CF_ERR_ARG;
+    if (!c->stat_pending) return CF_OK;
+    c->stat_pending = false;
+    return stat_host(c, c->stat_step, c->stat_every, c->stat_stream);
+}
+
+namespace {
+
+// cf_step's Statistic of the final U_: the pending one completed, U_ copied
+// (ghosts included) on the step's stream, the kernels on the Statistic's
+// stream after that copy; the host part waits for the next flush
+static int stat_overlapped(cf_ctx *c, int step, int statistic_step, double **st)
+{
+    if (int rc = cf_statistic_flush(c)) return rc;
+    if (!c->stat_stream) {
+        // the least priority: a caller that runs its steps on a stream of
+        // higher priority keeps the block scheduler's preference
+        int least = 0, greatest = 0;
+        if (int rc = cuda_check(c, cudaDeviceGetStreamPriorityRange(&least, &greatest), "cf_step stream")) return rc;
+        if (int rc = cuda_check(c, cudaStreamCreateWithPriority(&c->stat_stream, cudaStreamNonBlocking, least),
+                                "cf_step stream")) return rc;
+        if (int rc = cuda_check(c, cudaEventCreateWithFlags(&c->ev_stat, cudaEventDisableTiming), "cf_step event"))
+            return rc;
+    }
+    const size_t n = c->d.total();
+    double *snap = scratch(c, "stat_state", 5);
+    if (!snap) return fail(c, CF_ERR_NOMEM, "cf_step: Statistic state copy allocation failed");
+    double *p[16];
+    for (int v = 0; v < 5; v++) {
+        if (int rc = cuda_check(c, cudaMemcpyAsync(snap + v * n, R(c, st[v]), n * sizeof(double),
+                                                   cudaMemcpyDeviceToDevice, c->stream), "cf_step")) return rc;
+        p[v] = snap + v * n;
+    }
+    for (int v = 5; v < 16; v++) p[v] = st[v];
+    if (int rc = cuda_check(c, cudaEventRecord(c->ev_stat, c->stream), "cf_step")) return rc;
+    if (int rc = cuda_check(c, cudaStreamWaitEvent(c->stat_stream, c->ev_stat, 0), "cf_step")) return rc;
+    if (int rc = stat_launch(c, p, c->stat_stream)) return rc;
+    c->stat_pending = true;
+    c->stat_step = step;
+    c->stat_every = statistic_step;
+    return CF_OK;
+}
+
+}  // namespace
+
+int cf_Statistic(cf_ctx *c, int, int step, int, int statistic_step, double **p)
+{
+    if (!c || !p) return CF_ERR_ARG;
+    if (statistic_step <= 0) return fail(c, CF_ERR_ARG, "Statistic: statistic_step must be positive");
+    for (int i = 0; i < 16; i++)
+        if (!p[i]) return fail(c, CF_ERR_ARG, "Statistic: array argument %d is NULL", i);
+    if (int rc = cf_statistic_flush(c)) return rc;
+    if (int rc = stat_launch(c, p, c->stream)) return rc;
+    return stat_host(c, step, statistic_step, c->stream);
 }
 
 static int restart_args(cf_ctx *c, double *const *U, double *const *Uq, const double *J, cf_ptr5 &u, cf_ptr5 &uq,
@@ -1543,7 +1627,7 @@ int cf_step(cf_ctx *c, const cf_step_params *pp, int step, const cf_fields *f, i
         st[6] = f->face_J[1];
         for (int n = 0; n < 9; n++) st[7 + n] = f->face_metric[1][n];
         st[26] = f->Ep[1];
-        if (int rc = cf_Statistic(c, 0, step, it, pp->statistic_step, st)) return rc;
+        if (int rc = stat_overlapped(c, step, pp->statistic_step, st)) return rc;
     }
     cf_ptr5 u_, u, uq;
     for (int n = 0; n < 5; n++) {

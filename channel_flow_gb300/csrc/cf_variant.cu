@@ -341,7 +341,9 @@ static cudaError_t stat_kind(const cf_dims &d, const cf_stat_args &a, double *pa
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 132;
     }
-    int nchunk = std::max(1, std::min(d.X_out, (4 * sms + nrows - 1) / nrows));
+    // chunks of about four x planes (short blocks, which share the SMs
+    // well with kernels of other streams), at least four blocks per SM
+    int nchunk = std::max(1, std::min(d.X_out, std::max((4 * sms + nrows - 1) / nrows, (d.X_out + 3) / 4)));
     while ((size_t)nrows * nchunk * NQ > partial_len && nchunk > 1) nchunk--;
     if ((size_t)nrows * nchunk * NQ > partial_len) return cudaErrorInvalidValue;
     k_stat_rows<KIND><<<dim3((unsigned)nrows, (unsigned)nchunk), ST_THREADS, 0, s>>>(d, a, partial, nchunk, jsum);

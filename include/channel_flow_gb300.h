@@ -322,6 +322,12 @@ int cf_Statistic(cf_ctx *ctx, int myid, int step, int iteration, int statistic_s
  * SXY_up: 17*Y_m + 2 values */
 int cf_statistic_read(cf_ctx *ctx, double *out);
 int cf_statistic_reset(cf_ctx *ctx);
+/* Completes the Statistic that the last cf_step left running (its
+ * accumulators to the host, the Shear_stress.dat line, at the output steps
+ * ND/st files and cleared accumulators); nothing when none is pending.
+ * cf_step, cf_Statistic, cf_statistic_read, cf_statistic_reset and
+ * cf_destroy call it first. */
+int cf_statistic_flush(cf_ctx *ctx);
 
 /* Output.cpp:14 / Initial_condition.cpp:10: the restart image LES%05d.bin
  * (ten float64 blocks [X_out][Y_out][Z_out] of U1..U5, U1q..U5q times J)
@@ -363,7 +369,7 @@ typedef struct {
                                   (the sensor then stays fixed while the sub-iterations converge),
                                   0: no Filter (Ep as given) */
     double roe_criterion, e_high, e_low;
-    int statistic_step;        /* > 0: Statistic after the step */
+    int statistic_step;        /* > 0: Statistic after the step (its host part deferred, see cf_step) */
     int static_metrics;        /* 1: the metric arrays (J, cell and face metrics) stay unchanged between
                                   cf_step calls, so the FP32 path converts them to FP32 once and keeps
                                   the copies (cf_step_reset drops them) */
@@ -374,7 +380,12 @@ typedef struct {
  * Dual_time_stepping until the normalised residuals of fields 1-4 drop
  * below the tolerance (the maxima persist across steps, main.cpp:63, 387)
  * or max_iterations; then Driven_force (Q), Statistic when
- * statistic_step > 0, and Uq <- U, U <- U_.  Returns the iteration count,
+ * statistic_step > 0, and Uq <- U, U <- U_.  The Statistic adds the rows of
+ * a copy of the final U_ on a stream of its own, beside whatever the caller
+ * enqueues next; its host part (the Shear_stress.dat line, the ND/st files
+ * at the output steps) follows at the next cf_statistic_flush, which the
+ * next cf_step, cf_Statistic, cf_statistic_read/reset and cf_destroy make
+ * first.  Returns the iteration count,
  * the last normalised er1..er5 and Q (pointers may be NULL).  In
  * CF_PREC_FP32 the loop's intermediate arrays (inF, vF, LL, ML, MR, NR, NL)
  * are its scratch and hold FP32 values in their FP64 allocation afterwards.

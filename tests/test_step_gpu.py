@@ -170,3 +170,45 @@ def test_gpu_fp32_static_metrics_first_step_after_poisoned_memory(cuda_lib):
         del w, f
         torch.cuda.empty_cache()
     np.testing.assert_allclose(ers[True], ers[False], rtol=1e-3, atol=0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gpu_step_statistic_beside_next_step(precision, cuda_lib, tmp_path):
+    """cf_step's Statistic adds the rows of a copy of the final U_ on a
+    stream of its own, beside the next call's work, and its host part waits
+    for the next flush.  Three steps with statistic_step 2 (step 2 writes the
+    ND/st files and clears the accumulators) give the same files and
+    accumulators, bit for bit, as the same steps without the Statistic
+    followed each by the drop-in cf_Statistic on U_."""
+    import channel_flow_gb300 as cf
+    import torch
+    g = cases.grid((13, 9, 17))
+    f = cases.step_case(g, seed=5)
+    a, b = _to_dev(f), _to_dev(f)
+    da, db = tmp_path / "a", tmp_path / "b"
+    da.mkdir()
+    db.mkdir()
+    ctx_a = cf.Context(g, precision=precision)
+    ctx_b = cf.Context(g, precision=precision)
+    try:
+        ctx_a.set_output_dir(str(da))
+        ctx_b.set_output_dir(str(db))
+        scratch = [torch.zeros_like(b["J"]) for _ in range(10)]
+        for step in (1, 2, 3):
+            ctx_a.step(a, step=step, max_iterations=2, tolerance=1e-3, statistic_step=2)
+            ctx_b.step(b, step=step, max_iterations=2, tolerance=1e-3, statistic_step=0)
+            ctx_b.Statistic(step, 0, 2, *b["U_"], b["J"], b["face_J"][1], *b["face_metric"][1], *scratch,
+                            b["Ep"][1])
+        got = ctx_a.statistic_read()          # flushes step 3's host part first
+        want = ctx_b.statistic_read()
+        assert np.array_equal(got, want)
+        assert np.any(got[:17 * (g.Y_out + 4)])   # step 3 accumulated after the clearing at step 2
+        for name in ("Shear_stress.dat", "ND00002.dat", "st00002.dat"):
+            assert (da / name).read_bytes() == (db / name).read_bytes(), name
+        assert len((da / "Shear_stress.dat").read_text().splitlines()) == 3
+        for key in ("U_", "U", "Uq"):
+            for n in range(5):
+                assert torch.equal(a[key][n], b[key][n]), (key, n)
+    finally:
+        ctx_a.close()
+        ctx_b.close()
