@@ -21,9 +21,9 @@
 //   earlier in the same call, so nothing needs clearing, but calls that
 //   overlap on the GPU (different streams or host threads at the same time)
 //   race on it and must not be issued;
-// * the device address of the scratch is looked up once per device, on the
-//   first call made with that device current; make that first call before
-//   any stream capture begins;
+// * the device address of the scratch is looked up once per device
+//   (cudaGetSymbolAddress), on the first call made with that device
+//   current;
 // * the call ends by copying the five norms to the caller's host doubles and
 //   synchronising the stream.
 #include <cuda_runtime.h>

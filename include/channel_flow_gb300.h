@@ -251,8 +251,8 @@ int cf_DPLUSGS(cf_ctx *ctx, int myid, double deltaT, double *er1, double *er2, d
  * GPU, so grids needing more than 262144 reduction blocks
  * (ceil(cells_z/32) * ceil(cells_y/8) * cells_x) are rejected with CF_ERR_ARG.
  * All calls share that array: calls overlapping on the GPU race.  The first
- * call on a device looks the array's address up; make it before any stream
- * capture.  er1..er5 are host pointers; the call synchronises the stream. */
+ * call on a device looks the array's address up (cudaGetSymbolAddress).
+ * er1..er5 are host pointers; the call synchronises the stream. */
 int cf_DPLUSGS_noalloc(const cf_grid *g, void *cuda_stream, double deltaT, double *er1, double *er2,
                        double *er3, double *er4, double *er5, double **arrays64);
 
