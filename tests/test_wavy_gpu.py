@@ -175,3 +175,45 @@ def test_wavy_channel_steps(cuda_lib):
     for v in range(5):
         a, b = finals["fp32"][v], finals["fp64"][v]
         assert float((a - b).abs().max()) <= 1e-2 * float((b - start[v]).abs().max()), v
+
+
+@pytest.mark.gpu
+def test_wavy_channel_exact_equals_oracle(cuda_lib, port):
+    """The configuration schedule's physics on a wavy lower wall (0.05 h,
+    wavelength pi h, metrics of the numpy restatement): limited MUSCL-5 +
+    Roe with the consistent face-state scaling, the Filter at every
+    sub-iteration, 10 fixed sub-iterations per step, Mach 0.5, Re_b 11000,
+    dt = 0.005/8 h/U_b.  After each of four steps the no-FMA GPU state (U_,
+    U, Uq) equals the C oracle's bit for bit on the same inputs."""
+    import torch
+    import cases
+    import channel_flow_gb300 as cf
+    from channel_flow_gb300 import synthetic as syn
+    g = syn.channel_physics(syn.channel_grid(24, 16, 20), 0.5, 11000.0)
+    h = 0.5 * g.high
+    A, lam, gam = 0.05 * h, math.pi * h, 2.0
+    met = {w: mo.metrics(g.shape, g.deltaXI, g.deltaET, g.high, A, lam, gam, True, w) for w in ("cell", "u", "v", "w")}
+    J = met["cell"][0]
+    U = syn.channel_state(g, J, seed=0, mach=0.5, noise=0.05, jitter=0.01, gamma=gam, wall_damped=True)
+    z = lambda: np.zeros(g.shape)
+    f = {"U_": [u.copy() for u in U], "U": [u.copy() for u in U], "Uq": [u.copy() for u in U], "J": J,
+         "Y_point": mo.y_point(g.shape, g.deltaXI, g.deltaET, g.high, A, lam, gam), "cell_metric": met["cell"][1:],
+         "face_J": [met[w][0] for w in ("u", "v", "w")], "face_metric": [met[w][1:] for w in ("u", "v", "w")],
+         "Ep": [z() for _ in range(3)], "inF": [[z() for _ in range(5)] for _ in range(3)],
+         "vF": [z() for _ in range(4)], "LL": [z() for _ in range(4)], "ML": [z() for _ in range(4)],
+         "MR": [z() for _ in range(5)], "NR": [z() for _ in range(5)], "NL": [z() for _ in range(5)],
+         "Residual": [z() for _ in range(5)]}
+    dev = {k: ([[torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in w] if isinstance(w, list)
+                 else torch.from_numpy(np.ascontiguousarray(w)).cuda() for w in v] if isinstance(v, list)
+               else torch.from_numpy(np.ascontiguousarray(v)).cuda()) for k, v in f.items()}
+    dt = syn.time_step(g, 0.5) / 8
+    ctx = cf.Context(g, precision="fp64_exact", gamma=gam, scheme="consistent")
+    E = [0.0] * 5
+    try:
+        for s in range(1, 5):
+            ctx.step(dev, step=s, deltaT=dt, max_iterations=10, tolerance=0.0, limiter=True, filter=True,
+                     statistic_step=0, static_metrics=True)
+            cases.port_step(port, g, f, dt, 10, 0.0, E, scheme="consistent")
+            assert cases.state_digest(dev, lambda t: t.cpu().numpy()) == cases.state_digest(f), s
+    finally:
+        ctx.close()
