@@ -664,8 +664,11 @@ def physical_steps(torch, g, precision, steps, warmup):
     1e-6 from the extrapolated start, Statistic every step) of the
     configuration 2/3 physics on grid g: CUDA event time per step and per
     sub-iteration.  The timed steps are bracketed by cudaProfilerStart/Stop."""
+    import tempfile
     from channel_flow_gb300 import stepper
     g, ctx, w, dt = northstar_case(torch, (g.X_out, g.Y_out, g.Z_out), precision)
+    tmp = tempfile.TemporaryDirectory()       # the Statistic's Shear_stress.dat
+    ctx.set_output_dir(tmp.name)
     st = stepper.Stepper(ctx, stepper.fields_from_workload(w, torch, g), deltaT=dt, **NS_STEP)
     st.kw["statistic_step"] = 1 << 30          # Statistic accumulates every step, as in the comparison
     for n in range(max(warmup, 3)):
@@ -688,6 +691,7 @@ def physical_steps(torch, g, precision, steps, warmup):
     torch.cuda.cudart().cudaProfilerStop()
     total = e0.elapsed_time(e1)
     ctx.close()
+    tmp.cleanup()
     return {"step": "physical", "grid": [g.X_out, g.Y_out, g.Z_out], "precision": precision,
             "subiterations": its, "ms_total": total, "ms_per_step": total / max(1, steps),
             "ms_per_subiteration": total / max(1, sum(its))}
