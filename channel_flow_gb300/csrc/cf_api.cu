@@ -1227,7 +1227,9 @@ static int stat_alloc(cf_ctx *c)
         c->stat_acc = nullptr;
         return fail(c, CF_ERR_NOMEM, "Statistic: accumulator allocation failed");
     }
-    return cuda_check(c, cudaMemset(c->stat_acc, 0, n * sizeof(double)), "Statistic");
+    // cleared on the context's stream: whatever reads the accumulators
+    // next is ordered after it (cf_step's Statistic stream by its event)
+    return cuda_check(c, cudaMemsetAsync(c->stat_acc, 0, n * sizeof(double), c->stream), "Statistic");
 }
 
 int cf_statistic_reset(cf_ctx *c)
@@ -1350,6 +1352,7 @@ static int stat_overlapped(cf_ctx *c, int step, int statistic_step, double **st)
         if (int rc = cuda_check(c, cudaEventCreateWithFlags(&c->ev_stat, cudaEventDisableTiming), "cf_step event"))
             return rc;
     }
+    if (int rc = stat_alloc(c)) return rc;                 // before the event the kernels wait on
     const size_t n = c->d.total();
     double *snap = scratch(c, "stat_state", 5);
     if (!snap) return fail(c, CF_ERR_NOMEM, "cf_step: Statistic state copy allocation failed");
