@@ -461,12 +461,8 @@ def main():
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         total_ms, per_routine = timed_steps(ctx, calls, args.steps, stream, torch)
-    if dist:
-        t = torch.tensor([total_ms])
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = replica_value(torch, dist, total_ms, g.cells, args.steps, world)
     ms_per_step = total_ms / args.steps
-    value = g.cells * args.steps * world / (total_ms * 1e-3) / 1e6
 
     # roofline of the dominant single kernel (the slowest limited flux) with
     # the byte model; traffic = ncu DRAM bytes per cell x cells
@@ -650,6 +646,17 @@ def northstar_case(torch, dims, precision):
     ctx = new_context(cf, g, precision=precision, gamma=GAMMA, scheme="consistent")
     w = DeviceWorkload(ctx, g, host, torch)
     return g, ctx, w, syn.time_step(g, NS_MACH) * NS_DT_FACTOR
+
+
+def replica_value(torch, dist, total_ms, cells, steps, world):
+    """Whole-job throughput of `world` independent replicas: the slowest
+    rank's time (max over ranks when a process group is given) and
+    cells x steps x world cell updates in that time, in Mcell-updates/s."""
+    if dist is not None:
+        t = torch.tensor([float(total_ms)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, cells * steps * world / (total_ms * 1e-3) / 1e6
 
 
 def solver_stream(torch):
