@@ -72,7 +72,11 @@ __device__ __forceinline__ T met_ld(const double *p, const float *p32, size_t q)
 // x <- x + x (1 - d x), each doubling the correct bits, so the result lies
 // within about one unit in the last place of the rounded quotient, in fewer
 // FP64-pipe operations than an IEEE-rounded division.  d = 0 gives NaN
-// (callers guard ties).  FP32: the approximate division of the FP32 build.
+// (callers guard ties), and so does a subnormal d (|d| < 2.2e-308, flushed
+// to zero on input); a quotient below the normal range (|d| > 4.5e307)
+// flushes to zero.  The solver's divisors (densities, Jacobians, metric
+// norms, sound speeds) lie far inside these limits.  FP32: the approximate
+// division of the FP32 build.
 template <typename T>
 __device__ __forceinline__ T frcp(T d);
 template <>
